@@ -1,0 +1,231 @@
+/*
+ * stencil_cuda.h — C ABI of libstencilcuda.so, the GB300 (sm_103a) implementation of
+ * Stencils.jl's `mapstencil` / `mapstencil!` hot path.
+ *
+ * Every entry point takes plain pointers and sizes.  Grids are column-major (axis 0 is the
+ * contiguous one, exactly as a Julia `Array`), live in caller-owned device memory, and are
+ * described by `stc_grid`.  The library never frees caller memory.  Calls are ordered on the
+ * CUDA stream passed as `void* stream` (a `cudaStream_t`; NULL is the legacy default stream).
+ * Every call returns STC_OK (0) or a negative `stc_status`; `stc_strerror` names it.  The
+ * statuses mirror the `ArgumentError`s the reference raises, so a Julia shim can rethrow them.
+ *
+ * Reference interfaces replaced (Stencils.jl v0.3.6, paths within the package):
+ *   stc_map               gatherstencil!(f, dest, source::AbstractStencilArray)   src/gatherstencil.jl:89-103
+ *                         (and gatherstencil(f, source), which allocates dest,   src/gatherstencil.jl:14-39)
+ *   stc_map_steps         repeated  A = gatherstencil!(f, A::SwitchingStencilArray) src/gatherstencil.jl:77-83
+ *                         with switch(A)                                        src/array.jl:610-611
+ *   stc_update_boundary   update_boundary!(A::AbstractStencilArray)              src/array.jl:195-233
+ *   stc_mass              no counterpart: FP64 compensated total of a grid, used to report the mass
+ *                         drift of long multi-step runs.
+ *   stc_batch_*           no counterpart: many independent `mapstencil!` loops run as one
+ *                         CUDA-graph-captured persistent launch.
+ *   stc_server_*          no counterpart: a continuous-batching request loop over stc_batch.
+ * `mapstencil` / `mapstencil!` are the deprecated aliases of the above (src/gatherstencil.jl:127-128).
+ */
+#ifndef STENCIL_CUDA_H
+#define STENCIL_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define STC_API __attribute__((visibility("default")))
+#else
+#define STC_API
+#endif
+
+#define STC_ABI_VERSION 1
+
+/* ---- status codes (the reference's ArgumentError sites in comments) ---- */
+typedef enum {
+    STC_OK = 0,
+    STC_ERR_SIZE_MISMATCH = -1,   /* "Source array sizes must match"  src/gatherstencil.jl:121 */
+    STC_ERR_RADIUS = -2,          /* "stencil radius is larger than array axis"  src/array.jl:452, :578 */
+    STC_ERR_KERNEL_LENGTH = -3,   /* "Stencil length .. does not match kernel length"  src/stencils/kernel.jl:342 */
+    STC_ERR_UNSUPPORTED = -4,     /* shape / op / dtype / boundary combination not registered (a MethodError
+                                     in the reference, e.g. Use with Conditional padding has no getneighbor) */
+    STC_ERR_INVALID = -5,         /* malformed descriptor (null pointer, bad ndims, stride[0] != 1, ...) */
+    STC_ERR_CUDA = -6,            /* a CUDA runtime call failed */
+    STC_ERR_TIMEOUT = -7,         /* a bounded device-side wait ran out; the kernel returned early */
+    STC_ERR_NO_DEVICE = -8,       /* no usable sm_100-family GPU */
+    STC_ERR_BUDGET = -9,          /* request exceeds the server's HBM budget */
+    STC_ERR_BUSY = -10,           /* result not ready / queue full */
+    STC_ERR_CANCELLED = -11       /* job was cancelled before it finished */
+} stc_status;
+
+/* ---- element types ---- */
+typedef enum {
+    STC_F64 = 0, STC_F32 = 1, STC_BF16 = 2, STC_F16 = 3,
+    STC_U8 = 4, STC_BOOL = 5, STC_I32 = 6, STC_I64 = 7
+} stc_dtype;
+
+/* ---- registered reductions `f` (the reference takes any Julia function) ----
+ * MEAN     Statistics.mean(hood): left fold of `+` over the neighbours in offset order, / L
+ * SUM      sum(hood): the same left fold
+ * KDOT     kernelproduct(hood): s = 0; s += hood[i] * kernel[i] for i in 1:L   src/stencils/kernel.jl:264-270
+ * MIN/MAX  minimum/maximum(hood): left fold of Julia's min/max (NaN-propagating, -0.0 < +0.0)
+ * LIFE     outer-totalistic cellular automaton: n = count of nonzero neighbours, c = centre != 0,
+ *          result = c ? (survive_mask >> n) & 1 : (birth_mask >> n) & 1   (B3/S23: birth 1<<3,
+ *          survive 1<<2 | 1<<3).  Equals the closure `s == 3 || (c && s == 2)` on 0/1 states.
+ * DIFFUSE  c + alpha * (sum(hood) - L * c): explicit diffusion step, c = centre value.
+ */
+typedef enum {
+    STC_OP_MEAN = 0, STC_OP_SUM = 1, STC_OP_KDOT = 2, STC_OP_MIN = 3, STC_OP_MAX = 4,
+    STC_OP_LIFE = 5, STC_OP_DIFFUSE = 6
+} stc_opcode;
+
+/* ---- boundary conditions (src/boundary.jl:17-52) and padding (src/padding.jl:28-39) ---- */
+typedef enum { STC_REMOVE = 0, STC_WRAP = 1, STC_REFLECT = 2, STC_USE = 3 } stc_boundary;
+typedef enum { STC_CONDITIONAL = 0, STC_HALO_IN = 1, STC_HALO_OUT = 2 } stc_padding;
+
+/* ---- stencil shapes with specialised kernels; anything else runs from the offset table ---- */
+typedef enum {
+    STC_SHAPE_TABLE = 0,       /* arbitrary offsets (Positional, Rectangle, NamedStencil, Annulus, ...) */
+    STC_SHAPE_WINDOW = 1, STC_SHAPE_MOORE = 2, STC_SHAPE_VONNEUMANN = 3,
+    STC_SHAPE_CIRCLE = 4, STC_SHAPE_CROSS = 5
+} stc_shape;
+
+/* A grid: the PARENT array as Julia holds it (for Halo padding this includes the ring of width R).
+ * size[d] / stride[d] in elements for d < ndims; stride[0] must be 1. */
+typedef struct {
+    int32_t ndims;          /* 1..3 */
+    int32_t dtype;          /* stc_dtype */
+    int64_t size[3];
+    int64_t stride[3];
+    void*   data;           /* device pointer */
+} stc_grid;
+
+/* A stencil: the compile-time offsets Stencils.jl generates, lowered to a table.
+ * offsets[k*ndims + d] is component d of offset k (component 0 along the contiguous axis), in
+ * the reference's offset order (src/stencil.jl:224).  A stencil with fewer dims than the grid keeps
+ * the trailing indices fixed (src/stencil.jl:220-223). */
+typedef struct {
+    int32_t ndims;            /* stencil dims, <= grid ndims */
+    int32_t len;              /* L, 1..STC_MAX_LEN */
+    int32_t radius;           /* R: the halo width and the radius < axis check (src/array.jl:451-453) */
+    int32_t shape;            /* stc_shape; a specialised kernel is used only if the table matches it */
+    const int32_t* offsets;   /* host pointer, len*ndims */
+    const double*  weights;   /* host pointer, len; KDOT only (else NULL) */
+    int32_t weight_dtype;     /* STC_F64 or STC_F32: type of kernel[i] (products are promote(T, W)) */
+    int32_t reserved;
+} stc_stencil;
+
+#define STC_MAX_LEN 1024
+#define STC_MAX_RADIUS 64
+
+typedef struct {
+    int32_t  code;            /* stc_opcode */
+    int32_t  reserved;
+    uint32_t birth_mask;      /* LIFE */
+    uint32_t survive_mask;    /* LIFE */
+    double   alpha;           /* DIFFUSE */
+} stc_op;
+
+typedef struct {
+    int32_t boundary;         /* stc_boundary */
+    int32_t padding;          /* stc_padding */
+    double  padval;           /* Remove(padval) for float grids */
+    int64_t padval_int;       /* Remove(padval) for integer / Bool grids */
+} stc_bc;
+
+/* stc_map flags */
+#define STC_ASYNC 1u          /* do not synchronise the stream before returning (errors from the
+                                 kernel's own checks surface at the next synchronising call) */
+
+/* ---- library ---- */
+STC_API int         stc_abi_version(void);
+STC_API const char* stc_strerror(int status);
+STC_API int         stc_last_cuda_error(void);              /* the cudaError_t behind the last STC_ERR_CUDA */
+
+/* Output element type the reference would infer for (op, source dtype, weight dtype)
+ * (Base._return_type, src/gatherstencil.jl:41-56), or a negative status. */
+STC_API int stc_result_dtype(int32_t opcode, int32_t src_dtype, int32_t weight_dtype);
+
+/* One map: dst[I] = f(stencil(src, I)) for every logical index I.  `src` is the parent array;
+ * its logical size is size - 2R per axis for Halo padding.  `dst` is either the logical size
+ * (a plain array) or, with dst_padded != 0, a parent of the same padded size whose interior is
+ * written (the SwitchingStencilArray case, src/gatherstencil.jl:77-81).  For Halo padding the
+ * halo ring of src is refreshed first, as update_boundary! does. */
+STC_API int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded,
+            const stc_stencil* stencil, const stc_op* op, const stc_bc* bc,
+            void* stream, uint32_t flags);
+
+/* nsteps of `A = mapstencil!(f, A)` on a SwitchingStencilArray whose two parents are a and b,
+ * a holding the current source.  On return *out_src_is_b says which parent holds the result
+ * (the reference's switch()).  Multi-step runs of registered shapes are temporally blocked. */
+STC_API int stc_map_steps(const stc_grid* a, const stc_grid* b,
+                  const stc_stencil* stencil, const stc_op* op, const stc_bc* bc,
+                  int64_t nsteps, int32_t* out_src_is_b, void* stream, uint32_t flags);
+
+/* update_boundary!: write the halo ring of a Halo-padded parent from its interior. */
+STC_API int stc_update_boundary(const stc_grid* parent, int32_t radius, const stc_bc* bc,
+                        void* stream, uint32_t flags);
+
+/* FP64 total of the logical grid (Neumaier-compensated; radius/bc.padding locate the interior). */
+STC_API int stc_mass(const stc_grid* g, int32_t radius, const stc_bc* bc, double* out_total, void* stream);
+
+/* ---- tracing: per-launch device time from CUDA events on the launching stream ---- */
+/* Enable (1) or disable (0) recording; enabling clears earlier records.  No counterpart in the
+ * reference (which has only @time / BenchmarkTools around calls). */
+STC_API int stc_profile_enable(int32_t on);
+/* JSON object {kernel: {"launches", "ms", "alg_bytes", "updates"}} of everything recorded since
+ * enabling; synchronises on the recorded events.  Returns STC_OK, or the buffer size needed (> 0)
+ * when `len` is too small. */
+STC_API int stc_profile_report(char* buf, size_t len);
+
+/* ---- batched runs: many independent SwitchingStencilArray loops in one launch ---- */
+typedef struct stc_batch stc_batch;
+
+STC_API int stc_batch_create(stc_batch** out);
+STC_API int stc_batch_destroy(stc_batch* b);
+/* Add job: nsteps of stencil/op/bc on grids a (source) and b (scratch).  Returns the job index. */
+STC_API int stc_batch_add(stc_batch* b, const stc_grid* a, const stc_grid* bgrid,
+                  const stc_stencil* stencil, const stc_op* op, const stc_bc* bc, int64_t nsteps);
+/* Choose tile shapes and temporal depth per job (autotune != 0 times candidates on the GPU and
+ * caches the winners per (shape, dtype, size class)), build the work list and capture the graph. */
+STC_API int stc_batch_plan(stc_batch* b, int32_t autotune, void* stream);
+/* Run every job to completion: one graph launch. */
+STC_API int stc_batch_run(stc_batch* b, void* stream, uint32_t flags);
+/* After run: which parent holds job `idx`'s result. */
+STC_API int stc_batch_result(const stc_batch* b, int32_t idx, int32_t* out_src_is_b);
+/* Plain reference path for comparison: each job as its own stc_map_steps call. */
+STC_API int stc_batch_run_sequential(stc_batch* b, void* stream);
+
+/* ---- serving: continuous batching of stencil jobs with device-resident state ---- */
+typedef struct stc_server stc_server;
+
+typedef struct {
+    stc_grid    grid;         /* host-side description: data points to HOST memory holding the input */
+    stc_stencil stencil;
+    stc_op      op;
+    stc_bc      bc;
+    int64_t     nsteps;
+} stc_job;
+
+/* hbm_fraction: admission budget as a fraction of free device memory (e.g. 0.8);
+ * steps_per_tick: most steps any job advances per batched launch (continuous-batching tick). */
+STC_API int stc_server_create(stc_server** out, double hbm_fraction, int32_t steps_per_tick);
+STC_API int stc_server_destroy(stc_server* s);
+/* Queue a job (copied, including its host input).  *out_id identifies it. */
+STC_API int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id);
+/* Non-blocking: 1 if the job finished (its result can be fetched), 0 if not, or a status. */
+STC_API int stc_server_poll(stc_server* s, int64_t id);
+/* Copy a finished job's result into host memory `out` (logical size, the job's dtype, column-major)
+ * and release its device state.  Returns STC_ERR_BUSY if it has not finished. */
+STC_API int stc_server_fetch(stc_server* s, int64_t id, void* out, size_t out_bytes,
+                     double* out_latency_s);
+STC_API int stc_server_cancel(stc_server* s, int64_t id);
+/* Block until every submitted job finished or timeout_s passed (STC_ERR_TIMEOUT). */
+STC_API int stc_server_drain(stc_server* s, double timeout_s);
+/* Counters: jobs admitted, finished, ticks run, peak device bytes held. */
+STC_API int stc_server_stats(const stc_server* s, int64_t* admitted, int64_t* finished,
+                     int64_t* ticks, int64_t* peak_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STENCIL_CUDA_H */

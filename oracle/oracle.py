@@ -1,0 +1,148 @@
+"""ctypes binding of the CPU oracle (oracle/stencil_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, `__graft_entry__.smoke()` and bench.py's
+`cpu_baseline` / `--impl reference` legs, never by the product package.
+
+Arrays are numpy arrays in Julia axis order and column-major memory (`order="F"`); bf16
+arrays are carried as uint16 bit patterns.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libstencil_oracle.so"
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with its Makefile (gcc, OpenMP, no FP contraction)."""
+    if force or not LIB_PATH.exists() or \
+            LIB_PATH.stat().st_mtime < (HERE / "stencil_oracle.c").stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(LIB_PATH))
+        from stencils_gb300 import _abi as A  # noqa: F401  (struct layouts)
+        P = C.POINTER
+        _lib.orc_map.argtypes = [P(A.Grid), P(A.Grid), C.c_int, P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc), C.c_int]
+        _lib.orc_map_steps.argtypes = [P(A.Grid), P(A.Grid), P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc),
+                                       C.c_int64, C.c_int, P(C.c_int)]
+        _lib.orc_update_boundary.argtypes = [P(A.Grid), C.c_int, P(A.BcDesc)]
+        _lib.orc_mass.argtypes = [P(A.Grid), C.c_int, C.c_int]
+        _lib.orc_mass.restype = C.c_double
+        _lib.orc_result_dtype.argtypes = [C.c_int, C.c_int, C.c_int]
+        _lib.orc_max_threads.restype = C.c_int
+        _lib.orc_f32_to_bf16.argtypes = [C.c_float]
+        _lib.orc_f32_to_bf16.restype = C.c_uint16
+    return _lib
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        from stencils_gb300._abi import STATUS_NAMES
+        raise RuntimeError(f"oracle {what} failed: {STATUS_NAMES.get(rc, rc)}")
+
+
+def result_dtype(red, src_code: int, weight_code: int = 0) -> int:
+    rc = lib().orc_result_dtype(red.code, src_code, weight_code)
+    if rc < 0:
+        raise NotImplementedError("unsupported (op, dtype) combination")
+    return rc
+
+
+def f32_to_bf16_bits(x: np.ndarray) -> np.ndarray:
+    """Round float32 to bfloat16 (nearest even), returned as uint16 bits."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    nan = (u & 0x7FFFFFFF) > 0x7F800000
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16).astype(np.uint16)
+    r[nan] = ((u[nan] >> 16) | 0x40).astype(np.uint16)
+    return r.reshape(np.shape(x))
+
+
+def bf16_bits_to_f32(b: np.ndarray) -> np.ndarray:
+    return (np.asarray(b, dtype=np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def alloc(shape, code: int) -> np.ndarray:
+    from stencils_gb300._abi import NP_DTYPE
+    return np.zeros(shape, dtype=NP_DTYPE[code], order="F")
+
+
+def _grid(a: np.ndarray, code: int):
+    from stencils_gb300._abi import grid_from_numpy
+    return grid_from_numpy(a, code)
+
+
+def map(src: np.ndarray, src_code: int, stencil, red, boundary, padding, *,
+        dst_code: int | None = None, dst_padded: bool = False, nthreads: int = 1) -> np.ndarray:
+    """dst = mapstencil(f, StencilArray(src parent, ...)); updates src's halo like the reference."""
+    from stencils_gb300 import _abi as A
+    lst = A.LoweredStencil(stencil)
+    op = A.lower_op(red)
+    bc = A.lower_bc(boundary, padding)
+    if dst_code is None:
+        dst_code = result_dtype(red, src_code, lst.desc.weight_dtype)
+    R = stencil.radius
+    halo = padding.code != 0
+    shape = tuple(s - (2 * R if halo else 0) + (2 * R if (halo and dst_padded) else 0) for s in src.shape)
+    dst = alloc(shape, dst_code)
+    gs, gd = _grid(src, src_code), _grid(dst, dst_code)
+    _check(lib().orc_map(C.byref(gs), C.byref(gd), int(dst_padded), C.byref(lst.desc), C.byref(op),
+                         C.byref(bc), nthreads), "map")
+    return dst
+
+
+def map_into(src: np.ndarray, src_code: int, dst: np.ndarray, dst_code: int, stencil, red, boundary,
+             padding, *, dst_padded: bool = False, nthreads: int = 1):
+    from stencils_gb300 import _abi as A
+    lst = A.LoweredStencil(stencil)
+    op = A.lower_op(red)
+    bc = A.lower_bc(boundary, padding)
+    gs, gd = _grid(src, src_code), _grid(dst, dst_code)
+    _check(lib().orc_map(C.byref(gs), C.byref(gd), int(dst_padded), C.byref(lst.desc), C.byref(op),
+                         C.byref(bc), nthreads), "map")
+
+
+def map_steps(a: np.ndarray, b: np.ndarray, code: int, stencil, red, boundary, padding, nsteps: int,
+              *, nthreads: int = 1) -> bool:
+    """nsteps of A = mapstencil!(f, A) on parents (a, b); returns True if b holds the result."""
+    from stencils_gb300 import _abi as A
+    lst = A.LoweredStencil(stencil)
+    op = A.lower_op(red)
+    bc = A.lower_bc(boundary, padding)
+    ga, gb = _grid(a, code), _grid(b, code)
+    out = C.c_int(0)
+    _check(lib().orc_map_steps(C.byref(ga), C.byref(gb), C.byref(lst.desc), C.byref(op), C.byref(bc),
+                               int(nsteps), nthreads, C.byref(out)), "map_steps")
+    return bool(out.value)
+
+
+def update_boundary(parent: np.ndarray, code: int, radius: int, boundary, padding):
+    from stencils_gb300 import _abi as A
+    bc = A.lower_bc(boundary, padding)
+    g = _grid(parent, code)
+    _check(lib().orc_update_boundary(C.byref(g), radius, C.byref(bc)), "update_boundary")
+
+
+def mass(a: np.ndarray, code: int, radius: int = 0, padding_code: int = 0) -> float:
+    g = _grid(a, code)
+    return float(lib().orc_mass(C.byref(g), radius, padding_code))
+
+
+def default_threads() -> int:
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))

@@ -1,0 +1,27 @@
+"""stencils_gb300 — Stencils.jl's mapstencil hot path on one GB300 (sm_103a).
+
+The host API mirrors Stencils.jl: stencil shapes (Window, Moore, VonNeumann, Circle, Cross,
+Positional, Kernel, ...), boundary conditions (Remove, Wrap, Reflect, Use), padding (Conditional,
+Halo), StencilArray / SwitchingStencilArray, and mapstencil / mapstencil_ (the reference's
+mapstencil!).  The compute path is libstencilcuda.so (include/stencil_cuda.h), hand-written CUDA
+kernels for sm_103a; there is no CPU fallback.
+"""
+from .array import (AbstractStencilArray, StencilArray, SwitchingStencilArray, colmajor_empty, colmajor_like,
+                    colmajor_zeros, switch, to_device, to_host)
+from ._abi import ArgumentError
+from .boundary import Conditional, Halo, Reflect, Remove, Use, Wrap
+from .gather import gatherstencil, gatherstencil_, mapstencil, mapstencil_, mass, update_boundary_
+from .ops import Diffusion, LifeRule, kernelproduct, life, maximum, mean, minimum
+from .ops import sum  # noqa: A004
+from .stencil import (AngledCross, Annulus, BackSlash, Cardinal, Circle, Cross, Diamond, ForwardSlash, Horizontal,
+                      Kernel, Moore, NamedStencil, Ordinal, Positional, Rectangle, Stencil, Vertical, VonNeumann,
+                      Window)
+
+__all__ = [
+    "AbstractStencilArray", "StencilArray", "SwitchingStencilArray", "switch", "colmajor_empty", "colmajor_like",
+    "colmajor_zeros", "to_device", "to_host", "ArgumentError", "Conditional", "Halo", "Reflect", "Remove", "Use",
+    "Wrap", "gatherstencil", "gatherstencil_", "mapstencil", "mapstencil_", "mass", "update_boundary_",
+    "Diffusion", "LifeRule", "kernelproduct", "life", "maximum", "mean", "minimum", "sum", "AngledCross",
+    "Annulus", "BackSlash", "Cardinal", "Circle", "Cross", "Diamond", "ForwardSlash", "Horizontal", "Kernel",
+    "Moore", "NamedStencil", "Ordinal", "Positional", "Rectangle", "Stencil", "Vertical", "VonNeumann", "Window",
+]

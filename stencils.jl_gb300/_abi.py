@@ -1,0 +1,168 @@
+"""ctypes mirror of include/stencil_cuda.h: the descriptor structs and enum values.
+
+Nothing here touches a GPU; it only lowers host objects (stencils, reductions, boundary flags,
+array geometry) into the plain structs the C ABI takes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+STC_OK = 0
+
+
+class ArgumentError(ValueError):
+    """The reference's ArgumentError: mismatched sizes, radius >= axis, kernel length."""
+
+STATUS_NAMES = {
+    0: "STC_OK", -1: "STC_ERR_SIZE_MISMATCH", -2: "STC_ERR_RADIUS", -3: "STC_ERR_KERNEL_LENGTH",
+    -4: "STC_ERR_UNSUPPORTED", -5: "STC_ERR_INVALID", -6: "STC_ERR_CUDA", -7: "STC_ERR_TIMEOUT",
+    -8: "STC_ERR_NO_DEVICE", -9: "STC_ERR_BUDGET", -10: "STC_ERR_BUSY", -11: "STC_ERR_CANCELLED",
+}
+STC_ERR_BUSY = -10
+STC_ASYNC = 1
+
+F64, F32, BF16, F16, U8, BOOL, I32, I64 = range(8)
+DTYPE_SIZE = {F64: 8, F32: 4, BF16: 2, F16: 2, U8: 1, BOOL: 1, I32: 4, I64: 8}
+FLOAT_DTYPES = (F64, F32, BF16, F16)
+DTYPE_NAMES = {F64: "f64", F32: "f32", BF16: "bf16", F16: "f16", U8: "u8", BOOL: "bool",
+               I32: "i32", I64: "i64"}
+
+# numpy views of each element type (bf16 is carried as raw uint16 bits on the host)
+NP_DTYPE = {F64: np.float64, F32: np.float32, BF16: np.uint16, F16: np.float16, U8: np.uint8,
+            BOOL: np.uint8, I32: np.int32, I64: np.int64}
+
+
+def torch_dtype_code(dt) -> int:
+    import torch
+    table = {torch.float64: F64, torch.float32: F32, torch.bfloat16: BF16, torch.float16: F16,
+             torch.uint8: U8, torch.bool: BOOL, torch.int32: I32, torch.int64: I64}
+    if dt not in table:
+        raise TypeError(f"unsupported element type {dt}")
+    return table[dt]
+
+
+def torch_dtype(code: int):
+    import torch
+    return {F64: torch.float64, F32: torch.float32, BF16: torch.bfloat16, F16: torch.float16,
+            U8: torch.uint8, BOOL: torch.bool, I32: torch.int32, I64: torch.int64}[code]
+
+
+def numpy_dtype_code(dt) -> int:
+    dt = np.dtype(dt)
+    table = {np.dtype(np.float64): F64, np.dtype(np.float32): F32, np.dtype(np.float16): F16,
+             np.dtype(np.uint8): U8, np.dtype(np.bool_): BOOL, np.dtype(np.int32): I32,
+             np.dtype(np.int64): I64}
+    if dt not in table:
+        raise TypeError(f"unsupported element type {dt}")
+    return table[dt]
+
+
+class Grid(C.Structure):
+    _fields_ = [("ndims", C.c_int32), ("dtype", C.c_int32), ("size", C.c_int64 * 3),
+                ("stride", C.c_int64 * 3), ("data", C.c_void_p)]
+
+
+class StencilDesc(C.Structure):
+    _fields_ = [("ndims", C.c_int32), ("len", C.c_int32), ("radius", C.c_int32), ("shape", C.c_int32),
+                ("offsets", C.POINTER(C.c_int32)), ("weights", C.POINTER(C.c_double)),
+                ("weight_dtype", C.c_int32), ("reserved", C.c_int32)]
+
+
+class OpDesc(C.Structure):
+    _fields_ = [("code", C.c_int32), ("reserved", C.c_int32), ("birth_mask", C.c_uint32),
+                ("survive_mask", C.c_uint32), ("alpha", C.c_double)]
+
+
+class BcDesc(C.Structure):
+    _fields_ = [("boundary", C.c_int32), ("padding", C.c_int32), ("padval", C.c_double),
+                ("padval_int", C.c_int64)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("grid", Grid), ("stencil", StencilDesc), ("op", OpDesc), ("bc", BcDesc),
+                ("nsteps", C.c_int64)]
+
+
+def make_grid(ndims, dtype, size, stride, ptr) -> Grid:
+    g = Grid()
+    g.ndims = ndims
+    g.dtype = dtype
+    for d in range(3):
+        g.size[d] = int(size[d]) if d < ndims else 1
+        g.stride[d] = int(stride[d]) if d < ndims else 0
+    g.data = C.c_void_p(int(ptr))
+    return g
+
+
+def grid_from_torch(t) -> Grid:
+    if t.dim() < 1 or t.dim() > 3:
+        raise ValueError("grids have 1 to 3 dimensions")
+    if t.stride(0) != 1 and t.shape[0] > 1:
+        raise ValueError("axis 0 must be contiguous (column-major, as a Julia Array)")
+    strides = list(t.stride())
+    strides[0] = 1
+    return make_grid(t.dim(), torch_dtype_code(t.dtype), t.shape, strides, t.data_ptr())
+
+
+def grid_from_numpy(a: np.ndarray, code: int | None = None) -> Grid:
+    if a.ndim < 1 or a.ndim > 3:
+        raise ValueError("grids have 1 to 3 dimensions")
+    es = a.itemsize
+    strides = [s // es for s in a.strides]
+    if a.shape[0] > 1 and strides[0] != 1:
+        raise ValueError("axis 0 must be contiguous (use order='F')")
+    strides[0] = 1
+    code = numpy_dtype_code(a.dtype) if code is None else code
+    return make_grid(a.ndim, code, a.shape, strides, a.ctypes.data)
+
+
+class LoweredStencil:
+    """Keeps the ctypes arrays alive while a StencilDesc points at them."""
+
+    def __init__(self, stencil, grid_ndims: int | None = None):
+        from .stencil import Kernel
+        offs = stencil.offsets()
+        n = stencil.ndims
+        self.offsets = (C.c_int32 * (len(offs) * n))(*[c for o in offs for c in o])
+        self.weights = None
+        wdt = F64
+        if isinstance(stencil, Kernel):
+            self.weights = (C.c_double * len(offs))(*stencil.weights)
+            wdt = F32 if stencil.weight_dtype == "f32" else F64
+        d = StencilDesc()
+        d.ndims = n
+        d.len = len(offs)
+        d.radius = stencil.radius
+        d.shape = stencil.shape_id
+        d.offsets = C.cast(self.offsets, C.POINTER(C.c_int32))
+        d.weights = C.cast(self.weights, C.POINTER(C.c_double)) if self.weights is not None else None
+        d.weight_dtype = wdt
+        self.desc = d
+
+
+def lower_op(red) -> OpDesc:
+    o = OpDesc()
+    o.code = red.code
+    bm, sm, alpha = red.params()
+    o.birth_mask = bm
+    o.survive_mask = sm
+    o.alpha = alpha
+    return o
+
+
+def lower_bc(boundary, padding) -> BcDesc:
+    from .boundary import Remove
+    b = BcDesc()
+    b.boundary = boundary.code
+    b.padding = padding.code
+    if isinstance(boundary, Remove):
+        pv = boundary.padval
+        if pv is None:
+            raise ValueError("Remove() without a padval cannot feed a numeric reduction; use Remove(0)")
+        if isinstance(pv, (bool, np.bool_)):
+            pv = int(pv)
+        b.padval = float(pv)
+        b.padval_int = int(pv) if float(pv).is_integer() else 0
+    return b

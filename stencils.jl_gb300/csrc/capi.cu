@@ -1,0 +1,456 @@
+// capi.cu — the extern "C" entry points of libstencilcuda.so for single maps and multi-step runs.
+//
+// stc_map       replaces gatherstencil!(f, dest, source)            src/gatherstencil.jl:89-103
+// stc_map_steps replaces the loop A = gatherstencil!(f, A::Switching) src/gatherstencil.jl:77-83
+// stc_update_boundary replaces update_boundary!                      src/array.jl:195-233
+// Argument checks return the statuses that mirror the reference's ArgumentErrors.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "dispatch.h"
+#include "life.h"
+#include "map_kernel.cuh"
+#include "profile.h"
+
+namespace stc {
+
+// ---------------------------------------------------------------------------- registry
+static std::map<std::tuple<int, int, int, int, int>, KernelEntry>& registry() {
+    static std::map<std::tuple<int, int, int, int, int>, KernelEntry> r;
+    return r;
+}
+
+void register_kernel(int dt, int opv, int kind, int R, int N, const KernelEntry& e) {
+    registry()[std::make_tuple(dt, opv, kind, R, N)] = e;
+}
+
+const KernelEntry* find_kernel(int dt, int opv, int kind, int R, int N) {
+    auto& r = registry();
+    auto it = r.find(std::make_tuple(dt, opv, kind, kind == STC_SHAPE_TABLE ? 0 : R, kind == STC_SHAPE_TABLE ? 0 : N));
+    return it == r.end() ? nullptr : &it->second;
+}
+
+int dtype_size(int dt) {
+    switch (dt) {
+    case STC_F64: case STC_I64: return 8;
+    case STC_F32: case STC_I32: return 4;
+    case STC_BF16: case STC_F16: return 2;
+    case STC_U8: case STC_BOOL: return 1;
+    }
+    return 0;
+}
+
+bool is_float_dtype(int dt) { return dt == STC_F64 || dt == STC_F32 || dt == STC_BF16 || dt == STC_F16; }
+
+static thread_local int g_last_cuda_error = 0;
+
+int cuda_fail(cudaError_t e) {
+    if (e == cudaSuccess) return STC_OK;
+    g_last_cuda_error = (int)e;
+    return STC_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------------------- device context
+static std::mutex g_ctx_mu;
+static DeviceCtx g_ctx[64];
+
+int device_ctx(DeviceCtx** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { cuda_fail(e); return STC_ERR_NO_DEVICE; }
+    if (dev < 0 || dev >= 64) return STC_ERR_NO_DEVICE;
+    DeviceCtx& c = g_ctx[dev];
+    if (c.device == dev) { *out = &c; return STC_OK; }
+    std::lock_guard<std::mutex> g(g_ctx_mu);
+    if (c.device != dev) {
+        cudaDeviceProp prop;
+        e = cudaGetDeviceProperties(&prop, dev);
+        if (e != cudaSuccess) return cuda_fail(e);
+        if (prop.major < 10) return STC_ERR_NO_DEVICE;
+        c.num_sms = prop.multiProcessorCount;
+        c.max_smem_optin = (int)prop.sharedMemPerBlockOptin;
+        int* h = nullptr;
+        e = cudaHostAlloc((void**)&h, sizeof(int), cudaHostAllocMapped);
+        if (e != cudaSuccess) return cuda_fail(e);
+        *h = 0;
+        int* d = nullptr;
+        e = cudaHostGetDevicePointer((void**)&d, h, 0);
+        if (e != cudaSuccess) return cuda_fail(e);
+        c.status = d;
+        c.status_host = h;
+        c.device = dev;
+    }
+    *out = &c;
+    return STC_OK;
+}
+
+// reads and clears the status word after the stream finished
+static int finish_sync(cudaStream_t s, DeviceCtx* ctx) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e);
+    volatile int* h = ctx->status_host;
+    if (*h) {
+        *h = 0;
+        return STC_ERR_TIMEOUT;
+    }
+    return STC_OK;
+}
+
+// ---------------------------------------------------------------------------- tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encoder() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    return fn;
+}
+
+static CUtensorMapDataType tma_dtype(int dt) {
+    switch (dt) {
+    case STC_F64: return CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    case STC_F32: return CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    case STC_BF16: return CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    case STC_F16: return CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
+    case STC_I32: return CU_TENSOR_MAP_DATA_TYPE_INT32;
+    case STC_I64: return CU_TENSOR_MAP_DATA_TYPE_INT64;
+    default: return CU_TENSOR_MAP_DATA_TYPE_UINT8;
+    }
+}
+
+// ---------------------------------------------------------------------------- validation
+int result_dtype(int op, int sdt, int wdt) {
+    const bool sf = is_float_dtype(sdt);
+    if (dtype_size(sdt) == 0) return STC_ERR_UNSUPPORTED;
+    switch (op) {
+    case STC_OP_MEAN: return sf ? sdt : STC_F64;
+    case STC_OP_SUM: return sf ? sdt : (sdt == STC_BOOL ? STC_I64 : sdt);
+    case STC_OP_KDOT:
+        if (sf && sdt != STC_F64 && wdt == STC_F32) return sdt;
+        return STC_F64;
+    case STC_OP_MIN: case STC_OP_MAX: return sdt;
+    case STC_OP_LIFE: return sf ? STC_ERR_UNSUPPORTED : sdt;
+    case STC_OP_DIFFUSE: return sf ? sdt : STC_ERR_UNSUPPORTED;
+    }
+    return STC_ERR_UNSUPPORTED;
+}
+
+static int op_variant(const stc_op* op, int sdt, int wdt) {
+    switch (op->code) {
+    case STC_OP_MEAN: return OPV_MEAN;
+    case STC_OP_SUM: return OPV_SUM;
+    case STC_OP_KDOT: return (is_float_dtype(sdt) && sdt != STC_F64 && wdt == STC_F32) ? OPV_KDOT_F : OPV_KDOT_D;
+    case STC_OP_MIN: return OPV_MIN;
+    case STC_OP_MAX: return OPV_MAX;
+    case STC_OP_LIFE: return OPV_LIFE;
+    case STC_OP_DIFFUSE: return OPV_DIFFUSE;
+    }
+    return -1;
+}
+
+static int check_grid(const stc_grid* g) {
+    if (!g || g->ndims < 1 || g->ndims > 3 || dtype_size(g->dtype) == 0) return STC_ERR_INVALID;
+    if (g->size[0] > 1 && g->stride[0] != 1) return STC_ERR_INVALID;
+    for (int d = 0; d < g->ndims; ++d)
+        if (g->size[d] < 0 || g->stride[d] < 0) return STC_ERR_INVALID;
+    return STC_OK;
+}
+
+int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
+                 const stc_op* op, const stc_bc* bc) {
+    int rc;
+    if ((rc = check_grid(src)) || (rc = check_grid(dst))) return rc;
+    if (!st || !op || !bc || !st->offsets) return STC_ERR_INVALID;
+    if (st->len < 1 || st->len > STC_MAX_LEN || st->ndims < 1 || st->ndims > src->ndims) return STC_ERR_INVALID;
+    if (st->radius < 0 || st->radius > STC_MAX_RADIUS) return STC_ERR_UNSUPPORTED;
+    for (int k = 0; k < st->len * st->ndims; ++k)
+        if (st->offsets[k] > st->radius || st->offsets[k] < -st->radius) return STC_ERR_UNSUPPORTED;
+    if (op->code == STC_OP_KDOT && !st->weights) return STC_ERR_KERNEL_LENGTH;
+    if (op->code == STC_OP_LIFE && st->len > 31) return STC_ERR_UNSUPPORTED;
+    if (bc->boundary < STC_REMOVE || bc->boundary > STC_USE) return STC_ERR_INVALID;
+    if (bc->padding < STC_CONDITIONAL || bc->padding > STC_HALO_OUT) return STC_ERR_INVALID;
+    if (bc->boundary == STC_USE && bc->padding == STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
+    const int rdt = result_dtype(op->code, src->dtype, st->weight_dtype);
+    if (rdt < 0) return rdt;
+    if (dst->dtype != rdt) return STC_ERR_UNSUPPORTED;
+    if (dst->ndims != src->ndims) return STC_ERR_SIZE_MISMATCH;
+    // StencilArray constructor: radius < each parent axis (src/array.jl:451-453)
+    for (int d = 0; d < src->ndims; ++d)
+        if (!(st->radius < src->size[d])) return STC_ERR_RADIUS;
+    const bool halo = bc->padding != STC_CONDITIONAL;
+    for (int d = 0; d < src->ndims; ++d) {
+        const int64_t logical = src->size[d] - (halo ? 2 * st->radius : 0);
+        if (logical < 0) return STC_ERR_RADIUS;
+        const int64_t want = logical + ((halo && dst_padded) ? 2 * st->radius : 0);
+        if (dst->size[d] != want) return STC_ERR_SIZE_MISMATCH;  // _checksizes (src/gatherstencil.jl:118-124)
+    }
+    for (const stc_grid* g : {src, dst}) {
+        int64_t cells = 1;
+        for (int d = 0; d < g->ndims; ++d) cells *= g->size[d];
+        if (cells && !g->data) return STC_ERR_INVALID;
+    }
+    return STC_OK;
+}
+
+// ---------------------------------------------------------------------------- shapes
+static void generate_shape(int kind, int R, int N, std::vector<int>& out) {
+    out.clear();
+    const int zr = N >= 3 ? R : 0, yr = N >= 2 ? R : 0;
+    for (int z = -zr; z <= zr; ++z)
+        for (int y = -yr; y <= yr; ++y)
+            for (int x = -R; x <= R; ++x) {
+                const int m = abs(x) + abs(y) + abs(z);
+                const int s2 = x * x + y * y + z * z;
+                const int zeros = (x == 0) + (N >= 2 && y == 0) + (N >= 3 && z == 0);
+                bool in = false;
+                if (kind == STC_SHAPE_WINDOW) in = N <= 2;
+                else if (kind == STC_SHAPE_MOORE) in = m != 0;
+                else if (kind == STC_SHAPE_VONNEUMANN) in = m >= 1 && m <= R;
+                else if (kind == STC_SHAPE_CIRCLE) in = s2 <= R * R + R;
+                else if (kind == STC_SHAPE_CROSS) in = zeros >= N - 1;
+                if (!in) continue;
+                out.push_back(x);
+                if (N >= 2) out.push_back(y);
+                if (N >= 3) out.push_back(z);
+            }
+}
+
+static bool table_is_shape(const stc_stencil* st, int grid_ndims) {
+    if (st->shape == STC_SHAPE_TABLE || st->ndims != grid_ndims) return false;
+    std::vector<int> t;
+    generate_shape(st->shape, st->radius, st->ndims, t);
+    if ((int)t.size() != st->len * st->ndims) return false;
+    return std::memcmp(t.data(), st->offsets, t.size() * sizeof(int)) == 0;
+}
+
+// ---------------------------------------------------------------------------- planning
+static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+static inline int64_t align_up(int64_t a, int64_t b) { return cdiv(a, b) * b; }
+
+// Fills MapParams for one map of src -> dst and launches it (no synchronisation).
+int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st, const stc_op* op,
+               const stc_bc* bc, cudaStream_t stream, DeviceCtx* ctx) {
+    static thread_local MapParams* pp = nullptr;
+    if (!pp) {
+        void* mem = nullptr;
+        if (posix_memalign(&mem, alignof(MapParams), sizeof(MapParams))) return STC_ERR_INVALID;
+        pp = (MapParams*)mem;
+    }
+    MapParams& p = *pp;
+    memset(&p, 0, sizeof(MapParams));
+    const int nd = src->ndims;
+    const int es = dtype_size(src->dtype);
+    const bool halo = bc->padding != STC_CONDITIONAL;
+    const int R = st->radius;
+    p.src = src->data;
+    p.dst = dst->data;
+    p.ndims = nd;
+    p.halo = halo;
+    p.boundary = bc->boundary;
+    p.status = ctx->status;
+    p.L = st->len;
+    p.birth = op->birth_mask;
+    p.survive = op->survive_mask;
+    p.alpha = op->alpha;
+    int64_t cells = 1;
+    for (int d = 0; d < 3; ++d) {
+        p.n[d] = d < nd ? src->size[d] - (halo ? 2 * R : 0) : 1;
+        p.sst[d] = d < nd ? src->stride[d] : 0;
+        p.dstr[d] = d < nd ? dst->stride[d] : 0;
+        p.hx[d] = (d < nd && halo) ? R : 0;
+        p.src_org += (int64_t)p.hx[d] * p.sst[d];
+        if (halo && dst_padded && d < nd) p.dst_org += (int64_t)R * p.dstr[d];
+        cells *= p.n[d];
+    }
+    if (cells == 0) return STC_OK;
+    // Remove's padval in the source element type
+    p.padi = bc->padval_int;
+    p.padf = bc->padval;
+    if (!is_float_dtype(src->dtype)) p.padf = (double)bc->padval_int;
+    // offsets (padded with zeros for trailing grid axes) and weights
+    int rmax[3] = {0, 0, 0};
+    for (int k = 0; k < st->len; ++k)
+        for (int d = 0; d < 3; ++d) {
+            const int o = d < st->ndims ? st->offsets[k * st->ndims + d] : 0;
+            p.off[k][d] = (int8_t)o;
+            rmax[d] = std::max(rmax[d], abs(o));
+        }
+    if (st->weights)
+        for (int k = 0; k < st->len; ++k) {
+            p.w[k] = st->weights[k];
+            p.wf[k] = (float)st->weights[k];
+        }
+    p.rx = rmax[0];
+    p.ry = rmax[1];
+    p.rz = rmax[2];
+
+    const int opv = op_variant(op, src->dtype, st->weight_dtype);
+    const KernelEntry* e = nullptr;
+    if (table_is_shape(st, nd)) e = find_kernel(src->dtype, opv, st->shape, R, st->ndims);
+    if (e && !(p.rx == R && p.ry == (nd >= 2 ? R : 0) && p.rz == (nd >= 3 ? R : 0))) e = nullptr;
+    if (!e) e = find_kernel(src->dtype, opv, STC_SHAPE_TABLE, 0, 0);
+    if (!e) return STC_ERR_UNSUPPORTED;
+
+    // tile geometry
+    const bool specialised = e->kind != STC_SHAPE_TABLE;
+    p.tiles3d = specialised ? (e->N == 3) : (nd == 3);
+    p.tw = 32 * e->xt;
+    p.th = p.tiles3d ? kMapWarps : kMapWarps * e->vs;
+    p.tz = p.tiles3d ? e->vs : 1;
+    const int V = 16 / es;
+    p.padl = p.rx + (int)(((p.hx[0] - p.rx) % V + V) % V);
+    p.bw = (int)align_up(p.padl + p.tw + p.rx, V);
+    p.bh = p.th + 2 * p.ry;
+    p.bd = p.tz + 2 * p.rz;
+    p.ntx = cdiv(p.n[0], p.tw);
+    p.nty = cdiv(p.n[1], p.th);
+    p.ntz = cdiv(p.n[2], p.tz);
+    p.ntiles = p.ntx * p.nty * p.ntz;
+    p.box_bytes = (uint32_t)((int64_t)p.bw * p.bh * p.bd * es);
+    p.stage_bytes = (uint32_t)align_up(p.box_bytes, 128);
+    const int64_t smem_cap = (int64_t)ctx->max_smem_optin - 1024 - 8 * kMaxStages;
+
+    bool tma = nd >= 2 && encoder() != nullptr && ((uintptr_t)src->data % 16 == 0) && p.bw <= 256 &&
+               p.bh <= 256 && p.bd <= 256 && 2 * (int64_t)p.stage_bytes <= smem_cap;
+    for (int d = 1; d < nd; ++d)
+        if ((src->stride[d] * es) % 16 != 0) tma = false;
+    if (tma) {
+        p.stages = (int)std::min<int64_t>(kMaxStages, std::max<int64_t>(2, (100 * 1024) / p.stage_bytes));
+        while ((int64_t)p.stages * p.stage_bytes > smem_cap) --p.stages;
+        cuuint64_t gdim[3], gstr[2];
+        cuuint32_t box[3] = {(cuuint32_t)p.bw, (cuuint32_t)p.bh, (cuuint32_t)p.bd}, est[3] = {1, 1, 1};
+        for (int d = 0; d < nd; ++d) gdim[d] = (cuuint64_t)src->size[d];
+        for (int d = 1; d < nd; ++d) gstr[d - 1] = (cuuint64_t)(src->stride[d] * es);
+        CUresult r = encoder()(&p.tmap, tma_dtype(src->dtype), (cuuint32_t)nd, src->data, gdim, gstr, box, est,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) tma = false;
+    }
+    p.use_tma = tma;
+    if (!tma) p.stages = 1;
+    // After a TMA copy, out-of-range cells hold zeros: right for Halo (never read) and Remove(0).
+    bool zero_pad = bc->boundary == STC_REMOVE &&
+                    (is_float_dtype(src->dtype) ? (bc->padval == 0.0 && !std::signbit(bc->padval)) : bc->padval_int == 0);
+    p.fixup = !halo && !zero_pad;
+
+    cudaError_t err;
+    void* prof = prof_begin(stream);
+    const char* kname;
+    if (!tma && (int64_t)p.stage_bytes > smem_cap) {
+        if (!e->launch_direct) e = find_kernel(src->dtype, opv, STC_SHAPE_TABLE, 0, 0);
+        if (!e || !e->launch_direct) return STC_ERR_UNSUPPORTED;
+        err = e->launch_direct(p, stream, ctx->num_sms);
+        kname = "map_direct";
+    } else {
+        err = e->launch(p, stream, ctx->num_sms);
+        kname = specialised ? (tma ? "map_shape_tma" : "map_shape_ldg") : (tma ? "map_table_tma" : "map_table_ldg");
+    }
+    prof_end(prof, stream, kname, (double)cells * (es + dtype_size(dst->dtype)), (double)cells);
+    return cuda_fail(err);
+}
+
+}  // namespace stc
+
+using namespace stc;
+
+extern "C" {
+
+int stc_abi_version(void) { return STC_ABI_VERSION; }
+
+const char* stc_strerror(int status) {
+    switch (status) {
+    case STC_OK: return "ok";
+    case STC_ERR_SIZE_MISMATCH: return "Source array sizes must match";
+    case STC_ERR_RADIUS: return "stencil radius is larger than array axis";
+    case STC_ERR_KERNEL_LENGTH: return "Stencil length does not match kernel length";
+    case STC_ERR_UNSUPPORTED: return "unsupported shape / op / dtype / boundary combination";
+    case STC_ERR_INVALID: return "invalid argument";
+    case STC_ERR_CUDA: return "CUDA error";
+    case STC_ERR_TIMEOUT: return "a bounded device wait timed out";
+    case STC_ERR_NO_DEVICE: return "no sm_100-family GPU";
+    case STC_ERR_BUDGET: return "request exceeds the HBM budget";
+    case STC_ERR_BUSY: return "not finished";
+    case STC_ERR_CANCELLED: return "cancelled";
+    }
+    return "unknown status";
+}
+
+int stc_last_cuda_error(void) { return g_last_cuda_error; }
+
+int stc_result_dtype(int32_t opcode, int32_t src_dtype, int32_t weight_dtype) {
+    return result_dtype(opcode, src_dtype, weight_dtype);
+}
+
+int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded, const stc_stencil* st, const stc_op* op,
+            const stc_bc* bc, void* stream, uint32_t flags) {
+    int rc = validate_map(src, dst, dst_padded, st, op, bc);
+    if (rc) return rc;
+    DeviceCtx* ctx = nullptr;
+    if ((rc = device_ctx(&ctx))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = launch_halo_fill(src, st->radius, bc, s))) return rc;
+    if ((rc = launch_map(src, dst, dst_padded, st, op, bc, s, ctx))) return rc;
+    if (!(flags & STC_ASYNC)) rc = finish_sync(s, ctx);
+    return rc;
+}
+
+int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
+                  int64_t nsteps, int32_t* out_src_is_b, void* stream, uint32_t flags) {
+    if (nsteps < 0) return STC_ERR_INVALID;
+    int rc = validate_map(a, b, 1, st, op, bc);
+    if (rc) return rc;
+    for (int d = 0; d < a->ndims; ++d)
+        if (a->size[d] != b->size[d] || a->dtype != b->dtype) return STC_ERR_SIZE_MISMATCH;
+    if (a->data == b->data && nsteps > 0) return STC_ERR_INVALID;
+    DeviceCtx* ctx = nullptr;
+    if ((rc = device_ctx(&ctx))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int64_t done = 0;
+    int src_is_b = 0;
+    // Cellular automata on bit-packable grids run temporally blocked on a packed copy.
+    rc = life_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
+    if (rc) return rc;
+    const stc_grid* grids[2] = {a, b};
+    for (int64_t k = done; k < nsteps; ++k) {
+        const stc_grid* sg = grids[src_is_b];
+        const stc_grid* dg = grids[1 - src_is_b];
+        if ((rc = launch_halo_fill(sg, st->radius, bc, s))) return rc;
+        if ((rc = launch_map(sg, dg, 1, st, op, bc, s, ctx))) return rc;
+        src_is_b = 1 - src_is_b;
+    }
+    if (out_src_is_b) *out_src_is_b = src_is_b;
+    if (!(flags & STC_ASYNC)) rc = finish_sync(s, ctx);
+    return rc;
+}
+
+int stc_update_boundary(const stc_grid* parent, int32_t radius, const stc_bc* bc, void* stream, uint32_t flags) {
+    int rc = check_grid(parent);
+    if (rc) return rc;
+    if (!bc || radius < 0) return STC_ERR_INVALID;
+    for (int d = 0; d < parent->ndims; ++d)
+        if (!(radius < parent->size[d]) || parent->size[d] - 2 * radius < 0) return STC_ERR_RADIUS;
+    DeviceCtx* ctx = nullptr;
+    if ((rc = device_ctx(&ctx))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = launch_halo_fill(parent, radius, bc, s))) return rc;
+    if (!(flags & STC_ASYNC)) rc = finish_sync(s, ctx);
+    return rc;
+}
+
+}  // extern "C"

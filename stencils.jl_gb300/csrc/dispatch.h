@@ -1,0 +1,59 @@
+// dispatch.h — host-side registry of compiled map kernels and shared internals of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/stencil_cuda.h"
+
+namespace stc {
+
+struct MapParams;
+
+// Reduction variants a kernel is compiled for (an stc_opcode refined by accumulation type).
+enum OpVariant : int {
+    OPV_MEAN = 0, OPV_SUM = 1, OPV_KDOT_D = 2, OPV_KDOT_F = 3, OPV_MIN = 4, OPV_MAX = 5,
+    OPV_LIFE = 6, OPV_DIFFUSE = 7, OPV_COUNT = 8
+};
+
+using LaunchFn = cudaError_t (*)(MapParams& p, cudaStream_t stream, int num_sms);
+
+struct KernelEntry {
+    LaunchFn launch = nullptr;       // tiled kernel (TMA or cooperative loads)
+    LaunchFn launch_direct = nullptr;  // per-output global gather, for boxes too large for shared memory
+    int xt = 1, vs = 1;              // columns per thread, stream slots per thread
+    int kind = STC_SHAPE_TABLE, R = 0, N = 0;
+};
+
+// kind == STC_SHAPE_TABLE for the generic kernels (R, N ignored)
+void register_kernel(int src_dtype, int opv, int kind, int R, int N, const KernelEntry& e);
+const KernelEntry* find_kernel(int src_dtype, int opv, int kind, int R, int N);
+
+// element size of an stc_dtype (0 if unknown)
+int dtype_size(int dt);
+bool is_float_dtype(int dt);
+
+// Per-device context: SM count, status word, tensor-map encoder.
+struct DeviceCtx {
+    int device = -1;
+    int num_sms = 0;
+    int* status = nullptr;     // device view of a mapped host int, OR-ed by kernels that give up a bounded wait
+    int* status_host = nullptr;
+    int max_smem_optin = 0;
+};
+int device_ctx(DeviceCtx** out);
+
+// remembers the CUDA error behind an STC_ERR_CUDA
+int cuda_fail(cudaError_t e);
+
+int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
+                 const stc_op* op, const stc_bc* bc);
+int result_dtype(int op, int sdt, int wdt);
+// one map launch (halo fill not included), no synchronisation
+int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st, const stc_op* op,
+               const stc_bc* bc, cudaStream_t stream, DeviceCtx* ctx);
+
+// halo fill (update_boundary!) of a Halo-padded parent
+int launch_halo_fill(const stc_grid* parent, int radius, const stc_bc* bc, cudaStream_t stream);
+
+}  // namespace stc

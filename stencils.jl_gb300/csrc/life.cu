@@ -1,0 +1,331 @@
+// life.cu — K3: bit-packed, temporally blocked outer-totalistic Moore(1) cellular automata.
+//
+// Replaces the loop  A = mapstencil!(rule, A::SwitchingStencilArray)  (src/gatherstencil.jl:77-83,
+// src/array.jl:610-611) for 2D Moore(1) rules on UInt8 / Bool / Int32 / Int64 grids.
+//
+// Layout: the logical grid is packed 32 cells per 32-bit word along the contiguous axis (bit j of
+// word w is cell 32w + j), rows stacked along axis 1.  A launch advances every row band by up to k
+// generations: each CTA holds full rows (the x-wrap happens inside shared memory) for its band plus
+// k halo rows above and below (y-wrap or zero rows from global), steps them k times in a shared
+// ping-pong pair — the valid band shrinks by one row per generation — and writes the band back.
+// One HBM/L2 round trip per k generations instead of per generation.
+//
+// Per word, the 8 neighbour planes come from funnel shifts of the three rows' (w-1, w, w+1) words;
+// a carry-save adder network produces the 4-bit neighbour count and the rule is evaluated bitwise.
+// The neighbour count is the count of nonzero neighbours, exactly what the LIFE op counts, so the
+// result is bit-identical to the per-cell gather for any input values.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "life.h"
+#include "profile.h"
+
+namespace stc {
+
+constexpr int kLifeThreads = 512;
+
+struct Count4 { uint32_t b0, b1, b2, b3; };
+
+__device__ __forceinline__ void full_add(uint32_t a, uint32_t b, uint32_t c, uint32_t& s, uint32_t& cy) {
+    const uint32_t t = a ^ b;
+    s = t ^ c;
+    cy = (a & b) | (t & c);
+}
+
+// neighbour count of every bit of word c from the (left, centre, right) words of rows u, c, d
+__device__ __forceinline__ Count4 count8(uint32_t uL, uint32_t u, uint32_t uR, uint32_t cL, uint32_t c,
+                                         uint32_t cR, uint32_t dL, uint32_t d, uint32_t dR) {
+    const uint32_t n1 = __funnelshift_l(uL, u, 1), n2 = u, n3 = __funnelshift_r(u, uR, 1);
+    const uint32_t n4 = __funnelshift_l(cL, c, 1), n5 = __funnelshift_r(c, cR, 1);
+    const uint32_t n6 = __funnelshift_l(dL, d, 1), n7 = d, n8 = __funnelshift_r(d, dR, 1);
+    uint32_t s1, c1, s2, c2, b0, d1, e0, e1;
+    full_add(n1, n2, n3, s1, c1);
+    full_add(n4, n5, n6, s2, c2);
+    const uint32_t s3 = n7 ^ n8, c3 = n7 & n8;
+    full_add(s1, s2, s3, b0, d1);
+    full_add(c1, c2, c3, e0, e1);
+    Count4 k;
+    k.b0 = b0;
+    k.b1 = e0 ^ d1;
+    const uint32_t f1 = e0 & d1;
+    k.b2 = e1 ^ f1;
+    k.b3 = e1 & f1;
+    return k;
+}
+
+template <bool CONWAY>
+__device__ __forceinline__ uint32_t apply_rule(const Count4& k, uint32_t c, uint32_t birth, uint32_t survive) {
+    if constexpr (CONWAY) {
+        // B3/S23: count == 3, or count == 2 and alive
+        return k.b1 & ~k.b2 & ~k.b3 & (k.b0 | c);
+    } else {
+        uint32_t out = 0;
+#pragma unroll
+        for (int n = 0; n <= 8; ++n) {
+            const uint32_t m = ((n & 1) ? k.b0 : ~k.b0) & ((n & 2) ? k.b1 : ~k.b1) & ((n & 4) ? k.b2 : ~k.b2) &
+                               ((n & 8) ? k.b3 : ~k.b3);
+            if ((birth >> n) & 1u) out |= m & ~c;
+            if ((survive >> n) & 1u) out |= m & c;
+        }
+        return out;
+    }
+}
+
+struct LifeParams {
+    const uint32_t* in;
+    uint32_t* out;
+    int W;          // words per row
+    int n1;         // rows
+    int TB;         // band rows written back per CTA
+    int k;          // generations this launch
+    int wrap;       // 1: Wrap, 0: Remove(0)
+    uint32_t birth, survive;
+};
+
+template <bool CONWAY>
+__global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifeParams p) {
+    extern __shared__ __align__(16) uint32_t lsm[];
+    const int W = p.W, k = p.k;
+    const int rows = p.TB + 2 * k;
+    uint32_t* buf0 = lsm;
+    uint32_t* buf1 = lsm + (size_t)rows * W;
+    const int y0 = blockIdx.x * p.TB;
+    // load the band plus k halo rows
+    for (int i = threadIdx.x; i < rows * W; i += blockDim.x) {
+        const int r = i / W, w = i - r * W;
+        int gy = y0 - k + r;
+        uint32_t v = 0;
+        if (p.wrap) {
+            gy %= p.n1;
+            if (gy < 0) gy += p.n1;
+            v = p.in[(size_t)gy * W + w];
+        } else if (gy >= 0 && gy < p.n1) {
+            v = p.in[(size_t)gy * W + w];
+        }
+        buf0[i] = v;
+    }
+    __syncthreads();
+    // thread -> (column w, strip s); strips split the valid row range of each generation
+    const int strips = max(1, (int)blockDim.x / W);
+    for (int g = 0; g < k; ++g) {
+        const uint32_t* src = (g & 1) ? buf1 : buf0;
+        uint32_t* dst = (g & 1) ? buf0 : buf1;
+        const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of src
+        const int nr = hi - lo;
+        for (int col = threadIdx.x; col < W * strips; col += blockDim.x) {
+            const int w = col % W, s = col / W;
+            if (s >= strips) break;
+            const int ra = lo + (int)((int64_t)nr * s / strips), rb = lo + (int)((int64_t)nr * (s + 1) / strips);
+            if (ra >= rb) continue;
+            const int wl = w == 0 ? W - 1 : w - 1, wr = w == W - 1 ? 0 : w + 1;
+            const bool edge_l = !p.wrap && w == 0, edge_r = !p.wrap && w == W - 1;
+            auto ld = [&](int r, uint32_t& L, uint32_t& C, uint32_t& R) {
+                const uint32_t* row = src + (size_t)r * W;
+                C = row[w];
+                L = edge_l ? 0u : row[wl];
+                R = edge_r ? 0u : row[wr];
+            };
+            uint32_t uL, u, uR, cL, c, cR, dL, d, dR;
+            ld(ra - 1, uL, u, uR);
+            ld(ra, cL, c, cR);
+            for (int r = ra; r < rb; ++r) {
+                ld(r + 1, dL, d, dR);
+                const Count4 cnt = count8(uL, u, uR, cL, c, cR, dL, d, dR);
+                uint32_t nx = apply_rule<CONWAY>(cnt, c, p.birth, p.survive);
+                if (!p.wrap) {
+                    const int gy = y0 - k + r;
+                    if (gy < 0 || gy >= p.n1) nx = 0u;   // rows outside the grid stay dead
+                }
+                dst[(size_t)r * W + w] = nx;
+                uL = cL; u = c; uR = cR;
+                cL = dL; c = d; cR = dR;
+            }
+        }
+        __syncthreads();
+    }
+    const uint32_t* fin = (k & 1) ? buf1 : buf0;
+    for (int i = threadIdx.x; i < p.TB * W; i += blockDim.x) {
+        const int r = i / W, w = i - r * W;
+        const int gy = y0 + r;
+        if (gy < p.n1) p.out[(size_t)gy * W + w] = fin[(size_t)(r + k) * W + w];
+    }
+}
+
+// ------------------------------------------------------------------ pack / unpack
+struct PackParams {
+    const void* base;   // parent base
+    int64_t org;        // parent offset of logical (0, 0)
+    int64_t sy;         // parent row stride (elements)
+    int dt;
+    int W, n1;
+    uint32_t* P;
+};
+
+template <class T>
+__global__ void life_pack_kernel(const PackParams p) {
+    const T* base = (const T*)p.base;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t groups = (int64_t)p.n1 * ((p.W + 31) / 32);
+    for (int64_t gi = warp; gi < groups; gi += nwarps) {
+        const int gpr = (p.W + 31) / 32;
+        const int y = (int)(gi / gpr), w0 = (int)(gi % gpr) * 32;
+        const T* row = base + p.org + (int64_t)y * p.sy;
+        uint32_t mine = 0;
+        const int nw = min(32, p.W - w0);
+        for (int i = 0; i < nw; ++i) {
+            const uint32_t b = __ballot_sync(0xffffffffu, row[(int64_t)(w0 + i) * 32 + lane] != (T)0);
+            if (lane == i) mine = b;
+        }
+        if (lane < nw) p.P[(size_t)y * p.W + w0 + lane] = mine;
+    }
+}
+
+template <class T>
+__global__ void life_unpack_kernel(const PackParams p) {
+    T* base = (T*)p.base;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t groups = (int64_t)p.n1 * ((p.W + 31) / 32);
+    for (int64_t gi = warp; gi < groups; gi += nwarps) {
+        const int gpr = (p.W + 31) / 32;
+        const int y = (int)(gi / gpr), w0 = (int)(gi % gpr) * 32;
+        T* row = base + p.org + (int64_t)y * p.sy;
+        const int nw = min(32, p.W - w0);
+        const uint32_t mine = lane < nw ? p.P[(size_t)y * p.W + w0 + lane] : 0u;
+        for (int i = 0; i < nw; ++i) {
+            const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+            row[(int64_t)(w0 + i) * 32 + lane] = (T)((word >> lane) & 1u);
+        }
+    }
+}
+
+static int launch_pack(bool pack, const stc_grid* g, int64_t org, int W, int n1, uint32_t* P, cudaStream_t s,
+                       int num_sms) {
+    PackParams p{};
+    p.base = g->data;
+    p.org = org;
+    p.sy = g->stride[1];
+    p.dt = g->dtype;
+    p.W = W;
+    p.n1 = n1;
+    p.P = P;
+    const int64_t groups = (int64_t)n1 * ((W + 31) / 32);
+    int blocks = (int)std::min<int64_t>((groups * 32 + 255) / 256, (int64_t)num_sms * 8);
+    blocks = std::max(blocks, 1);
+    void* prof = prof_begin(s);
+#define STC_PACK_CASE(DT, T)                                                                       \
+    case DT:                                                                                       \
+        if (pack) life_pack_kernel<T><<<blocks, 256, 0, s>>>(p); else life_unpack_kernel<T><<<blocks, 256, 0, s>>>(p); \
+        break;
+    switch (g->dtype) {
+        STC_PACK_CASE(STC_U8, uint8_t)
+        STC_PACK_CASE(STC_BOOL, uint8_t)
+        STC_PACK_CASE(STC_I32, int32_t)
+        STC_PACK_CASE(STC_I64, int64_t)
+    default: return STC_ERR_UNSUPPORTED;
+    }
+#undef STC_PACK_CASE
+    prof_end(prof, s, pack ? "life_pack" : "life_unpack", (double)W * 32 * n1 * (dtype_size(g->dtype) + 0.125),
+             (double)W * 32 * n1);
+    return cuda_fail(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------ host
+static bool is_moore1_2d(const stc_stencil* st) {
+    if (st->ndims != 2 || st->len != 8 || st->radius != 1) return false;
+    static const int want[16] = {-1, -1, 0, -1, 1, -1, -1, 0, 1, 0, -1, 1, 0, 1, 1, 1};
+    for (int i = 0; i < 16; ++i)
+        if (st->offsets[i] != want[i]) return false;
+    return true;
+}
+
+// Band rows and generations per launch for a grid of W words x n1 rows: one band per SM when the
+// grid is tall enough (the kernel is ALU-bound, so every SM should hold one band), at most 16
+// generations per launch, and whatever fits in shared memory.
+void life_plan(int W, int n1, int64_t steps_left, int smem_cap, int num_sms, int* TB, int* k) {
+    int kk = (int)std::min<int64_t>(steps_left, 16);
+    int tb = std::max(8, (n1 + num_sms - 1) / num_sms);
+    while (kk > 1 && (int64_t)2 * (tb + 2 * kk) * W * 4 > smem_cap) --kk;
+    while (tb > 1 && (int64_t)2 * (tb + 2 * kk) * W * 4 > smem_cap) --tb;
+    *TB = tb;
+    *k = kk;
+}
+
+int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
+                   int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx, int64_t* done) {
+    *done = 0;
+    if (nsteps < 1 || op->code != STC_OP_LIFE || a->ndims != 2 || !is_moore1_2d(st)) return STC_OK;
+    if (!(a->dtype == STC_U8 || a->dtype == STC_BOOL || a->dtype == STC_I32 || a->dtype == STC_I64)) return STC_OK;
+    const bool halo = bc->padding != STC_CONDITIONAL;
+    const bool wrap = bc->boundary == STC_WRAP;
+    const bool remove0 = bc->boundary == STC_REMOVE && bc->padval_int == 0;
+    if (!wrap && !remove0) return STC_OK;   // Reflect / Use / nonzero padval take the per-step kernel
+    const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
+    if (n0 < 32 || n0 % 32 != 0 || n1 < 1 || n0 / 32 > 512 || n1 > (1 << 30)) return STC_OK;
+    const int W = (int)(n0 / 32);
+    const int smem_cap = ctx->max_smem_optin - 1024;
+    int TB, k;
+    life_plan(W, (int)n1, nsteps, smem_cap, ctx->num_sms, &TB, &k);
+    if ((int64_t)2 * (TB + 2 * k) * W * 4 > smem_cap) return STC_OK;
+
+    const size_t words = (size_t)W * n1;
+    uint32_t* P = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&P, 2 * words * sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    uint32_t* Pbuf[2] = {P, P + words};
+    const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
+    int rc = launch_pack(true, a, org_a, W, (int)n1, Pbuf[0], stream, ctx->num_sms);
+    if (rc) { cudaFreeAsync(P, stream); return rc; }
+
+    LifeParams lp{};
+    lp.W = W;
+    lp.n1 = (int)n1;
+    lp.wrap = wrap;
+    lp.birth = op->birth_mask;
+    lp.survive = op->survive_mask;
+    const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
+    int cur = 0;
+    int64_t left = nsteps;
+    while (left > 0) {
+        // the last generation runs alone so both packed buffers hold the last two states
+        const int64_t budget = left > 1 ? left - 1 : 1;
+        life_plan(W, (int)n1, budget, smem_cap, ctx->num_sms, &TB, &k);
+        lp.in = Pbuf[cur];
+        lp.out = Pbuf[1 - cur];
+        lp.TB = TB;
+        lp.k = k;
+        const size_t smem = (size_t)2 * (TB + 2 * k) * W * 4;
+        const int grid = (int)((n1 + TB - 1) / TB);
+        void* prof = prof_begin(stream);
+        if (conway) {
+            cudaFuncSetAttribute(life_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            life_block_kernel<true><<<grid, kLifeThreads, smem, stream>>>(lp);
+        } else {
+            cudaFuncSetAttribute(life_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            life_block_kernel<false><<<grid, kLifeThreads, smem, stream>>>(lp);
+        }
+        prof_end(prof, stream, "life_block", 2.0 * n0 * n1 * k, (double)n0 * n1 * k);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) { cudaFreeAsync(P, stream); return cuda_fail(e); }
+        cur = 1 - cur;
+        left -= k;
+    }
+    // Pbuf[cur] holds generation nsteps, Pbuf[1-cur] generation nsteps-1 (or the input if nsteps == 1).
+    // The reference leaves the result in b after an odd number of steps, in a after an even number.
+    const bool res_in_b = (nsteps & 1) != 0;
+    const stc_grid* res = res_in_b ? b : a;
+    const stc_grid* prev = res_in_b ? a : b;
+    rc = launch_pack(false, res, res_in_b ? org_b : org_a, W, (int)n1, Pbuf[cur], stream, ctx->num_sms);
+    if (!rc && nsteps > 1) rc = launch_pack(false, prev, res_in_b ? org_a : org_b, W, (int)n1, Pbuf[1 - cur], stream, ctx->num_sms);
+    cudaFreeAsync(P, stream);
+    if (rc) return rc;
+    *src_is_b = res_in_b ? 1 : 0;
+    *done = nsteps;
+    return STC_OK;
+}
+
+}  // namespace stc

@@ -1,0 +1,498 @@
+// map_kernel.cuh — K1, the gather-map kernel: dst[I] = f(stencil(src, I)) for every logical I.
+//
+// Replaces gatherstencil_kernel! (src/gatherstencil.jl:105-109) with stencil(A, I) (src/array.jl:22-30).
+//
+// Design (GB300):
+//  * persistent CTAs walk output tiles; each tile's input box (tile + halo) is staged into shared
+//    memory by TMA (cp.async.bulk.tensor, no multicast) through a multi-stage mbarrier pipeline, so
+//    the next tiles stream in while the current one is reduced;
+//  * boundary conditions live only in the loader: Halo padding reads the halo ring from memory,
+//    Remove with a zero padval uses TMA's zero fill, and Wrap / Reflect / nonzero Remove patch the
+//    out-of-range cells of edge tiles after the copy lands (src/array.jl:129-188);
+//  * parents whose strides are not 16-byte multiples (e.g. a 4098-wide UInt8 halo parent) use a
+//    cooperative load of the same box with the boundary mapping applied per element;
+//  * the reduction folds over the neighbours in offset order.  The generic kernel reads the offset
+//    table at run time; the shape-specialised kernels take the table as a compile-time constant and
+//    stream the box along the slowest tiled axis, so every loaded value is reused from registers by
+//    all outputs of the thread that need it, while keeping each output's fold order.
+#pragma once
+
+#include "common.cuh"
+
+namespace stc {
+
+constexpr int kMapThreads = 256;
+constexpr int kMapWarps = kMapThreads / 32;
+constexpr int kMaxStages = 4;
+
+struct MapParams {
+    CUtensorMap tmap;          // source parent, valid when use_tma
+    const void* src;           // source parent base
+    void* dst;                 // destination parent base
+    int64_t sst[3];            // source strides (elements; 0 beyond ndims)
+    int64_t dstr[3];           // destination strides
+    int64_t src_org;           // parent offset of logical (0,0,0)
+    int64_t dst_org;
+    int64_t n[3];              // logical size (1 beyond ndims)
+    int64_t ntx, nty, ntz, ntiles;
+    double padf;               // Remove padval in the source type (floats)
+    int64_t padi;              // Remove padval (integers)
+    double alpha;              // DIFFUSE
+    int32_t hx[3];             // parent coordinate of logical 0 per axis (R for Halo padding)
+    int32_t halo;              // halo ring present in memory
+    int32_t boundary;
+    int32_t ndims;
+    int32_t rx, ry, rz;        // box halo per axis (largest |offset| along it)
+    int32_t padl;              // shared-memory x index of the tile's first column
+    int32_t tw, th, tz;        // tile extents (outputs)
+    int32_t bw, bh, bd;        // box extents (inputs)
+    int32_t tiles3d;           // 1: threads map (warp, slot) -> (y, z); 0: -> (y)
+    int32_t use_tma;
+    int32_t stages;
+    int32_t fixup;             // edge tiles need patching after TMA (Wrap / Reflect / nonzero Remove)
+    uint32_t box_bytes;
+    uint32_t stage_bytes;
+    int32_t* status;
+    int32_t L;
+    uint32_t birth, survive;
+    int8_t off[STC_MAX_LEN][3];
+    float wf[STC_MAX_LEN];
+    double w[STC_MAX_LEN];
+};
+
+// ---------------------------------------------------------------------------- reductions
+// Each op: Acc type; first(v) = Base.reduce_first; step(a, v, k); finish(a, centre).
+// KDOT starts from zero and steps every term (src/stencils/kernel.jl:264-270).
+
+template <class Tin, class Tout, class Acc> struct OpMean {
+    static constexpr bool kZeroInit = false, kNeedsCentre = false;
+    using A = Acc;
+    __device__ static A first(Tin v, int) { return conv(v); }
+    __device__ static A step(A a, Tin v, int, const MapParams&) { return add(a, conv(v)); }
+    __device__ static Tout finish(A a, Tin, const MapParams& p) {
+        if constexpr (sizeof(A) == 8) return from_f64<Tout>(__ddiv_rn(a, (double)p.L));
+        else return from_f32<Tout>(__fdiv_rn(a, (float)p.L));
+    }
+    __device__ static A conv(Tin v) {
+        if constexpr (sizeof(A) == 8) return cvt_d(v); else return cvt_f(v);
+    }
+    __device__ static A add(A a, A b) {
+        if constexpr (sizeof(A) == 8) return __dadd_rn(a, b); else return __fadd_rn(a, b);
+    }
+};
+
+template <class Tin, class Tout, class Acc> struct OpSumF {
+    static constexpr bool kZeroInit = false, kNeedsCentre = false;
+    using A = Acc;
+    __device__ static A first(Tin v, int) { return OpMean<Tin, Tout, Acc>::conv(v); }
+    __device__ static A step(A a, Tin v, int, const MapParams&) {
+        return OpMean<Tin, Tout, Acc>::add(a, OpMean<Tin, Tout, Acc>::conv(v));
+    }
+    __device__ static Tout finish(A a, Tin, const MapParams&) {
+        if constexpr (sizeof(A) == 8) return from_f64<Tout>(a); else return from_f32<Tout>(a);
+    }
+};
+
+// integer sum: wraps at the accumulator's width (UInt8 sums stay UInt8; Bool widens to Int64)
+template <class Tin, class Tout, int ACC_DT> struct OpSumI {
+    static constexpr bool kZeroInit = false, kNeedsCentre = false;
+    using A = int64_t;
+    __device__ static A first(Tin v, int) { return cvt_i(v); }
+    __device__ static A step(A a, Tin v, int, const MapParams&) {
+        return wrap_int<ACC_DT>((int64_t)((uint64_t)a + (uint64_t)cvt_i(v)));
+    }
+    __device__ static Tout finish(A a, Tin, const MapParams&) { return (Tout)a; }
+};
+
+// kernelproduct in f64: product and sum rounded separately (no FMA), as the reference
+template <class Tin, class Tout> struct OpKdotD {
+    static constexpr bool kZeroInit = true, kNeedsCentre = false;
+    using A = double;
+    __device__ static A first(Tin v, int) { return 0.0; }
+    __device__ static A step(A a, Tin v, int k, const MapParams& p) {
+        return __dadd_rn(a, __dmul_rn(cvt_d(v), p.w[k]));
+    }
+    __device__ static Tout finish(A a, Tin, const MapParams&) { return from_f64<Tout>(a); }
+};
+
+// kernelproduct with f32 accumulation: fused multiply-add (tolerance path, error vs FP64 stated)
+template <class Tin, class Tout> struct OpKdotF {
+    static constexpr bool kZeroInit = true, kNeedsCentre = false;
+    using A = float;
+    __device__ static A first(Tin v, int) { return 0.0f; }
+    __device__ static A step(A a, Tin v, int k, const MapParams& p) { return fmaf(cvt_f(v), p.wf[k], a); }
+    __device__ static Tout finish(A a, Tin, const MapParams&) { return from_f32<Tout>(a); }
+};
+
+template <class Tin, class Tout, class Acc, bool MAX> struct OpMinMaxF {
+    static constexpr bool kZeroInit = false, kNeedsCentre = false;
+    using A = Acc;
+    __device__ static A first(Tin v, int) { return OpMean<Tin, Tout, Acc>::conv(v); }
+    __device__ static A step(A a, Tin v, int, const MapParams&) {
+        A b = OpMean<Tin, Tout, Acc>::conv(v);
+        return MAX ? jl_max(a, b) : jl_min(a, b);
+    }
+    __device__ static Tout finish(A a, Tin, const MapParams&) {
+        if constexpr (sizeof(A) == 8) return from_f64<Tout>(a); else return from_f32<Tout>(a);
+    }
+};
+
+template <class Tin, class Tout, bool MAX> struct OpMinMaxI {
+    static constexpr bool kZeroInit = false, kNeedsCentre = false;
+    using A = int64_t;
+    __device__ static A first(Tin v, int) { return cvt_i(v); }
+    __device__ static A step(A a, Tin v, int, const MapParams&) {
+        A b = cvt_i(v);
+        return MAX ? (b > a ? b : a) : (b < a ? b : a);
+    }
+    __device__ static Tout finish(A a, Tin, const MapParams&) { return (Tout)a; }
+};
+
+template <class Tin, class Tout> struct OpLife {
+    static constexpr bool kZeroInit = false, kNeedsCentre = true;
+    using A = int32_t;
+    __device__ static A first(Tin v, int) { return v != (Tin)0; }
+    __device__ static A step(A a, Tin v, int, const MapParams&) { return a + (v != (Tin)0); }
+    __device__ static Tout finish(A a, Tin c, const MapParams& p) {
+        uint32_t mask = (c != (Tin)0) ? p.survive : p.birth;
+        return (Tout)((mask >> a) & 1u);
+    }
+};
+
+// c + alpha * (sum(hood) - L*c), every operation rounded separately
+template <class Tin, class Tout, class Acc> struct OpDiffuse {
+    static constexpr bool kZeroInit = false, kNeedsCentre = true;
+    using A = Acc;
+    __device__ static A first(Tin v, int k) { return OpMean<Tin, Tout, Acc>::conv(v); }
+    __device__ static A step(A a, Tin v, int k, const MapParams& p) {
+        return OpMean<Tin, Tout, Acc>::add(a, OpMean<Tin, Tout, Acc>::conv(v));
+    }
+    __device__ static Tout finish(A s, Tin cv, const MapParams& p) {
+        if constexpr (sizeof(A) == 8) {
+            double c = cvt_d(cv);
+            double t = __dmul_rn((double)p.L, c);
+            t = __dsub_rn(s, t);
+            t = __dmul_rn(p.alpha, t);
+            return from_f64<Tout>(__dadd_rn(c, t));
+        } else {
+            float c = cvt_f(cv);
+            float t = __fmul_rn((float)p.L, c);
+            t = __fsub_rn(s, t);
+            t = __fmul_rn((float)p.alpha, t);
+            return from_f32<Tout>(__fadd_rn(c, t));
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------- shapes
+struct Off3 { int x, y, z; };
+template <int MAXL> struct OffTable { int len; Off3 o[MAXL]; };
+
+constexpr int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
+
+// The offsets Stencils.jl generates, in its column-major order (axis 0 fastest):
+// Window (src/stencils/window.jl:4-7, N<=2), Moore (moore.jl:5-18), VonNeumann (vonneumman.jl:5-15),
+// Circle (shapes.jl:58-67; sqrt(s) < R+0.5 <=> s <= R^2+R for integer s), Cross (shapes.jl:2-10).
+template <int KIND, int R, int N>
+constexpr OffTable<ipow(2 * R + 1, N)> make_shape() {
+    OffTable<ipow(2 * R + 1, N)> t{};
+    t.len = 0;
+    const int zr = N >= 3 ? R : 0, yr = N >= 2 ? R : 0;
+    for (int z = -zr; z <= zr; ++z)
+        for (int y = -yr; y <= yr; ++y)
+            for (int x = -R; x <= R; ++x) {
+                const int m = (x < 0 ? -x : x) + (y < 0 ? -y : y) + (z < 0 ? -z : z);
+                const int s2 = x * x + y * y + z * z;
+                const int zeros = (x == 0) + (N >= 2 && y == 0) + (N >= 3 && z == 0);
+                bool in = false;
+                if (KIND == STC_SHAPE_WINDOW) in = true;
+                else if (KIND == STC_SHAPE_MOORE) in = m != 0;
+                else if (KIND == STC_SHAPE_VONNEUMANN) in = m >= 1 && m <= R;
+                else if (KIND == STC_SHAPE_CIRCLE) in = s2 <= R * R + R;
+                else if (KIND == STC_SHAPE_CROSS) in = zeros >= N - 1;
+                if (in) t.o[t.len++] = Off3{x, y, z};
+            }
+    return t;
+}
+
+template <int KIND, int R, int N> struct Shape {
+    static constexpr int kKind = KIND, kR = R, kN = N;
+    static constexpr auto table = make_shape<KIND, R, N>();
+    static constexpr int L = table.len;
+};
+
+// ---------------------------------------------------------------------------- loaders
+__device__ __forceinline__ int64_t bound_axis(int boundary, int64_t i, int64_t s) {
+    if (boundary == STC_WRAP) return i < 0 ? i + s : (i >= s ? i - s : i);
+    // Reflect: 1-based 2-i / 2s-i, i.e. 0-based -j / 2s-2-j
+    return i < 0 ? -i : (i >= s ? 2 * s - 2 - i : i);
+}
+
+template <class Tin> __device__ __forceinline__ Tin padval_as(const MapParams& p);
+template <> __device__ __forceinline__ double padval_as<double>(const MapParams& p) { return p.padf; }
+template <> __device__ __forceinline__ float padval_as<float>(const MapParams& p) { return (float)p.padf; }
+template <> __device__ __forceinline__ __nv_bfloat16 padval_as<__nv_bfloat16>(const MapParams& p) {
+    return __float2bfloat16_rn((float)p.padf);
+}
+template <> __device__ __forceinline__ __half padval_as<__half>(const MapParams& p) {
+    return __double2half(p.padf);
+}
+template <> __device__ __forceinline__ uint8_t padval_as<uint8_t>(const MapParams& p) { return (uint8_t)p.padi; }
+template <> __device__ __forceinline__ int32_t padval_as<int32_t>(const MapParams& p) {
+    return (int32_t)(uint32_t)(uint64_t)p.padi;
+}
+template <> __device__ __forceinline__ int64_t padval_as<int64_t>(const MapParams& p) { return p.padi; }
+
+// Value of logical cell (x, y, z) for cells that may lie outside [0, n): the Conditional rules.
+template <class Tin>
+__device__ __forceinline__ Tin load_bounded(const MapParams& p, int64_t x, int64_t y, int64_t z) {
+    const Tin* src = (const Tin*)p.src;
+    if (p.halo) return src[p.src_org + x + y * p.sst[1] + z * p.sst[2]];
+    const bool in = x >= 0 && x < p.n[0] && y >= 0 && y < p.n[1] && z >= 0 && z < p.n[2];
+    if (!in) {
+        if (p.boundary == STC_REMOVE) return padval_as<Tin>(p);
+        x = bound_axis(p.boundary, x, p.n[0]);
+        y = bound_axis(p.boundary, y, p.n[1]);
+        z = bound_axis(p.boundary, z, p.n[2]);
+    }
+    return src[p.src_org + x + y * p.sst[1] + z * p.sst[2]];
+}
+
+struct TileOrigin { int64_t x0, y0, z0; };
+
+__device__ __forceinline__ TileOrigin tile_origin(const MapParams& p, int64_t t) {
+    TileOrigin o;
+    const int64_t tx = t % p.ntx;
+    const int64_t r = t / p.ntx;
+    o.x0 = tx * p.tw;
+    o.y0 = (r % p.nty) * p.th;
+    o.z0 = (r / p.nty) * p.tz;
+    return o;
+}
+
+// Needed input region of a tile (clipped at the array end for ragged tiles), in logical coords.
+struct Region { int64_t xa, xb, ya, yb, za, zb; };
+__device__ __forceinline__ Region needed_region(const MapParams& p, const TileOrigin& o) {
+    Region g;
+    g.xa = o.x0 - p.rx; g.xb = min(o.x0 + p.tw, p.n[0]) + p.rx;
+    g.ya = o.y0 - p.ry; g.yb = min(o.y0 + p.th, p.n[1]) + p.ry;
+    g.za = o.z0 - p.rz; g.zb = min(o.z0 + p.tz, p.n[2]) + p.rz;
+    return g;
+}
+
+__device__ __forceinline__ bool region_inside(const MapParams& p, const Region& g) {
+    return g.xa >= 0 && g.xb <= p.n[0] && g.ya >= 0 && g.yb <= p.n[1] && g.za >= 0 && g.zb <= p.n[2];
+}
+
+// smem index of logical (x, y, z) for a tile at origin o
+__device__ __forceinline__ int box_index(const MapParams& p, const TileOrigin& o, int64_t x, int64_t y,
+                                         int64_t z) {
+    return ((int)(z - o.z0 + p.rz) * p.bh + (int)(y - o.y0 + p.ry)) * p.bw + (int)(x - o.x0 + p.padl);
+}
+
+// Cooperative load (or patch) of the needed region.  only_outside: patch just the cells outside
+// [0, n) (after a TMA copy); otherwise load every needed cell.
+template <class Tin>
+__device__ void load_region(const MapParams& p, const TileOrigin& o, Tin* box, bool only_outside) {
+    const Region g = needed_region(p, o);
+    const int wx = (int)(g.xb - g.xa), wy = (int)(g.yb - g.ya), wz = (int)(g.zb - g.za);
+    const int total = wx * wy * wz;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+        const int ix = i % wx, r = i / wx;
+        const int64_t x = g.xa + ix, y = g.ya + r % wy, z = g.za + r / wy;
+        if (only_outside && x >= 0 && x < p.n[0] && y >= 0 && y < p.n[1] && z >= 0 && z < p.n[2]) continue;
+        box[box_index(p, o, x, y, z)] = load_bounded<Tin>(p, x, y, z);
+    }
+}
+
+__device__ __forceinline__ void issue_tile_tma(const MapParams& p, const TileOrigin& o, void* box,
+                                               uint64_t* bar) {
+    const int cx = (int)(o.x0 + p.hx[0] - p.padl);
+    const int cy = (int)(o.y0 + p.hx[1] - p.ry);
+    const int cz = (int)(o.z0 + p.hx[2] - p.rz);
+    mbar_arrive_expect_tx(bar, p.box_bytes);
+    if (p.ndims == 1) tma_load_1d(box, &p.tmap, bar, cx);
+    else if (p.ndims == 2) tma_load_2d(box, &p.tmap, bar, cx, cy);
+    else tma_load_3d(box, &p.tmap, bar, cx, cy, cz);
+}
+
+__device__ __forceinline__ void report(const MapParams& p, int code) {
+    if (p.status) atomicOr(p.status, code);
+}
+
+// ---------------------------------------------------------------------------- compute: generic
+// Thread owns XT columns (lane + 32 i) and VS slots; slot s is row warp*VS + s (2D tiles) or
+// (row warp, plane s) (3D tiles).  Each output folds over the run-time offset table.
+template <class Tin, class Tout, class Op, int XT, int VS>
+__device__ __forceinline__ void compute_generic(const MapParams& p, const TileOrigin& o, const Tin* box) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Tout* dst = (Tout*)p.dst;
+#pragma unroll
+    for (int s = 0; s < VS; ++s) {
+        const int ly = p.tiles3d ? warp : warp * VS + s;
+        const int lz = p.tiles3d ? s : 0;
+        const int64_t y = o.y0 + ly, z = o.z0 + lz;
+        if (y >= p.n[1] || z >= p.n[2]) continue;
+#pragma unroll
+        for (int i = 0; i < XT; ++i) {
+            const int lx = lane + 32 * i;
+            const int64_t x = o.x0 + lx;
+            if (x >= p.n[0]) continue;
+            const Tin* c = box + ((lz + p.rz) * p.bh + (ly + p.ry)) * p.bw + (lx + p.padl);
+            typename Op::A a;
+            int k0 = 0;
+            if constexpr (Op::kZeroInit) {
+                a = Op::first(c[0], 0);
+            } else {
+                a = Op::first(c[(p.off[0][2] * p.bh + p.off[0][1]) * p.bw + p.off[0][0]], 0);
+                k0 = 1;
+            }
+            for (int k = k0; k < p.L; ++k)
+                a = Op::step(a, c[(p.off[k][2] * p.bh + p.off[k][1]) * p.bw + p.off[k][0]], k, p);
+            dst[p.dst_org + x + y * p.dstr[1] + z * p.dstr[2]] = Op::finish(a, c[0], p);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------- compute: specialised
+// The box is streamed along the stream axis (y for 2D shapes, z for 3D shapes): for every input
+// row/plane r, the values the thread needs are loaded once and folded into each of its VS
+// outputs that uses them.  Rows are visited in increasing order and the generated tables are
+// sorted by (z, y, x), so each output still folds its neighbours in table order.
+template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
+__device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrigin& o, const Tin* box) {
+    constexpr int N = Sh::kN, R = Sh::kR, L = Sh::L;
+    constexpr int RS = R;                      // halo along the stream axis
+    constexpr int RX = R, RY = (N == 3) ? R : 0;
+    constexpr auto T = Sh::table;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    using A = typename Op::A;
+    A acc[XT][VS];
+    Tin ctr[XT][VS];
+#pragma unroll
+    for (int i = 0; i < XT; ++i)
+#pragma unroll
+        for (int s = 0; s < VS; ++s) {
+            if constexpr (Op::kZeroInit) acc[i][s] = Op::first(Tin(0), 0);
+            else acc[i][s] = A(0);
+            ctr[i][s] = Tin(0);
+        }
+    // (y, z) of slot 0 and the box coordinates of its stream origin
+    const int ly0 = (N == 3) ? warp : warp * VS;     // tile-local row of slot 0
+    const int lz0 = 0;
+#pragma unroll
+    for (int r = 0; r < VS + 2 * RS; ++r) {
+        // box row/plane index of stream position r
+        const int by = (N == 3) ? (ly0 + p.ry) : (ly0 + r);     // 2D: rows stream; 3D: fixed row
+        const int bz = (N == 3) ? (lz0 + r) : p.rz;             // 3D: planes stream
+        Tin v[XT][2 * RY + 1][2 * RX + 1];
+#pragma unroll
+        for (int i = 0; i < XT; ++i)
+#pragma unroll
+            for (int yy = 0; yy < 2 * RY + 1; ++yy)
+#pragma unroll
+                for (int xx = 0; xx < 2 * RX + 1; ++xx)
+                    v[i][yy][xx] = box[(bz * p.bh + by + yy - RY) * p.bw + lane + 32 * i + p.padl + xx - RX];
+#pragma unroll
+        for (int s = 0; s < VS; ++s) {
+            const int ds = r - RS - s;    // stream offset this row contributes at, for slot s
+            if (ds < -RS || ds > RS) continue;
+#pragma unroll
+            for (int k = 0; k < L; ++k) {
+                const int ko = (N == 3) ? T.o[k].z : T.o[k].y;
+                if (ko != ds) continue;
+                const int oy = (N == 3) ? T.o[k].y : 0;
+#pragma unroll
+                for (int i = 0; i < XT; ++i) {
+                    const Tin val = v[i][oy + RY][T.o[k].x + RX];
+                    if (!Op::kZeroInit && k == 0) acc[i][s] = Op::first(val, 0);
+                    else acc[i][s] = Op::step(acc[i][s], val, k, p);
+                }
+            }
+            if (Op::kNeedsCentre && ds == 0) {
+#pragma unroll
+                for (int i = 0; i < XT; ++i) ctr[i][s] = v[i][RY][RX];
+            }
+        }
+    }
+    Tout* dst = (Tout*)p.dst;
+#pragma unroll
+    for (int s = 0; s < VS; ++s) {
+        const int64_t y = o.y0 + ((N == 3) ? warp : warp * VS + s);
+        const int64_t z = o.z0 + ((N == 3) ? s : 0);
+        if (y >= p.n[1] || z >= p.n[2]) continue;
+#pragma unroll
+        for (int i = 0; i < XT; ++i) {
+            const int64_t x = o.x0 + lane + 32 * i;
+            if (x < p.n[0]) dst[p.dst_org + x + y * p.dstr[1] + z * p.dstr[2]] = Op::finish(acc[i][s], ctr[i][s], p);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------- the kernel
+template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
+__global__ void __launch_bounds__(kMapThreads) map_kernel(const __grid_constant__ MapParams p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t* bars = (uint64_t*)(smem_raw + (size_t)p.stages * p.stage_bytes);
+    auto stage_box = [&](int s) { return (Tin*)(smem_raw + (size_t)s * p.stage_bytes); };
+    auto compute = [&](const TileOrigin& o, const Tin* box) {
+        if constexpr (Sh::kKind == STC_SHAPE_TABLE) compute_generic<Tin, Tout, Op, XT, VS>(p, o, box);
+        else compute_shape<Tin, Tout, Op, Sh, XT, VS>(p, o, box);
+    };
+    const int64_t step = gridDim.x;
+    if (!p.use_tma) {
+        Tin* box = stage_box(0);
+        for (int64_t t = blockIdx.x; t < p.ntiles; t += step) {
+            const TileOrigin o = tile_origin(p, t);
+            load_region<Tin>(p, o, box, false);
+            __syncthreads();
+            compute(o, box);
+            __syncthreads();
+        }
+        return;
+    }
+    const int S = p.stages;
+    if (threadIdx.x == 0) {
+        prefetch_tensormap(&p.tmap);
+        for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int s = 0; s < S - 1; ++s) {
+            const int64_t t = blockIdx.x + (int64_t)s * step;
+            if (t < p.ntiles) issue_tile_tma(p, tile_origin(p, t), stage_box(s), &bars[s]);
+        }
+    int it = 0;
+    for (int64_t t = blockIdx.x; t < p.ntiles; t += step, ++it) {
+        const int s = it % S;
+        if (threadIdx.x == 0) {
+            const int64_t tn = t + (int64_t)(S - 1) * step;
+            if (tn < p.ntiles) {
+                fence_proxy_async();
+                const int sn = (it + S - 1) % S;
+                issue_tile_tma(p, tile_origin(p, tn), stage_box(sn), &bars[sn]);
+            }
+        }
+        const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((it / S) & 1));
+        if (!__syncthreads_and(ok)) {
+            // The copy never landed: record it, let in-flight copies drain (bounded), and leave.
+            if (threadIdx.x == 0) {
+                report(p, DEV_ERR_TIMEOUT);
+                for (int k = 0; k < S; ++k) mbar_wait_bounded(&bars[(it + k) % S], (uint32_t)(((it + k) / S) & 1), 100000000ll);
+            }
+            return;
+        }
+        const TileOrigin o = tile_origin(p, t);
+        Tin* box = stage_box(s);
+        if (p.fixup && !region_inside(p, needed_region(p, o))) {
+            load_region<Tin>(p, o, box, true);
+            fence_proxy_async();
+            __syncthreads();
+        }
+        compute(o, box);
+        __syncthreads();
+    }
+}
+
+}  // namespace stc

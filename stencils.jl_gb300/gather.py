@@ -1,0 +1,184 @@
+"""mapstencil / mapstencil_ (the reference's mapstencil!) and gatherstencil / gatherstencil_.
+
+Mirrors src/gatherstencil.jl.  Every map runs in libstencilcuda.so on the current CUDA device and
+stream; parents held in host memory (numpy) are staged to the device and the results (and, for
+Halo padding, the refreshed halo ring) copied back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from . import _lib
+from .array import (AbstractStencilArray, StencilArray, SwitchingStencilArray, _is_torch, colmajor_empty,
+                    to_device)
+from .boundary import Conditional, Halo
+from .ops import as_reduction
+from .stencil import Stencil
+
+
+def result_dtype_code(red, src_code: int, stencil) -> int:
+    lib = _lib.load()
+    wdt = A.LoweredStencil(stencil).desc.weight_dtype
+    rc = lib.stc_result_dtype(red.code, src_code, wdt)
+    if rc < 0:
+        raise NotImplementedError(f"{red} is not registered for element type {A.DTYPE_NAMES[src_code]}")
+    return rc
+
+
+def _code_of(x) -> int:
+    return A.torch_dtype_code(x.dtype) if _is_torch(x) else A.numpy_dtype_code(x.dtype)
+
+
+def _grid(x, code=None):
+    return A.grid_from_torch(x) if _is_torch(x) else A.grid_from_numpy(x, code)
+
+
+def _require_device(x):
+    if not _is_torch(x) or x.device.type != "cuda":
+        raise TypeError("expected a CUDA tensor")
+
+
+class _Staged:
+    """Device copies of host (numpy) parents, written back on exit."""
+
+    def __init__(self, *arrays, writeback=()):
+        self.host = arrays
+        self.writeback = set(writeback)
+        self.dev = []
+        for a in arrays:
+            if a is None or _is_torch(a):
+                self.dev.append(a)
+            else:
+                self.dev.append(to_device(a))
+
+    def done(self):
+        for i, (h, d) in enumerate(zip(self.host, self.dev)):
+            if h is not None and not _is_torch(h) and i in self.writeback:
+                h[...] = d.cpu().numpy()
+
+
+def _run_map(red, dest, src: AbstractStencilArray, dst_padded: bool):
+    lib = _lib.load()
+    st = A.LoweredStencil(src.stencil)
+    op = A.lower_op(red)
+    bc = A.lower_bc(src.boundary, src.padding if not isinstance(src, SwitchingStencilArray) else
+                    (Halo("in") if isinstance(src.padding, Halo) else src.padding))
+    halo = isinstance(src.padding, Halo)
+    stage = _Staged(src.parent, dest, writeback=(0, 1) if halo else (1,))
+    sp, dp = stage.dev
+    _require_device(sp)
+    gs, gd = _grid(sp), _grid(dp)
+    stream = _lib.current_stream_handle()
+    _lib.check(lib.stc_map(C.byref(gs), C.byref(gd), int(dst_padded), C.byref(st.desc), C.byref(op), C.byref(bc),
+                           stream, 0), "mapstencil")
+    stage.done()
+    return dest
+
+
+def _new_dest(like, shape, code):
+    if _is_torch(like):
+        return colmajor_empty(shape, A.torch_dtype(code), like.device)
+    if code == A.BF16:
+        raise TypeError("bfloat16 results need a device (torch) parent")
+    return np.empty(shape, dtype=A.NP_DTYPE[code], order="F")
+
+
+def mapstencil(f, *args, boundary=None, padding=None):
+    """mapstencil(f, A::StencilArray) or mapstencil(f, stencil, A; boundary, padding).
+
+    Returns a new array of size(A) holding f applied to the stencil around every cell
+    (src/gatherstencil.jl:14-39).  Extra array arguments (the reference's multi-array form) are not
+    registered reductions and raise NotImplementedError.
+    """
+    red = as_reduction(f)
+    if args and isinstance(args[0], Stencil):
+        hood, arr = args[0], args[1]
+        rest = args[2:]
+        sa = StencilArray(arr, hood, boundary, padding)
+    else:
+        sa, rest = args[0], args[1:]
+        if not isinstance(sa, AbstractStencilArray):
+            raise TypeError("mapstencil needs a StencilArray or (stencil, array)")
+    if rest:
+        raise NotImplementedError("extra array arguments are not part of the registered GPU path")
+    code = result_dtype_code(red, _code_of(sa.parent), sa.stencil)
+    dest = _new_dest(sa.parent, sa.shape, code)
+    if isinstance(sa, SwitchingStencilArray):
+        sa = StencilArray.from_parent(sa.source, sa.stencil, sa.boundary, sa.padding)
+    return _run_map(red, dest, sa, dst_padded=False)
+
+
+def mapstencil_(f, dest, source=None, *, steps: int = 1):
+    """mapstencil!(f, dest, source) or mapstencil!(f, A::SwitchingStencilArray).
+
+    For a SwitchingStencilArray, runs `steps` maps (default 1) and returns the switched array, as
+    `A = mapstencil!(f, A)` repeated `steps` times would (src/gatherstencil.jl:77-83).
+    """
+    red = as_reduction(f)
+    if isinstance(dest, SwitchingStencilArray):
+        return _run_steps(red, dest, int(steps))
+    if not isinstance(source, AbstractStencilArray):
+        raise TypeError("mapstencil_(f, dest, source) needs a StencilArray source")
+    if tuple(dest.shape) != tuple(source.shape):
+        padded = isinstance(source.padding, Halo) and tuple(dest.shape) == tuple(source.parent.shape)
+        if not padded:
+            raise A.ArgumentError(f"Source array sizes must match. Found: {tuple(source.shape)} and "
+                                  f"{tuple(dest.shape)}")
+        return _run_map(red, dest, source, dst_padded=True)
+    return _run_map(red, dest, source, dst_padded=False)
+
+
+def _run_steps(red, S: SwitchingStencilArray, steps: int) -> SwitchingStencilArray:
+    if steps < 0:
+        raise ValueError("steps must be >= 0")
+    lib = _lib.load()
+    st = A.LoweredStencil(S.stencil)
+    op = A.lower_op(red)
+    pad = Halo("in") if isinstance(S.padding, Halo) else Conditional()
+    bc = A.lower_bc(S.boundary, pad)
+    stage = _Staged(S.source, S.dest, writeback=(0, 1))
+    a, b = stage.dev
+    _require_device(a)
+    ga, gb = _grid(a), _grid(b)
+    out = C.c_int32(0)
+    stream = _lib.current_stream_handle()
+    _lib.check(lib.stc_map_steps(C.byref(ga), C.byref(gb), C.byref(st.desc), C.byref(op), C.byref(bc), steps,
+                                 C.byref(out), stream, 0), "mapstencil!")
+    stage.done()
+    if out.value:
+        return S.switch()
+    return S
+
+
+def update_boundary_(A_: AbstractStencilArray):
+    """update_boundary!(A): refresh the halo ring of a Halo-padded parent (src/array.jl:195-233)."""
+    if not isinstance(A_.padding, Halo):
+        return A_
+    lib = _lib.load()
+    bc = A.lower_bc(A_.boundary, A_.padding)
+    stage = _Staged(A_.parent, writeback=(0,))
+    g = _grid(stage.dev[0])
+    _lib.check(lib.stc_update_boundary(C.byref(g), A_.radius, C.byref(bc), _lib.current_stream_handle(), 0),
+               "update_boundary!")
+    stage.done()
+    return A_
+
+
+def mass(x, radius: int = 0, padding=None) -> float:
+    """FP64 compensated total of a device grid's logical cells."""
+    lib = _lib.load()
+    padding = Conditional() if padding is None else padding
+    bc = A.BcDesc()
+    bc.padding = padding.code
+    out = C.c_double(0.0)
+    _require_device(x)
+    g = _grid(x)
+    _lib.check(lib.stc_mass(C.byref(g), radius, C.byref(bc), C.byref(out), _lib.current_stream_handle()), "mass")
+    return out.value
+
+
+gatherstencil = mapstencil
+gatherstencil_ = mapstencil_
