@@ -290,18 +290,30 @@ __device__ __forceinline__ int box_index(const MapParams& p, const TileOrigin& o
     return ((int)(z - o.z0 + p.rz) * p.bh + (int)(y - o.y0 + p.ry)) * p.bw + (int)(x - o.x0 + p.padl);
 }
 
-// Cooperative load (or patch) of the needed region.  only_outside: patch just the cells outside
-// [0, n) (after a TMA copy); otherwise load every needed cell.
+// Cooperative load (or patch) of the needed region, one warp per box row.  only_outside: patch just
+// the cells outside [0, n) (after a TMA copy); otherwise load every needed cell.
 template <class Tin>
 __device__ void load_region(const MapParams& p, const TileOrigin& o, Tin* box, bool only_outside) {
     const Region g = needed_region(p, o);
-    const int wx = (int)(g.xb - g.xa), wy = (int)(g.yb - g.ya), wz = (int)(g.zb - g.za);
-    const int total = wx * wy * wz;
-    for (int i = threadIdx.x; i < total; i += blockDim.x) {
-        const int ix = i % wx, r = i / wx;
-        const int64_t x = g.xa + ix, y = g.ya + r % wy, z = g.za + r / wy;
-        if (only_outside && x >= 0 && x < p.n[0] && y >= 0 && y < p.n[1] && z >= 0 && z < p.n[2]) continue;
-        box[box_index(p, o, x, y, z)] = load_bounded<Tin>(p, x, y, z);
+    const int wy = (int)(g.yb - g.ya), wz = (int)(g.zb - g.za);
+    const int nrows = wy * wz;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const Tin* src = (const Tin*)p.src;
+    for (int row = warp; row < nrows; row += nwarps) {
+        const int64_t y = g.ya + row % wy, z = g.za + row / wy;
+        Tin* brow = box + ((int)(z - o.z0 + p.rz) * p.bh + (int)(y - o.y0 + p.ry)) * p.bw + p.padl;
+        const bool row_in = y >= 0 && y < p.n[1] && z >= 0 && z < p.n[2];
+        if (p.halo || (row_in && g.xa >= 0 && g.xb <= p.n[0])) {
+            if (only_outside) continue;   // (fixups never run for Halo padding)
+            // the whole row lies in memory: straight copy
+            const Tin* srow = src + p.src_org + y * p.sst[1] + z * p.sst[2];
+            for (int64_t x = g.xa + lane; x < g.xb; x += 32) brow[x - o.x0] = srow[x];
+            continue;
+        }
+        for (int64_t x = g.xa + lane; x < g.xb; x += 32) {
+            if (only_outside && row_in && x >= 0 && x < p.n[0]) continue;
+            brow[x - o.x0] = load_bounded<Tin>(p, x, y, z);
+        }
     }
 }
 
