@@ -54,7 +54,8 @@ typedef enum {
     STC_ERR_NO_DEVICE = -8,       /* no usable sm_100-family GPU */
     STC_ERR_BUDGET = -9,          /* request exceeds the server's HBM budget */
     STC_ERR_BUSY = -10,           /* result not ready / queue full */
-    STC_ERR_CANCELLED = -11       /* job was cancelled before it finished */
+    STC_ERR_CANCELLED = -11,      /* job was cancelled before it finished */
+    STC_ERR_TOO_LARGE = -12       /* grid larger than the fixed scratch of stc_life_steps_noalloc */
 } stc_status;
 
 /* ---- element types ---- */
@@ -167,6 +168,24 @@ STC_API int stc_update_boundary(const stc_grid* parent, int32_t radius, const st
 
 /* FP64 total of the logical grid (Neumaier-compensated; radius/bc.padding locate the interior). */
 STC_API int stc_mass(const stc_grid* g, int32_t radius, const stc_bc* bc, double* out_total, void* stream);
+
+/* ---- no-allocation variant of the bit-packed Life path ----
+ * No counterpart in the reference.  For callers that must not allocate device memory: code running
+ * inside a stream capture or a caller-managed memory pool, embedded hosts that own every byte of the
+ * device, or a Julia/C host whose allocator must stay the only one.  It runs the same bit-packed,
+ * temporally blocked Moore(1) kernels as stc_map_steps, but keeps the packed copies in a fixed
+ * device array that is part of the library image (4 MiB, held on every GPU that loads the library
+ * until the process exits) instead of allocating them.  The caller still owns and passes both
+ * parents.  Accepts only what that path runs: a 2D Moore(1) LIFE rule, UInt8/Bool/Int32/Int64
+ * grids whose width is a multiple of 32 cells, Wrap or Remove(0), at most 4096*4096 logical cells
+ * (larger grids return STC_ERR_TOO_LARGE, other inputs STC_ERR_UNSUPPORTED).  The first call on a
+ * device looks up the array's device address, so make that first call before any stream capture.
+ * All calls share the one array: calls whose work overlaps on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller.  Same results and parent switching as
+ * stc_map_steps. */
+STC_API int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, const stc_stencil* stencil,
+                                   const stc_op* op, const stc_bc* bc, int64_t nsteps,
+                                   int32_t* out_src_is_b, void* stream);
 
 /* ---- tracing: per-launch device time from CUDA events on the launching stream ---- */
 /* Enable (1) or disable (0) recording; enabling clears earlier records.  No counterpart in the

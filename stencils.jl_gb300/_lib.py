@@ -54,6 +54,8 @@ def load(path: str | Path | None = None):
                            P(C.c_int32), vp, C.c_uint32], C.c_int),
         "stc_update_boundary": ([P(A.Grid), C.c_int32, P(A.BcDesc), vp, C.c_uint32], C.c_int),
         "stc_mass": ([P(A.Grid), C.c_int32, P(A.BcDesc), P(C.c_double), vp], C.c_int),
+        "stc_life_steps_noalloc": ([P(A.Grid), P(A.Grid), P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc), C.c_int64,
+                                    P(C.c_int32), vp], C.c_int),
         "stc_profile_enable": ([C.c_int32], C.c_int),
         "stc_profile_report": ([C.c_char_p, C.c_size_t], C.c_int),
         "stc_batch_create": ([P(vp)], C.c_int),

@@ -387,6 +387,7 @@ const char* stc_strerror(int status) {
     case STC_ERR_BUDGET: return "request exceeds the HBM budget";
     case STC_ERR_BUSY: return "not finished";
     case STC_ERR_CANCELLED: return "cancelled";
+    case STC_ERR_TOO_LARGE: return "grid exceeds the fixed no-allocation scratch (4096*4096 cells)";
     }
     return "unknown status";
 }

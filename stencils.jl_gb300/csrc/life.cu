@@ -15,6 +15,7 @@
 // The neighbour count is the count of nonzero neighbours, exactly what the LIFE op counts, so the
 // result is bit-identical to the per-cell gather for any input values.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -329,3 +330,142 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
 }
 
 }  // namespace stc
+
+// ------------------------------------------------------------------ no-allocation variant
+// stc_life_steps_noalloc: the same packed kernels with the two packed copies in a fixed array that
+// is part of the library image, for callers that cannot allocate device memory (see the header).
+namespace stc {
+
+constexpr int64_t kNoAllocMaxCells = 4096ll * 4096ll;
+constexpr int64_t kNoAllocWords = kNoAllocMaxCells / 32;   // one packed copy
+
+// Two packed copies, 4 MiB in total.  In host code this name is only a stand-in for the device
+// array; the kernels get its device address from cudaGetSymbolAddress.
+static __device__ __align__(256) uint32_t g_noalloc_scratch[2 * kNoAllocWords];
+
+static std::mutex g_noalloc_mu;
+static uint32_t* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(int dev, uint32_t** out) {
+    if (dev < 0 || dev >= 64) return STC_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);   // current device is `dev`
+        if (e != cudaSuccess) return cuda_fail(e);
+        g_noalloc_ptr[dev] = (uint32_t*)ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return STC_OK;
+}
+
+template <class T>
+static void noalloc_pack(bool pack, const PackParams& p, int blocks, cudaStream_t s) {
+    if (pack) life_pack_kernel<T><<<blocks, 256, 0, s>>>(p);
+    else life_unpack_kernel<T><<<blocks, 256, 0, s>>>(p);
+}
+
+static int noalloc_pack_launch(bool pack, const stc_grid* g, int64_t org, int W, int n1, uint32_t* P,
+                               cudaStream_t s, int num_sms) {
+    PackParams p{};
+    p.base = g->data;
+    p.org = org;
+    p.sy = g->stride[1];
+    p.dt = g->dtype;
+    p.W = W;
+    p.n1 = n1;
+    p.P = P;
+    const int64_t groups = (int64_t)n1 * ((W + 31) / 32);
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((groups * 32 + 255) / 256, (int64_t)num_sms * 8));
+    switch (g->dtype) {
+    case STC_U8: case STC_BOOL: noalloc_pack<uint8_t>(pack, p, blocks, s); break;
+    case STC_I32: noalloc_pack<int32_t>(pack, p, blocks, s); break;
+    case STC_I64: noalloc_pack<int64_t>(pack, p, blocks, s); break;
+    default: return STC_ERR_UNSUPPORTED;
+    }
+    return cuda_fail(cudaGetLastError());
+}
+
+}  // namespace stc
+
+extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, const stc_stencil* st,
+                                      const stc_op* op, const stc_bc* bc, int64_t nsteps, int32_t* out_src_is_b,
+                                      void* stream) {
+    using namespace stc;
+    if (nsteps < 0) return STC_ERR_INVALID;
+    int rc = validate_map(a, b, 1, st, op, bc);
+    if (rc) return rc;
+    for (int d = 0; d < a->ndims; ++d)
+        if (a->size[d] != b->size[d] || a->dtype != b->dtype) return STC_ERR_SIZE_MISMATCH;
+    if (op->code != STC_OP_LIFE || a->ndims != 2 || !is_moore1_2d(st)) return STC_ERR_UNSUPPORTED;
+    if (!(a->dtype == STC_U8 || a->dtype == STC_BOOL || a->dtype == STC_I32 || a->dtype == STC_I64))
+        return STC_ERR_UNSUPPORTED;
+    const bool halo = bc->padding != STC_CONDITIONAL;
+    const bool wrap = bc->boundary == STC_WRAP;
+    const bool remove0 = bc->boundary == STC_REMOVE && bc->padval_int == 0;
+    if (!wrap && !remove0) return STC_ERR_UNSUPPORTED;
+    const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
+    if (n0 < 32 || n0 % 32 != 0 || n1 < 1) return STC_ERR_UNSUPPORTED;
+    if (n0 * n1 > kNoAllocMaxCells) return STC_ERR_TOO_LARGE;
+    if (nsteps > 0 && a->data == b->data) return STC_ERR_INVALID;
+    if (nsteps == 0) {
+        if (out_src_is_b) *out_src_is_b = 0;
+        return STC_OK;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { cuda_fail(e); return STC_ERR_NO_DEVICE; }
+    int num_sms = 0, smem_optin = 0;
+    if ((e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return cuda_fail(e);
+    if ((e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess)
+        return cuda_fail(e);
+    uint32_t* P = nullptr;
+    if ((rc = noalloc_scratch(dev, &P))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int W = (int)(n0 / 32);
+    const int smem_cap = smem_optin - 1024;
+    int TB, k;
+    life_plan(W, (int)n1, nsteps, smem_cap, num_sms, &TB, &k);
+    if ((int64_t)2 * (TB + 2 * k) * W * 4 > smem_cap) return STC_ERR_UNSUPPORTED;
+    uint32_t* Pbuf[2] = {P, P + kNoAllocWords};
+    const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
+    if ((rc = noalloc_pack_launch(true, a, org_a, W, (int)n1, Pbuf[0], s, num_sms))) return rc;
+    LifeParams lp{};
+    lp.W = W;
+    lp.n1 = (int)n1;
+    lp.wrap = wrap;
+    lp.birth = op->birth_mask;
+    lp.survive = op->survive_mask;
+    const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
+    int cur = 0;
+    int64_t left = nsteps;
+    while (left > 0) {
+        const int64_t budget = left > 1 ? left - 1 : 1;
+        life_plan(W, (int)n1, budget, smem_cap, num_sms, &TB, &k);
+        lp.in = Pbuf[cur];
+        lp.out = Pbuf[1 - cur];
+        lp.TB = TB;
+        lp.k = k;
+        const size_t smem = (size_t)2 * (TB + 2 * k) * W * 4;
+        const int grid = (int)((n1 + TB - 1) / TB);
+        if (conway) {
+            cudaFuncSetAttribute(life_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            life_block_kernel<true><<<grid, kLifeThreads, smem, s>>>(lp);
+        } else {
+            cudaFuncSetAttribute(life_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            life_block_kernel<false><<<grid, kLifeThreads, smem, s>>>(lp);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e);
+        cur = 1 - cur;
+        left -= k;
+    }
+    const bool res_in_b = (nsteps & 1) != 0;
+    const stc_grid* res = res_in_b ? b : a;
+    const stc_grid* prev = res_in_b ? a : b;
+    if ((rc = noalloc_pack_launch(false, res, res_in_b ? org_b : org_a, W, (int)n1, Pbuf[cur], s, num_sms))) return rc;
+    if (nsteps > 1 &&
+        (rc = noalloc_pack_launch(false, prev, res_in_b ? org_a : org_b, W, (int)n1, Pbuf[1 - cur], s, num_sms)))
+        return rc;
+    if (out_src_is_b) *out_src_is_b = res_in_b ? 1 : 0;
+    return cuda_fail(cudaStreamSynchronize(s));
+}
