@@ -239,6 +239,37 @@ static bool table_is_shape(const stc_stencil* st, int grid_ndims) {
     return std::memcmp(t.data(), st->offsets, t.size() * sizeof(int)) == 0;
 }
 
+// ---------------------------------------------------------------------------- exact division by L
+// The Float32 quotient path q' = RN(q + RN(a - q*L)*r), q = RN(a*r), r = RN(1/L) is used for a given L
+// only if it equals the correctly rounded a / L for every mantissa of the binade [1, 2): the kernels'
+// guard keeps intermediates normal, where the pattern repeats in every binade.  The reference quotient
+// is computed in double and rounded once more to float, which is exact for division (53 >= 2*24+2).
+static bool fastdiv_f_exact(int L) {
+    static std::mutex mu;
+    static std::map<int, bool> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(L);
+    if (it != cache.end()) return it->second;
+    const float r = (float)(1.0 / (double)L);
+    const float fl = (float)L;
+    bool ok = L > 0;
+    for (uint32_t m = 0; ok && m < (1u << 23); ++m) {
+        const uint32_t bits = 0x3f800000u | m;
+        float a;
+        std::memcpy(&a, &bits, 4);
+        volatile float q = a * r;
+        const float e = std::fmaf(-q, fl, a);
+        const float q2 = std::fmaf(e, r, q);
+        const float want = (float)((double)a / (double)L);
+        uint32_t u1, u2;
+        std::memcpy(&u1, &q2, 4);
+        std::memcpy(&u2, &want, 4);
+        ok = u1 == u2;
+    }
+    cache[L] = ok;
+    return ok;
+}
+
 // ---------------------------------------------------------------------------- planning
 static inline int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 static inline int64_t align_up(int64_t a, int64_t b) { return cdiv(a, b) * b; }
@@ -265,6 +296,10 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     p.boundary = bc->boundary;
     p.status = ctx->status;
     p.L = st->len;
+    p.rcp_f = (float)(1.0 / (double)st->len);
+    p.rcp_d = 1.0 / (double)st->len;
+    p.fastdiv_f = (op->code == STC_OP_MEAN && !is_float_dtype(src->dtype)) ? 0
+                  : (op->code == STC_OP_MEAN && src->dtype != STC_F64) ? (int)fastdiv_f_exact(st->len) : 0;
     p.birth = op->birth_mask;
     p.survive = op->survive_mask;
     p.alpha = op->alpha;
@@ -339,7 +374,7 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
         for (int d = 1; d < nd; ++d) gstr[d - 1] = (cuuint64_t)(src->stride[d] * es);
         CUresult r = encoder()(&p.tmap, tma_dtype(src->dtype), (cuuint32_t)nd, src->data, gdim, gstr, box, est,
                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) tma = false;
     }
     p.use_tma = tma;

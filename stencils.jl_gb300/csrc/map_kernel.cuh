@@ -55,6 +55,9 @@ struct MapParams {
     int32_t* status;
     int32_t L;
     uint32_t birth, survive;
+    float rcp_f;               // RN(1/L) in float, used when fastdiv_f (host-verified exact for this L)
+    int32_t fastdiv_f;
+    double rcp_d;              // RN(1/L) in double; every quotient is verified by its residual
     int8_t off[STC_MAX_LEN][3];
     float wf[STC_MAX_LEN];
     double w[STC_MAX_LEN];
@@ -64,14 +67,45 @@ struct MapParams {
 // Each op: Acc type; first(v) = Base.reduce_first; step(a, v, k); finish(a, centre).
 // KDOT starts from zero and steps every term (src/stencils/kernel.jl:264-270).
 
+// Correctly rounded a / L with L a small positive integer.
+// Float32: q = RN(a*r), e = a - q*L (exact by FMA), q' = RN(q + e*r) with r = RN(1/L).  The host enables
+// this only after checking, for this L, that q' equals the correctly rounded quotient for every
+// mantissa of one binade; the result pattern repeats in every binade while the intermediates stay
+// normal, hence the |a| >= 2^-90 guard.  Otherwise the IEEE division is used.
+template <class P> __device__ __forceinline__ float div_by_len(float a, const P& p) {
+    if (p.fastdiv_f && fabsf(a) >= 0x1p-90f && fabsf(a) <= 3.0e38f) {
+        const float q = __fmul_rn(a, p.rcp_f);
+        const float e = __fmaf_rn(-q, (float)p.L, a);
+        return __fmaf_rn(e, p.rcp_f, q);
+    }
+    return __fdiv_rn(a, (float)p.L);
+}
+// Float64: the same corrected quotient q1, accepted only when its exact residual a - q1*L proves it is
+// the correctly rounded a / L (|residual| < L * ulp(q1) / 4, conservative at binade edges);
+// otherwise the IEEE division.
+template <class P> __device__ __forceinline__ double div_by_len(double a, const P& p) {
+    const double L = (double)p.L;
+    const double fa = fabs(a);
+    if (fa >= 0x1p-900 && fa <= 0x1p+1000) {
+        const double q = __dmul_rn(a, p.rcp_d);
+        const double e = __fma_rn(-q, L, a);
+        const double q1 = __fma_rn(e, p.rcp_d, q);
+        const double e1 = __fma_rn(-q1, L, a);
+        const int ex = (int)((__double_as_longlong(q1) >> 52) & 0x7ff);
+        const double ulp = __longlong_as_double((long long)(ex - 52) << 52);   // 2^(exp-52), ex > 52 here
+        if (fabs(e1) < __dmul_rn(L, ulp) * 0.25) return q1;
+    }
+    return __ddiv_rn(a, L);
+}
+
 template <class Tin, class Tout, class Acc> struct OpMean {
     static constexpr bool kZeroInit = false, kNeedsCentre = false;
     using A = Acc;
     __device__ static A first(Tin v, int) { return conv(v); }
-    __device__ static A step(A a, Tin v, int, const MapParams&) { return add(a, conv(v)); }
-    __device__ static Tout finish(A a, Tin, const MapParams& p) {
-        if constexpr (sizeof(A) == 8) return from_f64<Tout>(__ddiv_rn(a, (double)p.L));
-        else return from_f32<Tout>(__fdiv_rn(a, (float)p.L));
+    template <class P> __device__ static A step(A a, Tin v, int, const P&) { return add(a, conv(v)); }
+    template <class P> __device__ static Tout finish(A a, Tin, const P& p) {
+        if constexpr (sizeof(A) == 8) return from_f64<Tout>(div_by_len(a, p));
+        else return from_f32<Tout>(div_by_len(a, p));
     }
     __device__ static A conv(Tin v) {
         if constexpr (sizeof(A) == 8) return cvt_d(v); else return cvt_f(v);
@@ -85,10 +119,10 @@ template <class Tin, class Tout, class Acc> struct OpSumF {
     static constexpr bool kZeroInit = false, kNeedsCentre = false;
     using A = Acc;
     __device__ static A first(Tin v, int) { return OpMean<Tin, Tout, Acc>::conv(v); }
-    __device__ static A step(A a, Tin v, int, const MapParams&) {
+    template <class P> __device__ static A step(A a, Tin v, int, const P&) {
         return OpMean<Tin, Tout, Acc>::add(a, OpMean<Tin, Tout, Acc>::conv(v));
     }
-    __device__ static Tout finish(A a, Tin, const MapParams&) {
+    template <class P> __device__ static Tout finish(A a, Tin, const P&) {
         if constexpr (sizeof(A) == 8) return from_f64<Tout>(a); else return from_f32<Tout>(a);
     }
 };
@@ -98,10 +132,10 @@ template <class Tin, class Tout, int ACC_DT> struct OpSumI {
     static constexpr bool kZeroInit = false, kNeedsCentre = false;
     using A = int64_t;
     __device__ static A first(Tin v, int) { return cvt_i(v); }
-    __device__ static A step(A a, Tin v, int, const MapParams&) {
+    template <class P> __device__ static A step(A a, Tin v, int, const P&) {
         return wrap_int<ACC_DT>((int64_t)((uint64_t)a + (uint64_t)cvt_i(v)));
     }
-    __device__ static Tout finish(A a, Tin, const MapParams&) { return (Tout)a; }
+    template <class P> __device__ static Tout finish(A a, Tin, const P&) { return (Tout)a; }
 };
 
 // kernelproduct in f64: product and sum rounded separately (no FMA), as the reference
@@ -109,10 +143,10 @@ template <class Tin, class Tout> struct OpKdotD {
     static constexpr bool kZeroInit = true, kNeedsCentre = false;
     using A = double;
     __device__ static A first(Tin v, int) { return 0.0; }
-    __device__ static A step(A a, Tin v, int k, const MapParams& p) {
+    template <class P> __device__ static A step(A a, Tin v, int k, const P& p) {
         return __dadd_rn(a, __dmul_rn(cvt_d(v), p.w[k]));
     }
-    __device__ static Tout finish(A a, Tin, const MapParams&) { return from_f64<Tout>(a); }
+    template <class P> __device__ static Tout finish(A a, Tin, const P&) { return from_f64<Tout>(a); }
 };
 
 // kernelproduct with f32 accumulation: fused multiply-add (tolerance path, error vs FP64 stated)
@@ -120,19 +154,19 @@ template <class Tin, class Tout> struct OpKdotF {
     static constexpr bool kZeroInit = true, kNeedsCentre = false;
     using A = float;
     __device__ static A first(Tin v, int) { return 0.0f; }
-    __device__ static A step(A a, Tin v, int k, const MapParams& p) { return fmaf(cvt_f(v), p.wf[k], a); }
-    __device__ static Tout finish(A a, Tin, const MapParams&) { return from_f32<Tout>(a); }
+    template <class P> __device__ static A step(A a, Tin v, int k, const P& p) { return fmaf(cvt_f(v), p.wf[k], a); }
+    template <class P> __device__ static Tout finish(A a, Tin, const P&) { return from_f32<Tout>(a); }
 };
 
 template <class Tin, class Tout, class Acc, bool MAX> struct OpMinMaxF {
     static constexpr bool kZeroInit = false, kNeedsCentre = false;
     using A = Acc;
     __device__ static A first(Tin v, int) { return OpMean<Tin, Tout, Acc>::conv(v); }
-    __device__ static A step(A a, Tin v, int, const MapParams&) {
+    template <class P> __device__ static A step(A a, Tin v, int, const P&) {
         A b = OpMean<Tin, Tout, Acc>::conv(v);
         return MAX ? jl_max(a, b) : jl_min(a, b);
     }
-    __device__ static Tout finish(A a, Tin, const MapParams&) {
+    template <class P> __device__ static Tout finish(A a, Tin, const P&) {
         if constexpr (sizeof(A) == 8) return from_f64<Tout>(a); else return from_f32<Tout>(a);
     }
 };
@@ -141,19 +175,19 @@ template <class Tin, class Tout, bool MAX> struct OpMinMaxI {
     static constexpr bool kZeroInit = false, kNeedsCentre = false;
     using A = int64_t;
     __device__ static A first(Tin v, int) { return cvt_i(v); }
-    __device__ static A step(A a, Tin v, int, const MapParams&) {
+    template <class P> __device__ static A step(A a, Tin v, int, const P&) {
         A b = cvt_i(v);
         return MAX ? (b > a ? b : a) : (b < a ? b : a);
     }
-    __device__ static Tout finish(A a, Tin, const MapParams&) { return (Tout)a; }
+    template <class P> __device__ static Tout finish(A a, Tin, const P&) { return (Tout)a; }
 };
 
 template <class Tin, class Tout> struct OpLife {
     static constexpr bool kZeroInit = false, kNeedsCentre = true;
     using A = int32_t;
     __device__ static A first(Tin v, int) { return v != (Tin)0; }
-    __device__ static A step(A a, Tin v, int, const MapParams&) { return a + (v != (Tin)0); }
-    __device__ static Tout finish(A a, Tin c, const MapParams& p) {
+    template <class P> __device__ static A step(A a, Tin v, int, const P&) { return a + (v != (Tin)0); }
+    template <class P> __device__ static Tout finish(A a, Tin c, const P& p) {
         uint32_t mask = (c != (Tin)0) ? p.survive : p.birth;
         return (Tout)((mask >> a) & 1u);
     }
@@ -164,10 +198,10 @@ template <class Tin, class Tout, class Acc> struct OpDiffuse {
     static constexpr bool kZeroInit = false, kNeedsCentre = true;
     using A = Acc;
     __device__ static A first(Tin v, int k) { return OpMean<Tin, Tout, Acc>::conv(v); }
-    __device__ static A step(A a, Tin v, int k, const MapParams& p) {
+    template <class P> __device__ static A step(A a, Tin v, int k, const P& p) {
         return OpMean<Tin, Tout, Acc>::add(a, OpMean<Tin, Tout, Acc>::conv(v));
     }
-    __device__ static Tout finish(A s, Tin cv, const MapParams& p) {
+    template <class P> __device__ static Tout finish(A s, Tin cv, const P& p) {
         if constexpr (sizeof(A) == 8) {
             double c = cvt_d(cv);
             double t = __dmul_rn((double)p.L, c);
@@ -345,11 +379,12 @@ __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOr
         const int lz = p.tiles3d ? s : 0;
         const int64_t y = o.y0 + ly, z = o.z0 + lz;
         if (y >= p.n[1] || z >= p.n[2]) continue;
+        Tout* drow = dst + p.dst_org + y * p.dstr[1] + z * p.dstr[2] + o.x0;
+        const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0);
 #pragma unroll
         for (int i = 0; i < XT; ++i) {
             const int lx = lane + 32 * i;
-            const int64_t x = o.x0 + lx;
-            if (x >= p.n[0]) continue;
+            if (lx >= nvx) continue;
             const Tin* c = box + ((lz + p.rz) * p.bh + (ly + p.ry)) * p.bw + (lx + p.padl);
             typename Op::A a;
             int k0 = 0;
@@ -361,82 +396,95 @@ __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOr
             }
             for (int k = k0; k < p.L; ++k)
                 a = Op::step(a, c[(p.off[k][2] * p.bh + p.off[k][1]) * p.bw + p.off[k][0]], k, p);
-            dst[p.dst_org + x + y * p.dstr[1] + z * p.dstr[2]] = Op::finish(a, c[0], p);
+            drow[lx] = Op::finish(a, c[0], p);
         }
     }
 }
 
 // ---------------------------------------------------------------------------- compute: specialised
-// The box is streamed along the stream axis (y for 2D shapes, z for 3D shapes): for every input
-// row/plane r, the values the thread needs are loaded once and folded into each of its VS
-// outputs that uses them.  Rows are visited in increasing order and the generated tables are
-// sorted by (z, y, x), so each output still folds its neighbours in table order.
+// Register-rotation stream along the slowest tiled axis (y for 2D shapes, z for 3D shapes).  The
+// thread owns XT columns (lane + 32 i) and VS consecutive outputs along the stream axis.  Input rows
+// r = 0 .. VS + 2R - 1 are visited once each, in increasing order; row r feeds the outputs
+// s = r - q for q = 0 .. D-1 (D = 2R+1, q = offset row + R).  Output s lives in accumulator slot
+// s mod D; the row loop is a run-time loop unrolled by D, so every slot index, offset and weight is a
+// compile-time constant.  Because rows ascend and the generated tables are sorted by (z, y, x), each
+// output folds its neighbours in table order; it is finished and stored right after its last row.
 template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
 __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrigin& o, const Tin* box) {
     constexpr int N = Sh::kN, R = Sh::kR, L = Sh::L;
-    constexpr int RS = R;                      // halo along the stream axis
-    constexpr int RX = R, RY = (N == 3) ? R : 0;
+    constexpr int D = 2 * R + 1;
+    constexpr int RY = (N == 3) ? R : 0;    // in-plane y halo for 3D shapes
     constexpr auto T = Sh::table;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    static_assert(((N == 3) ? T.o[0].z : T.o[0].y) == -R, "tables start at the lowest stream offset");
     using A = typename Op::A;
-    A acc[XT][VS];
-    Tin ctr[XT][VS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    A acc[XT][D];
+    Tin ctr[XT][D];
 #pragma unroll
     for (int i = 0; i < XT; ++i)
 #pragma unroll
-        for (int s = 0; s < VS; ++s) {
-            if constexpr (Op::kZeroInit) acc[i][s] = Op::first(Tin(0), 0);
-            else acc[i][s] = A(0);
-            ctr[i][s] = Tin(0);
-        }
-    // (y, z) of slot 0 and the box coordinates of its stream origin
-    const int ly0 = (N == 3) ? warp : warp * VS;     // tile-local row of slot 0
-    const int lz0 = 0;
+        for (int q = 0; q < D; ++q) { acc[i][q] = A(0); ctr[i][q] = Tin(0); }
+    // box coordinates of the thread's first stream row and its row within a plane
+    const int by0 = (N == 3) ? (warp + p.ry) : (warp * VS);   // 2D: box row of stream row 0; 3D: fixed row
+    const int bz0 = (N == 3) ? 0 : p.rz;
+    const int nrow = VS + 2 * R;
+    // tile-local extents that hold real outputs (ragged last tiles)
+    const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0);
+    const int nvs = (N == 3) ? (int)min((int64_t)VS, p.n[2] - o.z0) : (int)min((int64_t)VS, p.n[1] - o.y0 - warp * VS);
+    const bool row_ok = (N == 3) ? (o.y0 + warp < p.n[1]) : true;
+    Tout* dst = (Tout*)p.dst;
+    for (int r0 = 0; r0 < nrow; r0 += D) {
 #pragma unroll
-    for (int r = 0; r < VS + 2 * RS; ++r) {
-        // box row/plane index of stream position r
-        const int by = (N == 3) ? (ly0 + p.ry) : (ly0 + r);     // 2D: rows stream; 3D: fixed row
-        const int bz = (N == 3) ? (lz0 + r) : p.rz;             // 3D: planes stream
-        Tin v[XT][2 * RY + 1][2 * RX + 1];
+        for (int u = 0; u < D; ++u) {
+            const int r = r0 + u;
+            if (r >= nrow) break;
+            const int by = (N == 3) ? by0 : by0 + r;
+            const int bz = (N == 3) ? r : bz0;
+            Tin v[XT][2 * RY + 1][D];
 #pragma unroll
-        for (int i = 0; i < XT; ++i)
+            for (int i = 0; i < XT; ++i)
 #pragma unroll
-            for (int yy = 0; yy < 2 * RY + 1; ++yy)
+                for (int yy = 0; yy < 2 * RY + 1; ++yy)
 #pragma unroll
-                for (int xx = 0; xx < 2 * RX + 1; ++xx)
-                    v[i][yy][xx] = box[(bz * p.bh + by + yy - RY) * p.bw + lane + 32 * i + p.padl + xx - RX];
+                    for (int xx = 0; xx < D; ++xx)
+                        v[i][yy][xx] = box[(bz * p.bh + by + yy - RY) * p.bw + lane + 32 * i + p.padl + xx - R];
 #pragma unroll
-        for (int s = 0; s < VS; ++s) {
-            const int ds = r - RS - s;    // stream offset this row contributes at, for slot s
-            if (ds < -RS || ds > RS) continue;
+            for (int q = 0; q < D; ++q) {
+                const int sidx = r - q;               // output fed by this row at offset row q - R
+                if (sidx < 0 || sidx >= VS) continue;
+                const int slot = ((u - q) % D + D) % D;   // == sidx mod D (r0 is a multiple of D)
+                if (Op::kZeroInit && q == 0) {
 #pragma unroll
-            for (int k = 0; k < L; ++k) {
-                const int ko = (N == 3) ? T.o[k].z : T.o[k].y;
-                if (ko != ds) continue;
-                const int oy = (N == 3) ? T.o[k].y : 0;
+                    for (int i = 0; i < XT; ++i) acc[i][slot] = Op::first(Tin(0), 0);
+                }
 #pragma unroll
-                for (int i = 0; i < XT; ++i) {
-                    const Tin val = v[i][oy + RY][T.o[k].x + RX];
-                    if (!Op::kZeroInit && k == 0) acc[i][s] = Op::first(val, 0);
-                    else acc[i][s] = Op::step(acc[i][s], val, k, p);
+                for (int k = 0; k < L; ++k) {
+                    const int ko = (N == 3) ? T.o[k].z : T.o[k].y;
+                    if (ko != q - R) continue;
+                    const int oy = (N == 3) ? T.o[k].y : 0;
+#pragma unroll
+                    for (int i = 0; i < XT; ++i) {
+                        const Tin val = v[i][oy + RY][T.o[k].x + R];
+                        if (!Op::kZeroInit && k == 0) acc[i][slot] = Op::first(val, 0);
+                        else acc[i][slot] = Op::step(acc[i][slot], val, k, p);
+                    }
+                }
+                if (Op::kNeedsCentre && q == R) {
+#pragma unroll
+                    for (int i = 0; i < XT; ++i) ctr[i][slot] = v[i][RY][R];
+                }
+                if (q == D - 1 && sidx < nvs && row_ok) {
+                    // last row of output sidx: finish and store
+                    const int64_t y = o.y0 + ((N == 3) ? warp : warp * VS + sidx);
+                    const int64_t z = o.z0 + ((N == 3) ? sidx : 0);
+                    Tout* drow = dst + p.dst_org + y * p.dstr[1] + z * p.dstr[2] + o.x0;
+#pragma unroll
+                    for (int i = 0; i < XT; ++i) {
+                        const int lx = lane + 32 * i;
+                        if (lx < nvx) drow[lx] = Op::finish(acc[i][slot], ctr[i][slot], p);
+                    }
                 }
             }
-            if (Op::kNeedsCentre && ds == 0) {
-#pragma unroll
-                for (int i = 0; i < XT; ++i) ctr[i][s] = v[i][RY][RX];
-            }
-        }
-    }
-    Tout* dst = (Tout*)p.dst;
-#pragma unroll
-    for (int s = 0; s < VS; ++s) {
-        const int64_t y = o.y0 + ((N == 3) ? warp : warp * VS + s);
-        const int64_t z = o.z0 + ((N == 3) ? s : 0);
-        if (y >= p.n[1] || z >= p.n[2]) continue;
-#pragma unroll
-        for (int i = 0; i < XT; ++i) {
-            const int64_t x = o.x0 + lane + 32 * i;
-            if (x < p.n[0]) dst[p.dst_org + x + y * p.dstr[1] + z * p.dstr[2]] = Op::finish(acc[i][s], ctr[i][s], p);
         }
     }
 }
