@@ -9,15 +9,18 @@ kernels for sm_103a; there is no CPU fallback.
 from .array import (AbstractStencilArray, StencilArray, SwitchingStencilArray, colmajor_empty, colmajor_like,
                     colmajor_zeros, switch, to_device, to_host)
 from ._abi import ArgumentError
+from .batch import Batch
 from .boundary import Conditional, Halo, Reflect, Remove, Use, Wrap
 from .gather import gatherstencil, gatherstencil_, mapstencil, mapstencil_, mass, update_boundary_
 from .ops import Diffusion, LifeRule, kernelproduct, life, maximum, mean, minimum
 from .ops import sum  # noqa: A004
+from .serve import Server
 from .stencil import (AngledCross, Annulus, BackSlash, Cardinal, Circle, Cross, Diamond, ForwardSlash, Horizontal,
                       Kernel, Moore, NamedStencil, Ordinal, Positional, Rectangle, Stencil, Vertical, VonNeumann,
                       Window)
 
 __all__ = [
+    "Batch", "Server",
     "AbstractStencilArray", "StencilArray", "SwitchingStencilArray", "switch", "colmajor_empty", "colmajor_like",
     "colmajor_zeros", "to_device", "to_host", "ArgumentError", "Conditional", "Halo", "Reflect", "Remove", "Use",
     "Wrap", "gatherstencil", "gatherstencil_", "mapstencil", "mapstencil_", "mass", "update_boundary_",

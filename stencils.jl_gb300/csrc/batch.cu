@@ -1,0 +1,678 @@
+// batch.cu — K5: many independent SwitchingStencilArray loops in one persistent, graph-captured launch.
+//
+// No counterpart in the reference (each job there is its own `A = mapstencil!(f, A)` loop,
+// src/gatherstencil.jl:77-83).  A job is (two parents, stencil, reduction, boundary, steps); the batch
+// runs every job to completion in one launch:
+//   * A grid that fits in shared memory twice runs resident: one CTA loads it with a ring of R cells,
+//     performs every step in shared memory (refreshing the ring from the interior for Wrap, padval for
+//     Remove), and writes the result once.
+//   * Larger grids are split into tiles; a work item advances one tile by k steps (k per job) from a
+//     tile plus a k*R halo in shared memory, the halo's validity shrinking by R per step.  Item
+//     (job, round r) needs every tile of (job, round r-1): a per-(job, round) counter in global memory
+//     polled with a bounded wait.  Items are claimed in one queue from an atomic ticket, round-major,
+//     so the oldest unfinished item's inputs are always complete and the queue cannot deadlock.
+//     Round r reads parent r%2 and writes parent (r+1)%2; reads go through L2 (ld.global.cg) because
+//     other SMs wrote that parent.
+//   * Each cell's fold is the single-map kernel's (the same op structs), so every job's result is
+//     bit-identical to running it alone through stc_map_steps.
+// stc_batch_plan picks (tile, k) per job with an autotuner that times candidates on scratch grids of
+// the job's size class and caches the winner; the launch (counter reset + kernel) is captured into a
+// CUDA graph that stc_batch_run replays.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "batch.h"
+#include "dispatch.h"
+#include "map_kernel.cuh"
+#include "map_launch.cuh"
+#include "profile.h"
+
+namespace stc {
+
+
+
+
+
+
+template <class T> __device__ __forceinline__ T pad_of(const BatchJob& j);
+template <> __device__ __forceinline__ float pad_of<float>(const BatchJob& j) { return j.padf; }
+template <> __device__ __forceinline__ __nv_bfloat16 pad_of<__nv_bfloat16>(const BatchJob& j) {
+    return __float2bfloat16_rn(j.padf);
+}
+template <> __device__ __forceinline__ uint8_t pad_of<uint8_t>(const BatchJob& j) { return (uint8_t)j.padi; }
+
+template <class T> __device__ __forceinline__ T ld_l2(const T* p) { return *(const volatile T*)p; }
+template <> __device__ __forceinline__ float ld_l2<float>(const float* p) { return __ldcg(p); }
+
+__device__ __forceinline__ int wrapi(int i, int n) {
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+template <class T, class Op>
+__device__ __forceinline__ T batch_cell(const T* c, int pw, const int8_t* so, const OpArgs& a) {
+    typename Op::A acc;
+    int k0 = 0;
+    if constexpr (Op::kZeroInit) {
+        acc = Op::first(c[0], 0);
+    } else {
+        acc = Op::first(c[so[1] * pw + so[0]], 0);
+        k0 = 1;
+    }
+    for (int k = k0; k < a.L; ++k) acc = Op::step(acc, c[so[2 * k + 1] * pw + so[2 * k]], k, a);
+    return Op::finish(acc, c[0], a);
+}
+
+// The same fold with a compile-time table (the generated shape), in table order.
+template <class T, class Op, class Sh>
+__device__ __forceinline__ T batch_cell_shape(const T* c, int pw, const OpArgs& a) {
+    constexpr auto Tb = Sh::table;
+    typename Op::A acc;
+    if constexpr (Op::kZeroInit) acc = Op::first(c[0], 0);
+#pragma unroll
+    for (int k = 0; k < Sh::L; ++k) {
+        const T v = c[Tb.o[k].y * pw + Tb.o[k].x];
+        if (!Op::kZeroInit && k == 0) acc = Op::first(v, 0);
+        else acc = Op::step(acc, v, k, a);
+    }
+    return Op::finish(acc, c[0], a);
+}
+
+template <class T, class Op, class Sh>
+__device__ __forceinline__ T batch_fold(const T* c, int pw, const int8_t* so, const OpArgs& a) {
+    if constexpr (Sh::kKind == STC_SHAPE_TABLE) return batch_cell<T, Op>(c, pw, so, a);
+    else return batch_cell_shape<T, Op, Sh>(c, pw, a);
+}
+
+// Advance one tile of one job by it.steps steps (the whole grid when resident).
+template <class T, class Op, class Sh>
+__device__ void batch_item(const BatchJob& j, const BatchItem& it, unsigned char* smem, const int8_t* so,
+                           const OpArgs& oa) {
+    const int R = j.R;
+    const int steps = it.steps;
+    int x0, y0, tw, th, pad;
+    if (j.resident) {
+        x0 = 0; y0 = 0; tw = j.n0; th = j.n1; pad = R;
+    } else {
+        x0 = (it.tile % j.ntx) * j.tw; y0 = (it.tile / j.ntx) * j.th;
+        tw = j.tw; th = j.th; pad = steps * R;
+    }
+    const int pw = tw + 2 * pad, ph = th + 2 * pad;
+    T* b0 = (T*)smem;
+    T* b1 = b0 + (size_t)pw * ph;
+    const int src = j.resident ? 0 : (it.round & 1);
+    const int dstb = j.resident ? (j.nsteps & 1) : ((it.round + 1) & 1);
+    const T* sp = (const T*)j.buf[src] + j.org[src];
+    const T pv = pad_of<T>(j);
+    for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
+        const int bx = i % pw, by = i / pw;
+        int gx = x0 - pad + bx, gy = y0 - pad + by;
+        T v;
+        if (j.boundary == STC_WRAP) {
+            v = ld_l2(sp + (int64_t)wrapi(gy, j.n1) * j.sy[src] + wrapi(gx, j.n0));
+        } else if (gx >= 0 && gx < j.n0 && gy >= 0 && gy < j.n1) {
+            v = ld_l2(sp + (int64_t)gy * j.sy[src] + gx);
+        } else {
+            v = pv;
+        }
+        b0[i] = v;
+    }
+    __syncthreads();
+    for (int g = 0; g < steps; ++g) {
+        const T* in = (g & 1) ? b1 : b0;
+        T* out = (g & 1) ? b0 : b1;
+        const int lx = j.resident ? R : R * (g + 1), ly = lx;
+        const int hx = j.resident ? R + tw : pw - R * (g + 1), hy = j.resident ? R + th : ph - R * (g + 1);
+        const int cw = hx - lx, ch = hy - ly;
+        for (int i = threadIdx.x; i < cw * ch; i += blockDim.x) {
+            const int bx = lx + i % cw, by = ly + i / cw;
+            const int gx = x0 - pad + bx, gy = y0 - pad + by;
+            T v;
+            if (j.boundary != STC_WRAP && (gx < 0 || gx >= j.n0 || gy < 0 || gy >= j.n1)) v = pv;
+            else v = batch_fold<T, Op, Sh>(in + (size_t)by * pw + bx, pw, so, oa);
+            out[(size_t)by * pw + bx] = v;
+        }
+        __syncthreads();
+        if (j.resident && g + 1 < steps) {
+            for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
+                const int bx = i % pw, by = i / pw;
+                if (bx >= R && bx < R + tw && by >= R && by < R + th) continue;
+                out[i] = j.boundary == STC_WRAP ? out[(size_t)(wrapi(by - R, th) + R) * pw + wrapi(bx - R, tw) + R] : pv;
+            }
+            __syncthreads();
+        }
+    }
+    const T* fin = (steps & 1) ? b1 : b0;
+    T* dp = (T*)j.buf[dstb] + j.org[dstb];
+    for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
+        const int tx = i % tw, ty = i / tw;
+        const int gx = x0 + tx, gy = y0 + ty;
+        if (gx < j.n0 && gy < j.n1) dp[(int64_t)gy * j.sy[dstb] + gx] = fin[(size_t)(ty + pad) * pw + tx + pad];
+    }
+}
+
+// reduction types the batched kernel runs
+using OpF_Mean = OpMean<float, float, float>;
+using OpF_Sum = OpSumF<float, float, float>;
+using OpF_Kdot = OpKdotF<float, float>;
+using OpF_Min = OpMinMaxF<float, float, float, false>;
+using OpF_Max = OpMinMaxF<float, float, float, true>;
+using OpF_Diffuse = OpDiffuse<float, float, float>;
+using OpB_Mean = OpMean<__nv_bfloat16, __nv_bfloat16, float>;
+using OpB_Sum = OpSumF<__nv_bfloat16, __nv_bfloat16, float>;
+using OpB_Kdot = OpKdotF<__nv_bfloat16, __nv_bfloat16>;
+using OpB_Diffuse = OpDiffuse<__nv_bfloat16, __nv_bfloat16, float>;
+using OpU_Life = OpLife<uint8_t, uint8_t>;
+using OpU_Sum = OpSumI<uint8_t, uint8_t, STC_U8>;
+
+__global__ void __launch_bounds__(kBatchThreads) batch_kernel(const BatchDev d) {
+    extern __shared__ __align__(16) unsigned char bsm[];
+    __shared__ int s_item;
+    __shared__ int8_t so[2 * kBatchMaxL];
+    __shared__ float sw[kBatchMaxL];
+    while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(d.ticket, 1);
+        __syncthreads();
+        const int ii = s_item;
+        if (ii >= d.nitems || *((volatile int*)d.abort_flag)) return;
+        const BatchItem it = d.items[ii];
+        const BatchJob j = d.jobs[it.job];
+        if (threadIdx.x == 0 && it.round > 0) {
+            volatile int* ctr = d.counters + j.counter_base + it.round - 1;
+            const long long t0 = clock64();
+            while (*ctr < j.tiles) {
+                if (clock64() - t0 > 4000000000ll) {   // ~2 s: give up, flag, and stop the queue
+                    atomicOr(d.status, DEV_ERR_TIMEOUT);
+                    atomicExch(d.abort_flag, 1);
+                    break;
+                }
+                __nanosleep(100);
+            }
+            __threadfence();
+        }
+        for (int i = threadIdx.x; i < j.L; i += blockDim.x) {
+            so[2 * i] = d.offs[2 * (j.off_base + i)];
+            so[2 * i + 1] = d.offs[2 * (j.off_base + i) + 1];
+            sw[i] = d.wts[j.off_base + i];
+        }
+        __syncthreads();
+        if (*((volatile int*)d.abort_flag)) return;
+        OpArgs oa;
+        oa.L = j.L;
+        oa.birth = j.birth;
+        oa.survive = j.survive;
+        oa.alpha = j.alpha;
+        oa.rcp_f = j.rcp_f;
+        oa.fastdiv_f = j.fastdiv_f;
+        oa.rcp_d = j.rcp_d;
+        oa.wf = sw;
+        oa.w = nullptr;
+        const int key = j.dtype * 16 + j.opv;
+#define STC_B(DT, OPV, T, OP)                                                                   \
+    case DT * 16 + OPV:                                                                         \
+        batch_item<T, OP, TableShape>(j, it, bsm, so, oa);                                      \
+        break;
+#define STC_BS(DT, OPV, T, OP, KIND, RR)                                                        \
+    if (key == DT * 16 + OPV && j.shape == KIND && j.R == RR) {                                 \
+        batch_item<T, OP, Shape<KIND, RR, 2>>(j, it, bsm, so, oa);                              \
+        goto item_done;                                                                         \
+    }
+        // compile-time tables for the shapes batched workloads use
+        STC_BS(STC_F32, OPV_MEAN, float, OpF_Mean, STC_SHAPE_WINDOW, 1)
+        STC_BS(STC_F32, OPV_MEAN, float, OpF_Mean, STC_SHAPE_CIRCLE, 3)
+        STC_BS(STC_F32, OPV_SUM, float, OpF_Sum, STC_SHAPE_CROSS, 2)
+        STC_BS(STC_F32, OPV_KDOT_F, float, OpF_Kdot, STC_SHAPE_WINDOW, 2)
+        STC_BS(STC_BF16, OPV_MEAN, __nv_bfloat16, OpB_Mean, STC_SHAPE_WINDOW, 1)
+        STC_BS(STC_BF16, OPV_MEAN, __nv_bfloat16, OpB_Mean, STC_SHAPE_CIRCLE, 3)
+        STC_BS(STC_BF16, OPV_KDOT_F, __nv_bfloat16, OpB_Kdot, STC_SHAPE_WINDOW, 2)
+        STC_BS(STC_U8, OPV_LIFE, uint8_t, OpU_Life, STC_SHAPE_MOORE, 1)
+        switch (key) {
+        STC_B(STC_F32, OPV_MEAN, float, OpF_Mean)
+        STC_B(STC_F32, OPV_SUM, float, OpF_Sum)
+        STC_B(STC_F32, OPV_KDOT_F, float, OpF_Kdot)
+        STC_B(STC_F32, OPV_MIN, float, OpF_Min)
+        STC_B(STC_F32, OPV_MAX, float, OpF_Max)
+        STC_B(STC_F32, OPV_DIFFUSE, float, OpF_Diffuse)
+        STC_B(STC_BF16, OPV_MEAN, __nv_bfloat16, OpB_Mean)
+        STC_B(STC_BF16, OPV_SUM, __nv_bfloat16, OpB_Sum)
+        STC_B(STC_BF16, OPV_KDOT_F, __nv_bfloat16, OpB_Kdot)
+        STC_B(STC_BF16, OPV_DIFFUSE, __nv_bfloat16, OpB_Diffuse)
+        STC_B(STC_U8, OPV_LIFE, uint8_t, OpU_Life)
+        STC_B(STC_U8, OPV_SUM, uint8_t, OpU_Sum)
+        default: break;
+        }
+#undef STC_B
+#undef STC_BS
+    item_done:
+        __syncthreads();
+        if (!j.resident) {
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) atomicAdd(d.counters + j.counter_base + it.round, 1);
+        }
+    }
+}
+
+bool batch_supported(int dtype, int opv) {
+    switch (dtype * 16 + opv) {
+    case STC_F32 * 16 + OPV_MEAN: case STC_F32 * 16 + OPV_SUM: case STC_F32 * 16 + OPV_KDOT_F:
+    case STC_F32 * 16 + OPV_MIN: case STC_F32 * 16 + OPV_MAX: case STC_F32 * 16 + OPV_DIFFUSE:
+    case STC_BF16 * 16 + OPV_MEAN: case STC_BF16 * 16 + OPV_SUM: case STC_BF16 * 16 + OPV_KDOT_F:
+    case STC_BF16 * 16 + OPV_DIFFUSE: case STC_U8 * 16 + OPV_LIFE: case STC_U8 * 16 + OPV_SUM:
+        return true;
+    }
+    return false;
+}
+
+}  // namespace stc
+
+// ====================================================================== host side
+namespace stc {
+
+
+constexpr size_t kResidentSmem = 96 * 1024;   // a grid held twice below this runs resident
+constexpr size_t kTiledSmemCap = 200 * 1024;
+
+static size_t tiled_smem(const BatchSpec& s, const Geometry& g) {
+    const size_t es = dtype_size(s.a.dtype);
+    return 2 * (size_t)(g.tw + 2 * g.k * s.R) * (g.th + 2 * g.k * s.R) * es;
+}
+
+static size_t resident_smem(const BatchSpec& s) {
+    const size_t es = dtype_size(s.a.dtype);
+    return 2 * (size_t)(s.a.size[0] + 2 * s.R) * (s.a.size[1] + 2 * s.R) * es;
+}
+
+using TuneKey = std::tuple<int, int, int, int, int, int>;   // dtype, opv, L, R, boundary, size bucket
+static std::mutex g_tune_mu;
+static std::map<TuneKey, Geometry> g_tune_cache;
+
+static TuneKey tune_key(const BatchSpec& s) {
+    const double cells = (double)s.a.size[0] * (double)s.a.size[1];
+    const int bucket = (int)std::floor(std::log2(std::max(cells, 1.0)));
+    return TuneKey(s.a.dtype, s.opv, s.L, s.R, s.bc.boundary, bucket);
+}
+
+static Geometry default_geometry(const BatchSpec& s) {
+    Geometry g{64, 32, s.R <= 1 ? 4 : (s.R == 2 ? 2 : 1)};
+    g.k = (int)std::max<int64_t>(1, std::min<int64_t>(g.k, s.nsteps));
+    while (g.k > 1 && tiled_smem(s, g) > kTiledSmemCap) --g.k;
+    return g;
+}
+
+}  // namespace stc
+
+namespace stc {
+
+static void release_graph(stc_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+}
+
+static inline size_t align_to(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Build jobs, items and device tables, then capture (counter reset + kernel) as a graph.
+
+static int autotune_spec(const BatchSpec& s, DeviceCtx* ctx, cudaStream_t stream, Geometry* out) {
+    const TuneKey key = tune_key(s);
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) { *out = it->second; return STC_OK; }
+    }
+    const int64_t n0 = s.a.size[0], n1 = s.a.size[1];
+    const size_t es = dtype_size(s.a.dtype);
+    const int64_t steps = std::min<int64_t>(s.nsteps, 16);
+    std::vector<Geometry> cands;
+    const int tws[] = {32, 64, 128};
+    const int ths[] = {16, 32, 64};
+    const int ks[] = {1, 2, 4, 8};
+    for (int tw : tws)
+        for (int th : ths)
+            for (int k : ks) {
+                Geometry g{tw, th, k};
+                if (k > steps || tiled_smem(s, g) > kTiledSmemCap) continue;
+                if (tw * th < 1024 || tw * th > 8192) continue;
+                cands.push_back(g);
+            }
+    if (cands.empty()) { *out = default_geometry(s); return STC_OK; }
+    // enough copies of the job to fill the GPU the way a loaded batch would
+    const int64_t tiles = ((n0 + 63) / 64) * ((n1 + 31) / 32);
+    const int copies = (int)std::max<int64_t>(1, std::min<int64_t>(8, (2 * ctx->num_sms + tiles - 1) / tiles));
+    const size_t gbytes = (size_t)n0 * n1 * es;
+    void* scratch = nullptr;
+    cudaError_t e = cudaMalloc(&scratch, 2 * copies * gbytes);
+    if (e != cudaSuccess) return cuda_fail(e);
+    cudaMemsetAsync(scratch, 0, 2 * copies * gbytes, stream);
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    Geometry best = cands[0];
+    float best_ms = 1e30f;
+    int rc = STC_OK;
+    for (const Geometry& g : cands) {
+        stc_batch trial;
+        for (int c = 0; c < copies; ++c) {
+            BatchSpec t = s;
+            t.nsteps = steps;
+            t.a.data = (char*)scratch + (size_t)(2 * c) * gbytes;
+            t.b.data = (char*)scratch + (size_t)(2 * c + 1) * gbytes;
+            t.a.stride[1] = t.b.stride[1] = n0;
+            t.force_tw = g.tw;
+            t.force_th = g.th;
+            t.force_k = g.k;
+            trial.specs.push_back(t);
+        }
+        if ((rc = batch_build(&trial, false, stream, ctx))) break;
+        float ms = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            cudaEventRecord(t0, stream);
+            cudaGraphLaunch(trial.exec, stream);
+            cudaEventRecord(t1, stream);
+            cudaEventSynchronize(t1);
+            float m = 0.f;
+            cudaEventElapsedTime(&m, t0, t1);
+            if (rep > 0) ms = std::min(ms, m);
+        }
+        batch_free(&trial);
+        if (ms < best_ms) { best_ms = ms; best = g; }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaStreamSynchronize(stream);
+    cudaFree(scratch);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_tune_cache[key] = best;
+    }
+    *out = best;
+    return STC_OK;
+}
+
+int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx, bool capture) {
+    const int nj = (int)b->specs.size();
+    b->hjobs.assign(nj, BatchJob{});
+    b->hitems.clear();
+    b->hoffs.clear();
+    b->hwts.clear();
+    b->result_in_b.assign(nj, 0);
+    b->ncounters = 0;
+    b->planned_cell_steps = 0;
+    size_t smem = 0;
+    int max_rounds = 0;
+    std::vector<BatchItem> resident_items;
+    for (int i = 0; i < nj; ++i) {
+        const BatchSpec& s = b->specs[i];
+        BatchJob& j = b->hjobs[i];
+        j.buf[0] = s.a.data;
+        j.buf[1] = s.b.data;
+        j.org[0] = j.org[1] = 0;
+        j.sy[0] = s.a.stride[1];
+        j.sy[1] = s.b.stride[1];
+        j.n0 = (int32_t)s.a.size[0];
+        j.n1 = (int32_t)s.a.size[1];
+        j.dtype = s.a.dtype;
+        j.opv = s.opv;
+        j.boundary = s.bc.boundary;
+        j.L = s.L;
+        j.R = s.R;
+        j.nsteps = (int32_t)s.nsteps;
+        j.padf = (float)s.bc.padval;
+        j.padi = (int32_t)s.bc.padval_int;
+        j.alpha = s.op.alpha;
+        j.birth = s.op.birth_mask;
+        j.survive = s.op.survive_mask;
+        j.rcp_f = (float)(1.0 / (double)s.L);
+        j.rcp_d = 1.0 / (double)s.L;
+        j.fastdiv_f = (s.opv == OPV_MEAN && s.a.dtype != STC_F64 && is_float_dtype(s.a.dtype)) ? (int)fastdiv_f_exact(s.L) : 0;
+        j.shape = table_matches_shape(s.shape, s.R, 2, s.offs.data(), s.L) ? s.shape : STC_SHAPE_TABLE;
+        j.off_base = (int32_t)(b->hoffs.size() / 2);
+        for (int k = 0; k < s.L; ++k) {
+            b->hoffs.push_back((int8_t)s.offs[2 * k]);
+            b->hoffs.push_back((int8_t)s.offs[2 * k + 1]);
+            b->hwts.push_back(s.wts.empty() ? 0.f : (float)s.wts[k]);
+        }
+        b->planned_cell_steps += (double)j.n0 * j.n1 * s.nsteps;
+        if (s.nsteps == 0) { j.rounds = 0; continue; }
+        const bool forced = s.force_tw > 0;
+        if (!forced && resident_smem(s) <= kResidentSmem) {
+            j.resident = 1;
+            j.tw = j.n0; j.th = j.n1; j.k = j.nsteps;
+            j.ntx = j.nty = j.tiles = 1;
+            j.rounds = 1;
+            smem = std::max(smem, resident_smem(s));
+            resident_items.push_back(BatchItem{i, 0, 0, j.nsteps});
+            b->result_in_b[i] = (int)(s.nsteps & 1);
+            continue;
+        }
+        Geometry g;
+        if (forced) g = Geometry{s.force_tw, s.force_th, s.force_k};
+        else if (autotune) {
+            int rc = autotune_spec(s, ctx, stream, &g);
+            if (rc) return rc;
+        } else {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(tune_key(s));
+            g = it != g_tune_cache.end() ? it->second : default_geometry(s);
+        }
+        g.k = (int)std::max<int64_t>(1, std::min<int64_t>(g.k, s.nsteps));
+        j.resident = 0;
+        j.tw = g.tw; j.th = g.th; j.k = g.k;
+        j.ntx = (j.n0 + g.tw - 1) / g.tw;
+        j.nty = (j.n1 + g.th - 1) / g.th;
+        j.tiles = j.ntx * j.nty;
+        j.rounds = (int32_t)((s.nsteps + g.k - 1) / g.k);
+        j.counter_base = b->ncounters;
+        b->ncounters += j.rounds;
+        smem = std::max(smem, tiled_smem(s, g));
+        max_rounds = std::max(max_rounds, j.rounds);
+        b->result_in_b[i] = j.rounds & 1;
+    }
+    // resident jobs first, longest first, so they overlap the tiled rounds
+    std::sort(resident_items.begin(), resident_items.end(), [&](const BatchItem& x, const BatchItem& y) {
+        const BatchJob &a = b->hjobs[x.job], &c = b->hjobs[y.job];
+        return (double)a.n0 * a.n1 * a.nsteps * a.L > (double)c.n0 * c.n1 * c.nsteps * c.L;
+    });
+    b->hitems = resident_items;
+    for (int r = 0; r < max_rounds; ++r)
+        for (int i = 0; i < nj; ++i) {
+            const BatchJob& j = b->hjobs[i];
+            if (j.resident || r >= j.rounds) continue;
+            const int steps = (int)std::min<int64_t>(j.k, (int64_t)j.nsteps - (int64_t)r * j.k);
+            for (int t = 0; t < j.tiles; ++t) b->hitems.push_back(BatchItem{i, r, t, steps});
+        }
+    // device tables in one block: jobs | items | offs | wts | counters | ticket, abort
+    const size_t s_jobs = align_to(sizeof(BatchJob) * std::max(1, nj), 256);
+    const size_t s_items = align_to(sizeof(BatchItem) * std::max<size_t>(1, b->hitems.size()), 256);
+    const size_t s_offs = align_to(std::max<size_t>(2, b->hoffs.size()), 256);
+    const size_t s_wts = align_to(sizeof(float) * std::max<size_t>(1, b->hwts.size()), 256);
+    const size_t s_ctr = align_to(sizeof(int) * (size_t)(b->ncounters + 2), 256);
+    const size_t total = s_jobs + s_items + s_offs + s_wts + s_ctr;
+    cudaError_t e;
+    if (total > b->dmem_bytes) {
+        if (b->dmem) cudaFree(b->dmem);
+        b->dmem = nullptr;
+        if ((e = cudaMalloc(&b->dmem, total)) != cudaSuccess) return cuda_fail(e);
+        b->dmem_bytes = total;
+    }
+    char* base = (char*)b->dmem;
+    BatchDev& d = b->dev;
+    d.jobs = (const BatchJob*)base;
+    d.items = (const BatchItem*)(base + s_jobs);
+    d.offs = (const int8_t*)(base + s_jobs + s_items);
+    d.wts = (const float*)(base + s_jobs + s_items + s_offs);
+    d.counters = (int*)(base + s_jobs + s_items + s_offs + s_wts);
+    d.ticket = d.counters + b->ncounters;
+    d.abort_flag = d.ticket + 1;
+    d.nitems = (int)b->hitems.size();
+    d.status = ctx->status;
+    if (nj) cudaMemcpyAsync((void*)d.jobs, b->hjobs.data(), sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, stream);
+    if (!b->hitems.empty())
+        cudaMemcpyAsync((void*)d.items, b->hitems.data(), sizeof(BatchItem) * b->hitems.size(), cudaMemcpyHostToDevice, stream);
+    if (!b->hoffs.empty()) cudaMemcpyAsync((void*)d.offs, b->hoffs.data(), b->hoffs.size(), cudaMemcpyHostToDevice, stream);
+    if (!b->hwts.empty())
+        cudaMemcpyAsync((void*)d.wts, b->hwts.data(), sizeof(float) * b->hwts.size(), cudaMemcpyHostToDevice, stream);
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e);
+    // launch shape: persistent CTAs
+    b->smem = std::max<size_t>(smem, 16);
+    if ((e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem)) != cudaSuccess)
+        return cuda_fail(e);
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kBatchThreads, b->smem)) != cudaSuccess)
+        return cuda_fail(e);
+    if (per_sm < 1) return STC_ERR_UNSUPPORTED;
+    b->grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)per_sm * ctx->num_sms, std::max(1, d.nitems)));
+    b->planned = true;
+    if (!capture) return STC_OK;
+    // capture: reset counters and the ticket, run the queue
+    release_graph(b);
+    if (!b->cap_stream && (e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e);
+    if ((e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return cuda_fail(e);
+    cudaMemsetAsync(d.counters, 0, sizeof(int) * (size_t)(b->ncounters + 2), b->cap_stream);
+    if (d.nitems > 0) batch_kernel<<<b->grid, kBatchThreads, b->smem, b->cap_stream>>>(d);
+    if ((e = cudaStreamEndCapture(b->cap_stream, &b->graph)) != cudaSuccess) return cuda_fail(e);
+    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) return cuda_fail(e);
+    return STC_OK;
+}
+
+int batch_launch(stc_batch* b, cudaStream_t stream) {
+    BatchDev& d = b->dev;
+    cudaError_t e = cudaMemsetAsync(d.counters, 0, sizeof(int) * (size_t)(b->ncounters + 2), stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (d.nitems > 0) batch_kernel<<<b->grid, kBatchThreads, b->smem, stream>>>(d);
+    return cuda_fail(cudaGetLastError());
+}
+
+void batch_free(stc_batch* b) {
+    release_graph(b);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    if (b->dmem) cudaFree(b->dmem);
+    b->cap_stream = nullptr;
+    b->dmem = nullptr;
+    b->dmem_bytes = 0;
+}
+
+}  // namespace stc
+
+using namespace stc;
+
+extern "C" {
+
+int stc_batch_create(stc_batch** out) {
+    if (!out) return STC_ERR_INVALID;
+    *out = new stc_batch();
+    return STC_OK;
+}
+
+int stc_batch_destroy(stc_batch* b) {
+    if (!b) return STC_ERR_INVALID;
+    batch_free(b);
+    delete b;
+    return STC_OK;
+}
+
+int stc_batch_add(stc_batch* b, const stc_grid* a, const stc_grid* bg, const stc_stencil* st, const stc_op* op,
+                  const stc_bc* bc, int64_t nsteps) {
+    if (!b || nsteps < 0) return STC_ERR_INVALID;
+    int rc = validate_map(a, bg, 1, st, op, bc);
+    if (rc) return rc;
+    if (a->ndims != 2 || st->ndims != 2 || bc->padding != STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
+    if (!(bc->boundary == STC_REMOVE || bc->boundary == STC_WRAP)) return STC_ERR_UNSUPPORTED;
+    if (st->len > kBatchMaxL || st->radius > kBatchMaxR) return STC_ERR_UNSUPPORTED;
+    for (int d = 0; d < 2; ++d)
+        if (a->size[d] != bg->size[d] || a->dtype != bg->dtype) return STC_ERR_SIZE_MISMATCH;
+    if (a->size[0] < 1 || a->size[1] < 1) return STC_ERR_INVALID;
+    BatchSpec s;
+    s.a = *a;
+    s.b = *bg;
+    s.L = st->len;
+    s.R = st->radius;
+    s.wdt = st->weight_dtype;
+    s.shape = st->shape;
+    s.offs.assign(st->offsets, st->offsets + 2 * st->len);
+    if (st->weights) s.wts.assign(st->weights, st->weights + st->len);
+    s.op = *op;
+    s.bc = *bc;
+    s.nsteps = nsteps;
+    switch (op->code) {
+    case STC_OP_MEAN: s.opv = OPV_MEAN; break;
+    case STC_OP_SUM: s.opv = OPV_SUM; break;
+    case STC_OP_KDOT: s.opv = (a->dtype != STC_F64 && is_float_dtype(a->dtype) && st->weight_dtype == STC_F32) ? OPV_KDOT_F : OPV_KDOT_D; break;
+    case STC_OP_MIN: s.opv = OPV_MIN; break;
+    case STC_OP_MAX: s.opv = OPV_MAX; break;
+    case STC_OP_LIFE: s.opv = OPV_LIFE; break;
+    case STC_OP_DIFFUSE: s.opv = OPV_DIFFUSE; break;
+    default: return STC_ERR_UNSUPPORTED;
+    }
+    if (!batch_supported(a->dtype, s.opv)) return STC_ERR_UNSUPPORTED;
+    b->specs.push_back(s);
+    b->planned = false;
+    return (int)b->specs.size() - 1;
+}
+
+int stc_batch_plan(stc_batch* b, int32_t autotune, void* stream) {
+    if (!b) return STC_ERR_INVALID;
+    DeviceCtx* ctx = nullptr;
+    int rc = device_ctx(&ctx);
+    if (rc) return rc;
+    return batch_build(b, autotune != 0, (cudaStream_t)stream, ctx);
+}
+
+int stc_batch_run(stc_batch* b, void* stream, uint32_t flags) {
+    if (!b) return STC_ERR_INVALID;
+    DeviceCtx* ctx = nullptr;
+    int rc = device_ctx(&ctx);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!b->planned && (rc = batch_build(b, false, s, ctx))) return rc;
+    void* prof = prof_begin(s);
+    cudaError_t e = cudaGraphLaunch(b->exec, s);
+    double bytes = 0;
+    for (const BatchSpec& sp : b->specs) bytes += 2.0 * dtype_size(sp.a.dtype) * sp.a.size[0] * sp.a.size[1] * sp.nsteps;
+    prof_end(prof, s, "batch_kernel", bytes, b->planned_cell_steps);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (!(flags & STC_ASYNC)) {
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e);
+        volatile int* h = ctx->status_host;
+        if (*h) { *h = 0; return STC_ERR_TIMEOUT; }
+    }
+    return STC_OK;
+}
+
+int stc_batch_result(const stc_batch* b, int32_t idx, int32_t* out_src_is_b) {
+    if (!b || !out_src_is_b || idx < 0 || idx >= (int)b->specs.size()) return STC_ERR_INVALID;
+    if (!b->planned) return STC_ERR_BUSY;
+    *out_src_is_b = b->result_in_b[idx];
+    return STC_OK;
+}
+
+int stc_batch_run_sequential(stc_batch* b, void* stream) {
+    if (!b) return STC_ERR_INVALID;
+    for (const BatchSpec& s : b->specs) {
+        stc_stencil st{};
+        st.ndims = 2;
+        st.len = s.L;
+        st.radius = s.R;
+        st.shape = s.shape;
+        st.offsets = s.offs.data();
+        st.weights = s.wts.empty() ? nullptr : s.wts.data();
+        st.weight_dtype = s.wdt;
+        int32_t in_b = 0;
+        int rc = stc_map_steps(&s.a, &s.b, &st, &s.op, &s.bc, s.nsteps, &in_b, stream, 0);
+        if (rc) return rc;
+    }
+    return STC_OK;
+}
+
+}  // extern "C"

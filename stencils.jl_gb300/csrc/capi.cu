@@ -231,12 +231,17 @@ static void generate_shape(int kind, int R, int N, std::vector<int>& out) {
             }
 }
 
-static bool table_is_shape(const stc_stencil* st, int grid_ndims) {
-    if (st->shape == STC_SHAPE_TABLE || st->ndims != grid_ndims) return false;
+bool table_matches_shape(int shape, int R, int N, const int32_t* offsets, int len) {
+    if (shape == STC_SHAPE_TABLE) return false;
     std::vector<int> t;
-    generate_shape(st->shape, st->radius, st->ndims, t);
-    if ((int)t.size() != st->len * st->ndims) return false;
-    return std::memcmp(t.data(), st->offsets, t.size() * sizeof(int)) == 0;
+    generate_shape(shape, R, N, t);
+    if ((int)t.size() != len * N) return false;
+    return std::memcmp(t.data(), offsets, t.size() * sizeof(int)) == 0;
+}
+
+static bool table_is_shape(const stc_stencil* st, int grid_ndims) {
+    if (st->ndims != grid_ndims) return false;
+    return table_matches_shape(st->shape, st->radius, st->ndims, st->offsets, st->len);
 }
 
 // ---------------------------------------------------------------------------- exact division by L
@@ -244,7 +249,7 @@ static bool table_is_shape(const stc_stencil* st, int grid_ndims) {
 // only if it equals the correctly rounded a / L for every mantissa of the binade [1, 2): the kernels'
 // guard keeps intermediates normal, where the pattern repeats in every binade.  The reference quotient
 // is computed in double and rounded once more to float, which is exact for division (53 >= 2*24+2).
-static bool fastdiv_f_exact(int L) {
+bool fastdiv_f_exact(int L) {
     static std::mutex mu;
     static std::map<int, bool> cache;
     std::lock_guard<std::mutex> g(mu);

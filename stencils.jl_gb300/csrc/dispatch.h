@@ -49,6 +49,10 @@ int cuda_fail(cudaError_t e);
 int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
                  const stc_op* op, const stc_bc* bc);
 int result_dtype(int op, int sdt, int wdt);
+// true if the FMA-corrected Float32 quotient by L is exact for every input (checked once per L)
+bool fastdiv_f_exact(int L);
+// true if `offsets` (len entries of N components) is the table Stencils.jl generates for the shape
+bool table_matches_shape(int shape, int R, int N, const int32_t* offsets, int len);
 // one map launch (halo fill not included), no synchronisation
 int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st, const stc_op* op,
                const stc_bc* bc, cudaStream_t stream, DeviceCtx* ctx);

@@ -1,0 +1,88 @@
+"""Serving: continuous batching of stencil jobs with device-resident state (stc_server_* in the C ABI).
+
+No counterpart in the reference.  Jobs are host grids (numpy, Julia axis order); the server admits
+them by an HBM budget, keeps their state on the GPU across batched ticks, and returns each result
+with its latency from submission.  Each result equals running the job alone.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from . import _lib
+from .boundary import Conditional
+from .ops import as_reduction
+
+
+class Server:
+    def __init__(self, hbm_fraction: float = 0.8, steps_per_tick: int = 16):
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        _lib.check(self._lib.stc_server_create(C.byref(h), float(hbm_fraction), int(steps_per_tick)),
+                   "stc_server_create")
+        self._h = h
+        self._meta = {}
+
+    def submit(self, grid: np.ndarray, stencil, f, boundary, steps: int, code: int | None = None) -> int:
+        """Queue `steps` iterations of mapstencil_(f, ·) on a copy of `grid` (2D, Julia axis order).
+        `code` overrides the element type (A.BF16 for bfloat16 bit patterns held as uint16)."""
+        red = as_reduction(f)
+        a = np.asfortranarray(grid)
+        code = A.numpy_dtype_code(a.dtype) if code is None else code
+        job = A.JobDesc()
+        job.grid = A.grid_from_numpy(a, code)
+        st = A.LoweredStencil(stencil)
+        job.stencil = st.desc
+        job.op = A.lower_op(red)
+        job.bc = A.lower_bc(boundary, Conditional())
+        job.nsteps = int(steps)
+        out = C.c_int64(0)
+        _lib.check(self._lib.stc_server_submit(self._h, C.byref(job), C.byref(out)), "stc_server_submit")
+        self._meta[out.value] = (a.shape, a.dtype, code)
+        return out.value
+
+    def poll(self, job_id: int) -> bool:
+        rc = self._lib.stc_server_poll(self._h, job_id)
+        if rc < 0:
+            _lib.check(rc, "stc_server_poll")
+        return rc == 1
+
+    def fetch(self, job_id: int):
+        """(result array, latency in seconds); raises StencilError(BUSY) if not finished."""
+        shape, dtype, code = self._meta[job_id]
+        out = np.empty(shape, dtype=dtype, order="F")
+        lat = C.c_double(0.0)
+        _lib.check(self._lib.stc_server_fetch(self._h, job_id, out.ctypes.data_as(C.c_void_p), out.nbytes,
+                                              C.byref(lat)), "stc_server_fetch")
+        del self._meta[job_id]
+        return out, lat.value
+
+    def cancel(self, job_id: int):
+        _lib.check(self._lib.stc_server_cancel(self._h, job_id), "stc_server_cancel")
+
+    def drain(self, timeout_s: float = 60.0):
+        _lib.check(self._lib.stc_server_drain(self._h, float(timeout_s)), "stc_server_drain")
+
+    def stats(self) -> dict:
+        v = [C.c_int64(0) for _ in range(4)]
+        _lib.check(self._lib.stc_server_stats(self._h, *[C.byref(x) for x in v]), "stc_server_stats")
+        return {"admitted": v[0].value, "finished": v[1].value, "ticks": v[2].value, "peak_bytes": v[3].value}
+
+    def close(self):
+        if self._h:
+            self._lib.stc_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # pragma: no cover
+            pass
