@@ -313,6 +313,312 @@ def run_gpu(args):
     return 0
 
 
+# ------------------------------------------------------------------ other BASELINE configurations
+def _timed_steps(fn, steps, warmup, flush):
+    """Device time of `steps` calls of fn(), L2 flushed (outside the timing) before each."""
+    import torch
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1) / 1e3
+    return total
+
+
+def _kernel_roofline(prof, peak_gbs):
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    k = dom[1]
+    ach = k["alg_bytes"] / (k["ms"] / 1e3) / 1e9
+    return {"kernel": dom[0], "achieved_gbs": ach, "frac_of_measured_hbm": ach / peak_gbs,
+            "avg_launch_us": 1e3 * k["ms"] / k["launches"], "gcell_s": k["updates"] / (k["ms"] / 1e3) / 1e9}
+
+
+def _peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(f.read_text()) if f.exists() else {"hbm_gbs": 6800.0}
+
+
+def run_mean_blur(args):
+    """Config 1: mapstencil(mean, StencilArray(rand(1000,1000), Window(1))), Float64, Remove(0.0),
+    Conditional, one map per step; device time per map with L2 flushed before each."""
+    import torch
+    entry.build()
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    from oracle import oracle as orc
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    rng = np.random.Generator(np.random.PCG64(1))
+    a = np.asfortranarray(rng.random((1000, 1000)))
+    d = st.to_device(a)
+    sa = st.StencilArray(d, st.Window(1))
+    out = st.mapstencil(st.mean, sa)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    _lib.profile_enable(True)
+    t = _timed_steps(lambda: st.mapstencil_(st.mean, out, sa), args.steps, args.warmup, flush)
+    prof = _lib.profile_report()
+    _lib.profile_enable(False)
+    exact = np.array_equal(st.to_host(out).view(np.uint64),
+                           orc.map(a, A.F64, st.Window(1), st.mean, st.Remove(0.0), st.Conditional()).view(np.uint64))
+    thr = orc.max_threads()
+    t0 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t0 < 3.0:
+        orc.map(a, A.F64, st.Window(1), st.mean, st.Remove(0.0), st.Conditional(), nthreads=thr)
+        reps += 1
+    cpu = reps * 1e6 / (time.perf_counter() - t0) / 1e9
+    line = {"workload": "mean blur 1000x1000 Float64, Window(1), Remove(0), Conditional", "metric": METRIC,
+            "value": args.steps * 1e6 / t / 1e9, "unit": UNIT, "us_per_map": 1e6 * t / args.steps,
+            "bit_exact_vs_oracle": bool(exact), "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"]),
+            "cpu_baseline": {"value": cpu, "unit": UNIT, "cores": thr, "kind": "port"},
+            "reference_published": {"cpu_min_ms": 2.755, "mx330_min_ms": 0.9168, "gtx1080_ms": 0.216}}
+    print(json.dumps(line), flush=True)
+
+
+def _gauss_weights(st):
+    import math
+    w = np.array([math.exp(-d * d / (2 * 1.5 ** 2)) for d in st.Window(3).distances()])
+    return w / w.sum()
+
+
+def run_gauss(args):
+    """Config 3a: Kernel(Window(3)) normalised Gaussian (sigma 1.5) on 8192^2 Float32 U[0,1), Remove(0);
+    FP32 and BF16 storage; max relative error against the FP64 oracle (over the whole grid)."""
+    import torch
+    entry.build()
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    from oracle import oracle as orc
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    rng = np.random.Generator(np.random.PCG64(3))
+    a32 = np.asfortranarray(rng.random((8192, 8192), dtype=np.float32))
+    w = _gauss_weights(st)
+    ref = orc.map(np.asfortranarray(a32.astype(np.float64)), A.F64, st.Kernel(st.Window(3), w), st.kernelproduct,
+                  st.Remove(0.0), st.Conditional(), nthreads=orc.max_threads())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    res = {}
+    for name, tdt in (("f32", torch.float32), ("bf16", torch.bfloat16)):
+        d = st.to_device(a32)
+        if tdt != torch.float32:
+            d2 = st.colmajor_empty(a32.shape, tdt)
+            d2.copy_(d)
+            d = d2
+        K = st.Kernel(st.Window(3), w.astype(np.float32), weight_dtype="f32")
+        sa = st.StencilArray(d, K, st.Remove(0.0))
+        out = st.mapstencil(st.kernelproduct, sa)
+        _lib.profile_enable(True)
+        t = _timed_steps(lambda: st.mapstencil_(st.kernelproduct, out, sa), args.steps, args.warmup, flush)
+        prof = _lib.profile_report()
+        _lib.profile_enable(False)
+        got = out.float().cpu().numpy().T.T.astype(np.float64)
+        rel = np.max(np.abs(got - ref) / np.abs(ref))
+        res[name] = {"gcell_s": args.steps * a32.size / t / 1e9, "ms_per_map": 1e3 * t / args.steps,
+                     "max_rel_err_vs_fp64": float(rel), "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"])}
+        del d, out, sa
+    line = {"workload": "7x7 Gaussian Kernel(Window(3)) 8192x8192, Remove(0)", "metric": METRIC, "unit": UNIT,
+            "value": res["f32"]["gcell_s"], "results": res, "fma_bound_note": "49 FMA per cell"}
+    print(json.dumps(line), flush=True)
+
+
+def run_diffusion(args):
+    """Config 3b: VonNeumann(1,3) explicit diffusion c + 0.1 (sum - 6c) on 512^3 U[0,1), Wrap, 200 steps,
+    FP32 and BF16 storage; FP64 total-mass drift on the GPU (K4); max relative error vs the FP64
+    oracle measured on a 96^3 grid run the same 200 steps."""
+    import torch
+    entry.build()
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    from oracle import oracle as orc
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    rng = np.random.Generator(np.random.PCG64(4))
+    steps = 200
+    a = np.asfortranarray(rng.random((512, 512, 512), dtype=np.float32))
+    small = np.asfortranarray(rng.random((96, 96, 96), dtype=np.float32))
+    pa, pb = np.asfortranarray(small.astype(np.float64)), np.asfortranarray(small.astype(np.float64))
+    in_b = orc.map_steps(pa, pb, A.F64, st.VonNeumann(1, 3), st.Diffusion(0.1), st.Wrap(), st.Conditional(), steps,
+                         nthreads=orc.max_threads())
+    ref_small = pb if in_b else pa
+    res = {}
+    for name, tdt in (("f32", torch.float32), ("bf16", torch.bfloat16)):
+        def mk(arr):
+            d = st.to_device(arr)
+            if tdt != torch.float32:
+                d2 = st.colmajor_empty(arr.shape, tdt)
+                d2.copy_(d)
+                d = d2
+            return d
+        S = st.SwitchingStencilArray(mk(a), st.VonNeumann(1, 3), st.Wrap())
+        m0 = st.mass(S.source)
+        torch.cuda.synchronize()
+        _lib.profile_enable(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        S = st.mapstencil_(st.Diffusion(0.1), S, steps=steps)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        prof = _lib.profile_report()
+        _lib.profile_enable(False)
+        m1 = st.mass(S.source)
+        Ss = st.mapstencil_(st.Diffusion(0.1), st.SwitchingStencilArray(mk(small), st.VonNeumann(1, 3), st.Wrap()),
+                            steps=steps)
+        got = Ss.source.float().cpu().numpy().astype(np.float64)
+        rel = float(np.max(np.abs(got - ref_small) / np.abs(ref_small)))
+        res[name] = {"gcell_s": a.size * steps / t / 1e9, "s_total": t, "mass_drift_rel": (m1 - m0) / m0,
+                     "max_rel_err_vs_fp64_96cube": rel, "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"])}
+        del S, Ss
+    line = {"workload": "7-point diffusion VonNeumann(1,3) 512^3, Wrap, 200 steps", "metric": METRIC, "unit": UNIT,
+            "value": res["f32"]["gcell_s"], "results": res}
+    print(json.dumps(line), flush=True)
+
+
+def _batched_jobs(st, rng, n=256):
+    import math
+    k5 = rng.standard_normal(25).astype(np.float32)
+    sten = [(st.mean, st.Window(1)), (st.mean, st.Circle(3)), (st.sum, st.Cross(2)),
+            (st.kernelproduct, st.Kernel(st.Window(2), k5, weight_dtype="f32"))]
+    jobs = []
+    for _ in range(n):
+        side = int(round(math.exp(rng.uniform(math.log(64), math.log(2048)))))
+        red, hood = sten[int(rng.integers(4))]
+        bnd = st.Wrap() if rng.random() < 0.5 else st.Remove(0.0)
+        jobs.append((rng.random((side, side), dtype=np.float32), red, hood, bnd, int(rng.integers(1, 51))))
+    return jobs
+
+
+def run_batched(args):
+    """Config 4: 256 Float32 grids, side log-uniform [64, 2048], stencil from {Window(1) mean, Circle(3) mean,
+    Cross(2) sum, 5x5 N(0,1) kernel}, 1-50 steps, Remove or Wrap: one graph-captured persistent launch
+    (autotuned) against 256 plain synchronising mapstencil! loops."""
+    import torch
+    entry.build()
+    st = entry.load_package()
+    rng = np.random.Generator(np.random.PCG64(5))
+    jobs = _batched_jobs(st, rng)
+    cells = sum(a.size * n for a, _, _, _, n in jobs)
+    dev = [st.to_device(a) for a, *_ in jobs]
+
+    def make():
+        b = st.Batch()
+        for d, (a, red, hood, bnd, n) in zip(dev, jobs):
+            c = st.colmajor_empty(d.shape, d.dtype)
+            c.copy_(d)
+            b.add(red, st.SwitchingStencilArray(c, hood, bnd, st.Conditional()), n)
+        return b
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    b = make()
+    t0 = time.perf_counter()
+    b.plan(autotune=True)
+    plan_s = time.perf_counter() - t0
+    tb = _timed_steps(lambda: b.run(sync=False), args.steps, args.warmup, flush)
+    seq = make()
+    seq.plan(autotune=False)
+    ts = _timed_steps(seq.run_sequential, max(2, args.steps // 3), 1, flush)
+    tb_s, ts_s = tb / args.steps, ts / max(2, args.steps // 3)
+    line = {"workload": "256 uneven Float32 grids, config-4 mix", "metric": METRIC, "unit": UNIT,
+            "value": cells / tb_s / 1e9, "ms_per_batch": 1e3 * tb_s, "plain_ms": 1e3 * ts_s,
+            "plain_gcell_s": cells / ts_s / 1e9, "speedup_vs_plain": ts_s / tb_s, "cell_steps": cells,
+            "plan_and_autotune_s": plan_s}
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args):
+    """Config 5: Poisson arrivals at several rates; jobs {side log-uniform [128, 4096], Float32 / BF16 /
+    UInt8, config-4 stencils or Moore(1) Life, steps U{1..200}}; continuous batching against the same
+    arrivals served one at a time by plain calls (host->device, mapstencil! loop, device->host)."""
+    import math
+    import torch
+    entry.build()
+    st = entry.load_package()
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    from oracle.oracle import f32_to_bf16_bits
+    rng = np.random.Generator(np.random.PCG64(6))
+    njobs = args.serve_jobs
+    k5 = rng.standard_normal(25).astype(np.float32)
+    sten = [(st.mean, st.Window(1)), (st.mean, st.Circle(3)), (st.sum, st.Cross(2)),
+            (st.kernelproduct, st.Kernel(st.Window(2), k5, weight_dtype="f32"))]
+
+    def make_job():
+        side = int(round(math.exp(rng.uniform(math.log(128), math.log(4096)))))
+        kind = ["f32", "bf16", "u8"][int(rng.integers(3))]
+        steps = int(rng.integers(1, 201))
+        if kind == "u8" or rng.random() < 0.2:
+            g = (rng.random((side, side)) < 0.3).astype(np.uint8)
+            return g, None, st.Moore(1), st.life, st.Wrap(), steps
+        red, hood = sten[int(rng.integers(4))]
+        bnd = st.Wrap() if rng.random() < 0.5 else st.Remove(0.0)
+        g = rng.random((side, side), dtype=np.float32)
+        if kind == "bf16":
+            return np.asfortranarray(f32_to_bf16_bits(g)), A.BF16, hood, (st.mean if red is st.sum else red), bnd, steps
+        return np.asfortranarray(g), None, hood, red, bnd, steps
+
+    def plain(job):
+        g, code, hood, red, bnd, steps = job
+        if code == A.BF16:
+            t = st.colmajor_empty(g.shape, torch.bfloat16)
+            t.view(torch.int16).copy_(torch.from_numpy(g.view(np.int16)))
+        else:
+            t = st.to_device(g)
+        S = st.mapstencil_(red, st.SwitchingStencilArray(t, hood, bnd, st.Conditional()), steps=steps)
+        S.source.cpu()
+
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    out = {}
+    for rate in rates:
+        jobs = [make_job() for _ in range(njobs)]
+        cells = sum(j[0].size * j[5] for j in jobs)
+        gaps = rng.exponential(1.0 / rate, size=njobs)
+        arrivals = np.cumsum(gaps) - gaps[0]
+        # served: submit at the arrival times
+        with st.Server(hbm_fraction=0.8, steps_per_tick=args.serve_tick) as srv:
+            ids = []
+            t0 = time.perf_counter()
+            for j, at in zip(jobs, arrivals):
+                dt = at - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                g, code, hood, red, bnd, steps = j
+                ids.append(srv.submit(g, hood, red, bnd, steps, code=code))
+            srv.drain(600.0)
+            makespan = time.perf_counter() - t0
+            lat = [srv.fetch(i)[1] for i in ids]
+        # plain: one job at a time in arrival order (FIFO), latency = finish - arrival
+        plain(jobs[0])
+        torch.cuda.synchronize()
+        service = []
+        for j in jobs:
+            t1 = time.perf_counter()
+            plain(j)
+            torch.cuda.synchronize()
+            service.append(time.perf_counter() - t1)
+        fin, plat = 0.0, []
+        for at, sv in zip(arrivals, service):
+            fin = max(fin, at) + sv
+            plat.append(fin - at)
+        out[str(int(rate))] = {
+            "served": {"gcell_s": cells / makespan / 1e9, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                       "p99_ms": 1e3 * float(np.percentile(lat, 99)), "makespan_s": makespan},
+            "plain_sequential": {"gcell_s": cells / fin / 1e9, "p50_ms": 1e3 * float(np.percentile(plat, 50)),
+                                 "p99_ms": 1e3 * float(np.percentile(plat, 99)), "makespan_s": fin},
+            "jobs": njobs, "cell_steps": cells}
+    best = max(out.values(), key=lambda v: v["served"]["gcell_s"])
+    line = {"workload": "serving stream, Poisson arrivals, config-5 job mix", "metric": METRIC, "unit": UNIT,
+            "value": best["served"]["gcell_s"], "rates": out, "steps_per_tick": args.serve_tick}
+    print(json.dumps(line), flush=True)
+
+
+WORKLOADS = {"mean_blur": run_mean_blur, "gauss": run_gauss, "diffusion": run_diffusion, "batched": run_batched,
+             "serving": run_serving}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -321,12 +627,19 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="life", choices=["life"] + sorted(WORKLOADS),
+                    help="life (the headline line) or one of the other BASELINE configurations")
+    ap.add_argument("--serve-jobs", type=int, default=120)
+    ap.add_argument("--serve-rates", default="100,300,1000,3000,5000")
+    ap.add_argument("--serve-tick", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     entry.load_package()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "life":
+        return WORKLOADS[args.workload](args)
     return run_gpu(args)
 
 

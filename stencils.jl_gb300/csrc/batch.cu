@@ -211,7 +211,6 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(const BatchDev d) 
         oa.alpha = j.alpha;
         oa.rcp_f = j.rcp_f;
         oa.fastdiv_f = j.fastdiv_f;
-        oa.rcp_d = j.rcp_d;
         oa.wf = sw;
         oa.w = nullptr;
         const int key = j.dtype * 16 + j.opv;
@@ -433,7 +432,6 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
         j.birth = s.op.birth_mask;
         j.survive = s.op.survive_mask;
         j.rcp_f = (float)(1.0 / (double)s.L);
-        j.rcp_d = 1.0 / (double)s.L;
         j.fastdiv_f = (s.opv == OPV_MEAN && s.a.dtype != STC_F64 && is_float_dtype(s.a.dtype)) ? (int)fastdiv_f_exact(s.L) : 0;
         j.shape = table_matches_shape(s.shape, s.R, 2, s.offs.data(), s.L) ? s.shape : STC_SHAPE_TABLE;
         j.off_base = (int32_t)(b->hoffs.size() / 2);

@@ -20,7 +20,6 @@ struct OpArgs {
     double alpha;
     float rcp_f;
     int32_t fastdiv_f;
-    double rcp_d;
     const float* wf;
     const double* w;
 };
@@ -44,7 +43,6 @@ struct BatchJob {
     uint32_t birth, survive;
     float rcp_f;
     int32_t fastdiv_f;
-    double rcp_d;
 };
 
 struct BatchItem { int32_t job, round, tile, steps; };

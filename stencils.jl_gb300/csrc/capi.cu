@@ -18,6 +18,7 @@
 #include "life.h"
 #include "map_kernel.cuh"
 #include "profile.h"
+#include "tblock.h"
 
 namespace stc {
 
@@ -302,7 +303,6 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     p.status = ctx->status;
     p.L = st->len;
     p.rcp_f = (float)(1.0 / (double)st->len);
-    p.rcp_d = 1.0 / (double)st->len;
     p.fastdiv_f = (op->code == STC_OP_MEAN && !is_float_dtype(src->dtype)) ? 0
                   : (op->code == STC_OP_MEAN && src->dtype != STC_F64) ? (int)fastdiv_f_exact(st->len) : 0;
     p.birth = op->birth_mask;
@@ -467,6 +467,11 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
     // Cellular automata on bit-packable grids run temporally blocked on a packed copy.
     rc = life_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
     if (rc) return rc;
+    // 3D radius-1 float maps: k steps per pass over HBM; the last step runs below
+    if (done == 0) {
+        rc = tb3d_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
+        if (rc) return rc;
+    }
     const stc_grid* grids[2] = {a, b};
     for (int64_t k = done; k < nsteps; ++k) {
         const stc_grid* sg = grids[src_is_b];

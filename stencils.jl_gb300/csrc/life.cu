@@ -10,8 +10,9 @@
 // ping-pong pair — the valid band shrinks by one row per generation — and writes the band back.
 // One HBM/L2 round trip per k generations instead of per generation.
 //
-// Per word, the 8 neighbour planes come from funnel shifts of the three rows' (w-1, w, w+1) words;
-// a carry-save adder network produces the 4-bit neighbour count and the rule is evaluated bitwise.
+// Per word, each row's 3-cell sum (2 bits, from funnel shifts of its (w-1, w, w+1) words) is formed
+// once as the row enters a rolling three-row window; a carry-save adder adds the three rows' sums into
+// the 4-bit 3x3 total and the rule is evaluated bitwise on it (neighbours = total - centre).
 // The neighbour count is the count of nonzero neighbours, exactly what the LIFE op counts, so the
 // result is bit-identical to the per-cell gather for any input values.
 #include <algorithm>
@@ -34,40 +35,45 @@ __device__ __forceinline__ void full_add(uint32_t a, uint32_t b, uint32_t c, uin
     cy = (a & b) | (t & c);
 }
 
-// neighbour count of every bit of word c from the (left, centre, right) words of rows u, c, d
-__device__ __forceinline__ Count4 count8(uint32_t uL, uint32_t u, uint32_t uR, uint32_t cL, uint32_t c,
-                                         uint32_t cR, uint32_t dL, uint32_t d, uint32_t dR) {
-    const uint32_t n1 = __funnelshift_l(uL, u, 1), n2 = u, n3 = __funnelshift_r(u, uR, 1);
-    const uint32_t n4 = __funnelshift_l(cL, c, 1), n5 = __funnelshift_r(c, cR, 1);
-    const uint32_t n6 = __funnelshift_l(dL, d, 1), n7 = d, n8 = __funnelshift_r(d, dR, 1);
-    uint32_t s1, c1, s2, c2, b0, d1, e0, e1;
-    full_add(n1, n2, n3, s1, c1);
-    full_add(n4, n5, n6, s2, c2);
-    const uint32_t s3 = n7 ^ n8, c3 = n7 & n8;
-    full_add(s1, s2, s3, b0, d1);
-    full_add(c1, c2, c3, e0, e1);
-    Count4 k;
-    k.b0 = b0;
-    k.b1 = e0 ^ d1;
-    const uint32_t f1 = e0 & d1;
-    k.b2 = e1 ^ f1;
-    k.b3 = e1 & f1;
-    return k;
+// 3-cell horizontal sum of a row around every bit: (a, b) with L + C + R = a + 2b
+struct Sum3 { uint32_t a, b; };
+__device__ __forceinline__ Sum3 row_sum3(uint32_t wl, uint32_t c, uint32_t wr) {
+    const uint32_t L = __funnelshift_l(wl, c, 1), R = __funnelshift_r(c, wr, 1);
+    Sum3 s;
+    s.a = L ^ c ^ R;
+    s.b = (L & c) | (R & (L ^ c));
+    return s;
 }
 
+// 4-bit total of the 3x3 block (centre included) from three rows' 3-cell sums
+__device__ __forceinline__ Count4 total9(const Sum3& u, const Sum3& c, const Sum3& d) {
+    Count4 t;
+    uint32_t k0, x1, k1;
+    full_add(u.a, c.a, d.a, t.b0, k0);     // weight 1 and its carry (weight 2)
+    full_add(u.b, c.b, d.b, x1, k1);       // weight 2 and its carry (weight 4)
+    t.b1 = x1 ^ k0;
+    const uint32_t k2 = x1 & k0;           // weight 4
+    t.b2 = k1 ^ k2;
+    t.b3 = k1 & k2;                         // weight 8
+    return t;
+}
+
+// next state from the 3x3 total (neighbour count n = total - centre)
 template <bool CONWAY>
-__device__ __forceinline__ uint32_t apply_rule(const Count4& k, uint32_t c, uint32_t birth, uint32_t survive) {
+__device__ __forceinline__ uint32_t rule_from_total(const Count4& t, uint32_t c, uint32_t birth, uint32_t survive) {
     if constexpr (CONWAY) {
-        // B3/S23: count == 3, or count == 2 and alive
-        return k.b1 & ~k.b2 & ~k.b3 & (k.b0 | c);
+        // B3/S23: n == 3 (total 3 when dead, 4 when alive) or alive with n == 2 (total 3)
+        const uint32_t is3 = t.b0 & t.b1 & ~t.b2 & ~t.b3;
+        const uint32_t is4 = ~t.b0 & ~t.b1 & t.b2 & ~t.b3;
+        return is3 | (c & is4);
     } else {
         uint32_t out = 0;
 #pragma unroll
-        for (int n = 0; n <= 8; ++n) {
-            const uint32_t m = ((n & 1) ? k.b0 : ~k.b0) & ((n & 2) ? k.b1 : ~k.b1) & ((n & 4) ? k.b2 : ~k.b2) &
-                               ((n & 8) ? k.b3 : ~k.b3);
-            if ((birth >> n) & 1u) out |= m & ~c;
-            if ((survive >> n) & 1u) out |= m & c;
+        for (int v = 0; v <= 9; ++v) {
+            const uint32_t m = ((v & 1) ? t.b0 : ~t.b0) & ((v & 2) ? t.b1 : ~t.b1) & ((v & 4) ? t.b2 : ~t.b2) &
+                               ((v & 8) ? t.b3 : ~t.b3);
+            if (v <= 8 && ((birth >> v) & 1u)) out |= m & ~c;             // dead: n = total
+            if (v >= 1 && ((survive >> (v - 1)) & 1u)) out |= m & c;     // alive: n = total - 1
         }
         return out;
     }
@@ -127,20 +133,25 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
                 L = edge_l ? 0u : row[wl];
                 R = edge_r ? 0u : row[wr];
             };
-            uint32_t uL, u, uR, cL, c, cR, dL, d, dR;
-            ld(ra - 1, uL, u, uR);
-            ld(ra, cL, c, cR);
+            // rolling window of three rows; each row's 3-cell sum is formed once and reused
+            uint32_t L_, C_, R_;
+            ld(ra - 1, L_, C_, R_);
+            Sum3 su = row_sum3(L_, C_, R_);
+            ld(ra, L_, C_, R_);
+            Sum3 sc = row_sum3(L_, C_, R_);
+            uint32_t c = C_;
             for (int r = ra; r < rb; ++r) {
-                ld(r + 1, dL, d, dR);
-                const Count4 cnt = count8(uL, u, uR, cL, c, cR, dL, d, dR);
-                uint32_t nx = apply_rule<CONWAY>(cnt, c, p.birth, p.survive);
+                ld(r + 1, L_, C_, R_);
+                const Sum3 sd = row_sum3(L_, C_, R_);
+                uint32_t nx = rule_from_total<CONWAY>(total9(su, sc, sd), c, p.birth, p.survive);
                 if (!p.wrap) {
                     const int gy = y0 - k + r;
                     if (gy < 0 || gy >= p.n1) nx = 0u;   // rows outside the grid stay dead
                 }
                 dst[(size_t)r * W + w] = nx;
-                uL = cL; u = c; uR = cR;
-                cL = dL; c = d; cR = dR;
+                su = sc;
+                sc = sd;
+                c = C_;
             }
         }
         __syncthreads();

@@ -57,7 +57,6 @@ struct MapParams {
     uint32_t birth, survive;
     float rcp_f;               // RN(1/L) in float, used when fastdiv_f (host-verified exact for this L)
     int32_t fastdiv_f;
-    double rcp_d;              // RN(1/L) in double; every quotient is verified by its residual
     int8_t off[STC_MAX_LEN][3];
     float wf[STC_MAX_LEN];
     double w[STC_MAX_LEN];
@@ -80,22 +79,10 @@ template <class P> __device__ __forceinline__ float div_by_len(float a, const P&
     }
     return __fdiv_rn(a, (float)p.L);
 }
-// Float64: the same corrected quotient q1, accepted only when its exact residual a - q1*L proves it is
-// the correctly rounded a / L (|residual| < L * ulp(q1) / 4, conservative at binade edges);
-// otherwise the IEEE division.
+// Float64 uses the IEEE division: on GB300 every FP64 instruction is costly, and a verified FMA
+// quotient needs more of them than __ddiv_rn.
 template <class P> __device__ __forceinline__ double div_by_len(double a, const P& p) {
-    const double L = (double)p.L;
-    const double fa = fabs(a);
-    if (fa >= 0x1p-900 && fa <= 0x1p+1000) {
-        const double q = __dmul_rn(a, p.rcp_d);
-        const double e = __fma_rn(-q, L, a);
-        const double q1 = __fma_rn(e, p.rcp_d, q);
-        const double e1 = __fma_rn(-q1, L, a);
-        const int ex = (int)((__double_as_longlong(q1) >> 52) & 0x7ff);
-        const double ulp = __longlong_as_double((long long)(ex - 52) << 52);   // 2^(exp-52), ex > 52 here
-        if (fabs(e1) < __dmul_rn(L, ulp) * 0.25) return q1;
-    }
-    return __ddiv_rn(a, L);
+    return __ddiv_rn(a, (double)p.L);
 }
 
 template <class Tin, class Tout, class Acc> struct OpMean {
