@@ -110,18 +110,23 @@ __device__ void batch_item(const BatchJob& j, const BatchItem& it, unsigned char
     const int dstb = j.resident ? (j.nsteps & 1) : ((it.round + 1) & 1);
     const T* sp = (const T*)j.buf[src] + j.org[src];
     const T pv = pad_of<T>(j);
-    for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
-        const int bx = i % pw, by = i / pw;
-        int gx = x0 - pad + bx, gy = y0 - pad + by;
-        T v;
-        if (j.boundary == STC_WRAP) {
-            v = ld_l2(sp + (int64_t)wrapi(gy, j.n1) * j.sy[src] + wrapi(gx, j.n0));
-        } else if (gx >= 0 && gx < j.n0 && gy >= 0 && gy < j.n1) {
-            v = ld_l2(sp + (int64_t)gy * j.sy[src] + gx);
-        } else {
-            v = pv;
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        for (int by = warp; by < ph; by += nwarps) {
+            const int gy = y0 - pad + by;
+            const bool wr = j.boundary == STC_WRAP;
+            const int gyw = wr ? wrapi(gy, j.n1) : gy;
+            const bool row_in = wr || (gy >= 0 && gy < j.n1);
+            const T* srow = sp + (int64_t)gyw * j.sy[src];
+            for (int bx = lane; bx < pw; bx += 32) {
+                const int gx = x0 - pad + bx;
+                T v;
+                if (wr) v = ld_l2(srow + (gx >= 0 && gx < j.n0 ? gx : wrapi(gx, j.n0)));
+                else if (row_in && gx >= 0 && gx < j.n0) v = ld_l2(srow + gx);
+                else v = pv;
+                b0[by * pw + bx] = v;
+            }
         }
-        b0[i] = v;
     }
     __syncthreads();
     for (int g = 0; g < steps; ++g) {
@@ -129,31 +134,43 @@ __device__ void batch_item(const BatchJob& j, const BatchItem& it, unsigned char
         T* out = (g & 1) ? b0 : b1;
         const int lx = j.resident ? R : R * (g + 1), ly = lx;
         const int hx = j.resident ? R + tw : pw - R * (g + 1), hy = j.resident ? R + th : ph - R * (g + 1);
-        const int cw = hx - lx, ch = hy - ly;
-        for (int i = threadIdx.x; i < cw * ch; i += blockDim.x) {
-            const int bx = lx + i % cw, by = ly + i / cw;
-            const int gx = x0 - pad + bx, gy = y0 - pad + by;
-            T v;
-            if (j.boundary != STC_WRAP && (gx < 0 || gx >= j.n0 || gy < 0 || gy >= j.n1)) v = pv;
-            else v = batch_fold<T, Op, Sh>(in + (size_t)by * pw + bx, pw, so, oa);
-            out[(size_t)by * pw + bx] = v;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        for (int by = ly + warp; by < hy; by += nwarps) {
+            const int gy = y0 - pad + by;
+            const bool row_out = j.boundary != STC_WRAP && (gy < 0 || gy >= j.n1);
+            for (int bx = lx + lane; bx < hx; bx += 32) {
+                const int gx = x0 - pad + bx;
+                T v;
+                if (row_out || (j.boundary != STC_WRAP && (gx < 0 || gx >= j.n0))) v = pv;
+                else v = batch_fold<T, Op, Sh>(in + by * pw + bx, pw, so, oa);
+                out[by * pw + bx] = v;
+            }
         }
         __syncthreads();
         if (j.resident && g + 1 < steps) {
-            for (int i = threadIdx.x; i < pw * ph; i += blockDim.x) {
-                const int bx = i % pw, by = i / pw;
-                if (bx >= R && bx < R + tw && by >= R && by < R + th) continue;
-                out[i] = j.boundary == STC_WRAP ? out[(size_t)(wrapi(by - R, th) + R) * pw + wrapi(bx - R, tw) + R] : pv;
+            // refresh the ring of R cells around the resident grid from its new interior
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+            for (int by = warp; by < ph; by += nwarps) {
+                const bool ring_row = by < R || by >= R + th;
+                const int sy = wrapi(by - R, th) + R;
+                for (int bx = lane; bx < pw; bx += 32) {
+                    if (!ring_row && bx >= R && bx < R + tw) continue;
+                    out[by * pw + bx] = j.boundary == STC_WRAP ? out[sy * pw + wrapi(bx - R, tw) + R] : pv;
+                }
             }
             __syncthreads();
         }
     }
     const T* fin = (steps & 1) ? b1 : b0;
     T* dp = (T*)j.buf[dstb] + j.org[dstb];
-    for (int i = threadIdx.x; i < tw * th; i += blockDim.x) {
-        const int tx = i % tw, ty = i / tw;
-        const int gx = x0 + tx, gy = y0 + ty;
-        if (gx < j.n0 && gy < j.n1) dp[(int64_t)gy * j.sy[dstb] + gx] = fin[(size_t)(ty + pad) * pw + tx + pad];
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        const int nvx = min(tw, j.n0 - x0), nvy = min(th, j.n1 - y0);
+        for (int ty = warp; ty < nvy; ty += nwarps) {
+            T* drow = dp + (int64_t)(y0 + ty) * j.sy[dstb] + x0;
+            const T* frow = fin + (ty + pad) * pw + pad;
+            for (int tx = lane; tx < nvx; tx += 32) drow[tx] = frow[tx];
+        }
     }
 }
 

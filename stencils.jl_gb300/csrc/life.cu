@@ -113,7 +113,8 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
         buf0[i] = v;
     }
     __syncthreads();
-    // thread -> (column w, strip s); strips split the valid row range of each generation
+    // thread -> (column w, strip s); strips split the valid row range of each generation.  The
+    // per-column setup is hoisted out of the generation loop.
     const int strips = max(1, (int)blockDim.x / W);
     for (int g = 0; g < k; ++g) {
         const uint32_t* src = (g & 1) ? buf1 : buf0;
@@ -122,13 +123,12 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
         const int nr = hi - lo;
         for (int col = threadIdx.x; col < W * strips; col += blockDim.x) {
             const int w = col % W, s = col / W;
-            if (s >= strips) break;
-            const int ra = lo + (int)((int64_t)nr * s / strips), rb = lo + (int)((int64_t)nr * (s + 1) / strips);
+            const int ra = lo + (nr * s) / strips, rb = lo + (nr * (s + 1)) / strips;
             if (ra >= rb) continue;
             const int wl = w == 0 ? W - 1 : w - 1, wr = w == W - 1 ? 0 : w + 1;
             const bool edge_l = !p.wrap && w == 0, edge_r = !p.wrap && w == W - 1;
             auto ld = [&](int r, uint32_t& L, uint32_t& C, uint32_t& R) {
-                const uint32_t* row = src + (size_t)r * W;
+                const uint32_t* row = src + r * W;
                 C = row[w];
                 L = edge_l ? 0u : row[wl];
                 R = edge_r ? 0u : row[wr];
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
                     const int gy = y0 - k + r;
                     if (gy < 0 || gy >= p.n1) nx = 0u;   // rows outside the grid stay dead
                 }
-                dst[(size_t)r * W + w] = nx;
+                dst[r * W + w] = nx;
                 su = sc;
                 sc = sd;
                 c = C_;

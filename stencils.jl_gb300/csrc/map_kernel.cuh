@@ -281,13 +281,15 @@ __device__ __forceinline__ Tin load_bounded(const MapParams& p, int64_t x, int64
 
 struct TileOrigin { int64_t x0, y0, z0; };
 
+// tile counts per axis and in total stay below 2^31 (axes are < 2^31 cells), so 32-bit math suffices
 __device__ __forceinline__ TileOrigin tile_origin(const MapParams& p, int64_t t) {
     TileOrigin o;
-    const int64_t tx = t % p.ntx;
-    const int64_t r = t / p.ntx;
-    o.x0 = tx * p.tw;
-    o.y0 = (r % p.nty) * p.th;
-    o.z0 = (r / p.nty) * p.tz;
+    const uint32_t ti = (uint32_t)t, ntx = (uint32_t)p.ntx, nty = (uint32_t)p.nty;
+    const uint32_t r = ti / ntx;
+    o.x0 = (int64_t)(ti - r * ntx) * p.tw;
+    const uint32_t rz = r / nty;
+    o.y0 = (int64_t)(r - rz * nty) * p.th;
+    o.z0 = (int64_t)rz * p.tz;
     return o;
 }
 

@@ -6,7 +6,8 @@
 // A CTA owns an (x, y) tile of TX x TY outputs with a k-cell halo and a chunk of z.  It streams the
 // input planes z0-k .. z1+k-1 through a TMA ring in shared memory (cp.async.bulk.tensor.3d, one plane
 // per copy, no multicast); after plane i lands, time level t = 1..k computes its plane i-t from the
-// three level t-1 planes below, above and at it (each level keeps a 3-plane ring), the valid region
+// three level t-1 planes below, above and at it (each level keeps a 4-plane ring, skewed so one
+// barrier per plane suffices), the valid region
 // shrinking by one cell per level in x and y.  Level k planes are the outputs.  So one pass over HBM
 // advances the grid k steps.  Wrap: cells outside the grid are wrapped copies and evolve like the
 // cells they copy.  Remove: cells outside the grid are reset to padval at every level.  Every cell
@@ -26,6 +27,7 @@ namespace stc {
 
 constexpr int kTbThreads = 256;
 constexpr int kTbRing0 = 6;          // input planes in flight (prefetch distance kTbRing0 - 3)
+constexpr int kTbRingL = 4;          // planes kept per intermediate time level (skewed schedule)
 
 struct TBParams {
     CUtensorMap tmap;                // source parent (rank 3)
@@ -101,10 +103,12 @@ __global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant_
     extern __shared__ __align__(128) unsigned char tsm[];
     const int k = p.k, PX = p.PX, PY = p.PY;
     const size_t pb = p.plane_bytes;
-    // layout: level-0 ring (kTbRing0 planes), levels 1..k-1 (3 planes each), mbarriers
+    // layout: level-0 ring (kTbRing0 planes), levels 1..k-1 (kTbRingL planes each), mbarriers
     auto plane0 = [&](int j) { return (T*)(tsm + (size_t)(j % kTbRing0) * pb); };
-    auto planeL = [&](int t, int j) { return (T*)(tsm + (size_t)(kTbRing0 + 3 * (t - 1) + (j % 3)) * pb); };
-    uint64_t* bars = (uint64_t*)(tsm + (size_t)(kTbRing0 + 3 * (k - 1)) * pb);
+    auto planeL = [&](int t, int j) {
+        return (T*)(tsm + (size_t)(kTbRing0 + kTbRingL * (t - 1) + (j % kTbRingL)) * pb);
+    };
+    uint64_t* bars = (uint64_t*)(tsm + (size_t)(kTbRing0 + kTbRingL * (k - 1)) * pb);
 
     int64_t t_id = blockIdx.x;
     const int tx = (int)(t_id % p.ntx);
@@ -141,39 +145,51 @@ __global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant_
         for (int j = 0; j < min(ahead, NI); ++j) issue(j);
     // region of the box holding real tile columns/rows
     const bool edge_xy = x0 - k < 0 || y0 - k < 0 || x0 + p.TX + k > p.n[0] || y0 + p.TY + k > p.n[1];
-    for (int i = 0; i < NI; ++i) {
-        if (threadIdx.x == 0 && i + ahead < NI) {
-            fence_proxy_async();
-            issue(i + ahead);
-        }
-        const bool ok = mbar_wait_bounded(&bars[i % kTbRing0], (uint32_t)((i / kTbRing0) & 1));
-        if (!__syncthreads_and(ok)) {
-            if (threadIdx.x == 0) {
-                atomicOr(p.status, DEV_ERR_TIMEOUT);
-                for (int j = i; j < min(i + ahead, NI); ++j)
-                    mbar_wait_bounded(&bars[j % kTbRing0], (uint32_t)((j / kTbRing0) & 1), 100000000ll);
+    // Skewed wavefront: at iteration i, level t computes its plane j = i - 2t + 1.  Level 1 reads
+    // level-0 planes i-2 .. i (plane i just landed); level t >= 2 reads level t-1 planes j-1 .. j+1,
+    // all finished in earlier iterations.  So every level of an iteration is independent of the
+    // others and one barrier per iteration suffices.  Iterations continue past the last input plane
+    // until level k has produced every output plane.
+    const int iters = NI + 2 * k - 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int i = 0; i < iters; ++i) {
+        if (i < NI) {
+            if (threadIdx.x == 0 && i + ahead < NI) {
+                fence_proxy_async();
+                issue(i + ahead);
             }
-            return;
-        }
-        // level-0 plane i: patch cells outside the grid (Wrap copies / Remove padval)
-        {
+            const bool ok = mbar_wait_bounded(&bars[i % kTbRing0], (uint32_t)((i / kTbRing0) & 1));
+            if (!__syncthreads_and(ok)) {
+                if (threadIdx.x == 0) {
+                    atomicOr(p.status, DEV_ERR_TIMEOUT);
+                    for (int j = i; j < min(i + ahead, NI); ++j)
+                        mbar_wait_bounded(&bars[j % kTbRing0], (uint32_t)((j / kTbRing0) & 1), 100000000ll);
+                }
+                return;
+            }
+            // level-0 plane i: patch cells outside the grid (Wrap copies / Remove padval)
             T* P0 = plane0(i);
             const int64_t z = plane_z(i);
             const bool zout = z < 0 || z >= p.n[2];
             if (!wrapb && zout) {
                 for (int c = threadIdx.x; c < PX * PY; c += blockDim.x) P0[c] = pv;
+                fence_proxy_async();   // generic writes before a later TMA refill of this slot
+                __syncthreads();
             } else if (p.fixup && edge_xy) {
-                for (int c = threadIdx.x; c < PX * PY; c += blockDim.x) {
-                    const int bx = c % PX, by = c / PX;
-                    const int64_t gx = x0 - p.padl + bx, gy = y0 - k + by;
-                    if (gx < 0 || gx >= p.n[0] || gy < 0 || gy >= p.n[1]) P0[c] = tb_load<T>(p, gx, gy, z);
+                for (int by = warp; by < PY; by += nwarps) {
+                    const int64_t gy = y0 - k + by;
+                    const bool row_in = gy >= 0 && gy < p.n[1];
+                    for (int bx = lane; bx < PX; bx += 32) {
+                        const int64_t gx = x0 - p.padl + bx;
+                        if (!row_in || gx < 0 || gx >= p.n[0]) P0[by * PX + bx] = tb_load<T>(p, gx, gy, z);
+                    }
                 }
+                fence_proxy_async();
+                __syncthreads();
             }
-            fence_proxy_async();
         }
-        __syncthreads();
         for (int t = 1; t <= k; ++t) {
-            const int j = i - t;                       // plane index at level t
+            const int j = i - 2 * t + 1;               // plane index at level t
             if (j < t || j > NI - 1 - t) continue;     // uniform across the CTA
             const T* lo = (t == 1) ? plane0(j - 1) : planeL(t - 1, j - 1);
             const T* mid = (t == 1) ? plane0(j) : planeL(t - 1, j);
@@ -181,35 +197,36 @@ __global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant_
             const int64_t z = plane_z(j);
             const int xa = p.padl - k + t, xb = p.padl + p.TX + k - t;
             const int ya = t, yb = p.TY + 2 * k - t;
-            const int cw = xb - xa, ch = yb - ya;
             if (t < k) {
                 T* out = planeL(t, j);
                 const bool zout = z < 0 || z >= p.n[2];
-                for (int c = threadIdx.x; c < cw * ch; c += blockDim.x) {
-                    const int bx = xa + c % cw, by = ya + c / cw;
-                    const int off = by * PX + bx;
-                    T v;
-                    const int64_t gx = x0 - p.padl + bx, gy = y0 - k + by;
-                    if (!wrapb && (zout || gx < 0 || gx >= p.n[0] || gy < 0 || gy >= p.n[1])) {
-                        v = pv;
-                    } else {
-                        v = tb_fold<T, Op, Sh>(lo + off, mid + off, hi + off, PX, p);
+                for (int by = ya + warp; by < yb; by += nwarps) {
+                    const int64_t gy = y0 - k + by;
+                    const bool row_out = !wrapb && (zout || gy < 0 || gy >= p.n[1]);
+                    for (int bx = xa + lane; bx < xb; bx += 32) {
+                        const int off = by * PX + bx;
+                        const int64_t gx = x0 - p.padl + bx;
+                        T v;
+                        if (row_out || (!wrapb && (gx < 0 || gx >= p.n[0]))) v = pv;
+                        else v = tb_fold<T, Op, Sh>(lo + off, mid + off, hi + off, PX, p);
+                        out[off] = v;
                     }
-                    out[off] = v;
                 }
             } else {
                 // level k: the outputs, tile interior only
                 T* dst = (T*)p.dst;
                 const int nvx = (int)min((int64_t)p.TX, p.n[0] - x0), nvy = (int)min((int64_t)p.TY, p.n[1] - y0);
-                T* dplane = dst + p.dst_org + z * p.dstr[2];
-                for (int c = threadIdx.x; c < nvx * nvy; c += blockDim.x) {
-                    const int lx = c % nvx, ly = c / nvx;
-                    const int off = (ly + k) * PX + lx + p.padl;
-                    dplane[(y0 + ly) * p.dstr[1] + x0 + lx] = tb_fold<T, Op, Sh>(lo + off, mid + off, hi + off, PX, p);
+                T* dplane = dst + p.dst_org + z * p.dstr[2] + x0;
+                for (int ly = warp; ly < nvy; ly += nwarps) {
+                    T* drow = dplane + (y0 + ly) * p.dstr[1];
+                    for (int lx = lane; lx < nvx; lx += 32) {
+                        const int off = (ly + k) * PX + lx + p.padl;
+                        drow[lx] = tb_fold<T, Op, Sh>(lo + off, mid + off, hi + off, PX, p);
+                    }
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();
     }
 }
 
@@ -308,7 +325,17 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     p.nzc = (int)((p.n[2] + p.ZC - 1) / p.ZC);
     // launches: the first nsteps-1 steps, split so that state nsteps-1 ends in the parent the reference
     // leaves it in (a after an odd number of steps... i.e. m launches with m = nsteps-1 (mod 2))
-    const int kmax = 4;
+    // deepest k <= 4 whose rings keep two CTAs per SM (<= 110 KB of shared memory)
+    int kmax = 4;
+    {
+        while (kmax > 1) {
+            const int padl = kmax + (((p.hx[0] - kmax) % V) + V) % V;
+            const int PX = (padl + p.TX + kmax + V - 1) / V * V;
+            const size_t pbytes = ((size_t)PX * (p.TY + 2 * kmax) * es + 127) / 128 * 128;
+            if ((size_t)(kTbRing0 + kTbRingL * (kmax - 1)) * pbytes <= 110 * 1024) break;
+            --kmax;
+        }
+    }
     const int64_t blocked = nsteps - 1;
     int64_t m = (blocked + kmax - 1) / kmax;
     if ((m - blocked) % 2 != 0) ++m;
@@ -325,7 +352,7 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         p.PX = (p.padl + p.TX + kk + V - 1) / V * V;
         p.PY = p.TY + 2 * kk;
         p.plane_bytes = (uint32_t)(((size_t)p.PX * p.PY * es + 127) / 128 * 128);
-        const size_t smem = (size_t)(kTbRing0 + 3 * (kk - 1)) * p.plane_bytes + 8 * kTbRing0;
+        const size_t smem = (size_t)(kTbRing0 + kTbRingL * (kk - 1)) * p.plane_bytes + 8 * kTbRing0;
         if (smem > (size_t)smem_cap || p.PX > 256 || p.PY > 256) return *done ? STC_ERR_UNSUPPORTED : STC_OK;
         p.src = sg->data;
         p.dst = dg->data;
