@@ -227,6 +227,9 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(const BatchDev d) 
         oa.survive = j.survive;
         oa.alpha = j.alpha;
         oa.rcp_f = j.rcp_f;
+        oa.Lf = (float)j.L;
+        oa.Ld = (double)j.L;
+        oa.alpha_f = (float)j.alpha;
         oa.fastdiv_f = j.fastdiv_f;
         oa.wf = sw;
         oa.w = nullptr;

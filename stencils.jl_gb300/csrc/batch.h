@@ -20,6 +20,9 @@ struct OpArgs {
     double alpha;
     float rcp_f;
     int32_t fastdiv_f;
+    float Lf;
+    double Ld;
+    float alpha_f;
     const float* wf;
     const double* w;
 };

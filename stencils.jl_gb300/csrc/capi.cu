@@ -303,6 +303,9 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     p.status = ctx->status;
     p.L = st->len;
     p.rcp_f = (float)(1.0 / (double)st->len);
+    p.Lf = (float)st->len;
+    p.Ld = (double)st->len;
+    p.alpha_f = (float)op->alpha;
     p.fastdiv_f = (op->code == STC_OP_MEAN && !is_float_dtype(src->dtype)) ? 0
                   : (op->code == STC_OP_MEAN && src->dtype != STC_F64) ? (int)fastdiv_f_exact(st->len) : 0;
     p.birth = op->birth_mask;
@@ -371,7 +374,7 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     for (int d = 1; d < nd; ++d)
         if ((src->stride[d] * es) % 16 != 0) tma = false;
     if (tma) {
-        p.stages = (int)std::min<int64_t>(kMaxStages, std::max<int64_t>(2, (100 * 1024) / p.stage_bytes));
+        p.stages = (int)std::min<int64_t>(kMaxStages, std::max<int64_t>(2, (64 * 1024) / p.stage_bytes));
         while ((int64_t)p.stages * p.stage_bytes > smem_cap) --p.stages;
         cuuint64_t gdim[3], gstr[2];
         cuuint32_t box[3] = {(cuuint32_t)p.bw, (cuuint32_t)p.bh, (cuuint32_t)p.bd}, est[3] = {1, 1, 1};

@@ -90,7 +90,19 @@ struct LifeParams {
     uint32_t birth, survive;
 };
 
-template <bool CONWAY>
+// one column's rolling window: the 3-cell sums of the rows above and at the current row, and the
+// current row's own word
+struct ColState { Sum3 su, sc; uint32_t c; };
+
+template <bool WRAP>
+__device__ __forceinline__ Sum3 load_sum3(const uint32_t* row, int w, int wl, int wr, int W) {
+    const uint32_t C = row[w];
+    const uint32_t L = (!WRAP && w == 0) ? 0u : row[wl];
+    const uint32_t R = (!WRAP && w == W - 1) ? 0u : row[wr];
+    return row_sum3(L, C, R);
+}
+
+template <bool CONWAY, bool WRAP>
 __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifeParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
     const int W = p.W, k = p.k;
@@ -103,7 +115,7 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
         const int r = i / W, w = i - r * W;
         int gy = y0 - k + r;
         uint32_t v = 0;
-        if (p.wrap) {
+        if (WRAP) {
             gy %= p.n1;
             if (gy < 0) gy += p.n1;
             v = p.in[(size_t)gy * W + w];
@@ -113,45 +125,55 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
         buf0[i] = v;
     }
     __syncthreads();
-    // thread -> (column w, strip s); strips split the valid row range of each generation.  The
-    // per-column setup is hoisted out of the generation loop.
-    const int strips = max(1, (int)blockDim.x / W);
+    // Thread -> (column pair, strip).  Each thread carries two independent columns (w and w + W/2
+    // when W is even) through its strip of rows, so the two adder networks interleave.  Strips split
+    // the valid row range of each generation.
+    const int cols = (W % 2 == 0) ? 2 : 1;
+    const int Wc = W / cols;
+    const int strips = max(1, (int)blockDim.x / Wc);
     for (int g = 0; g < k; ++g) {
         const uint32_t* src = (g & 1) ? buf1 : buf0;
         uint32_t* dst = (g & 1) ? buf0 : buf1;
         const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of src
         const int nr = hi - lo;
-        for (int col = threadIdx.x; col < W * strips; col += blockDim.x) {
-            const int w = col % W, s = col / W;
+        for (int item = threadIdx.x; item < Wc * strips; item += blockDim.x) {
+            const int cb = item % Wc, s = item / Wc;
             const int ra = lo + (nr * s) / strips, rb = lo + (nr * (s + 1)) / strips;
             if (ra >= rb) continue;
-            const int wl = w == 0 ? W - 1 : w - 1, wr = w == W - 1 ? 0 : w + 1;
-            const bool edge_l = !p.wrap && w == 0, edge_r = !p.wrap && w == W - 1;
-            auto ld = [&](int r, uint32_t& L, uint32_t& C, uint32_t& R) {
-                const uint32_t* row = src + r * W;
-                C = row[w];
-                L = edge_l ? 0u : row[wl];
-                R = edge_r ? 0u : row[wr];
-            };
-            // rolling window of three rows; each row's 3-cell sum is formed once and reused
-            uint32_t L_, C_, R_;
-            ld(ra - 1, L_, C_, R_);
-            Sum3 su = row_sum3(L_, C_, R_);
-            ld(ra, L_, C_, R_);
-            Sum3 sc = row_sum3(L_, C_, R_);
-            uint32_t c = C_;
+            int w[2], wl[2], wr[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                w[j] = cb + j * Wc;
+                wl[j] = w[j] == 0 ? W - 1 : w[j] - 1;
+                wr[j] = w[j] == W - 1 ? 0 : w[j] + 1;
+            }
+            ColState st[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                if (j >= cols) break;
+                st[j].su = load_sum3<WRAP>(src + (ra - 1) * W, w[j], wl[j], wr[j], W);
+                st[j].sc = load_sum3<WRAP>(src + ra * W, w[j], wl[j], wr[j], W);
+                st[j].c = src[ra * W + w[j]];
+            }
             for (int r = ra; r < rb; ++r) {
-                ld(r + 1, L_, C_, R_);
-                const Sum3 sd = row_sum3(L_, C_, R_);
-                uint32_t nx = rule_from_total<CONWAY>(total9(su, sc, sd), c, p.birth, p.survive);
-                if (!p.wrap) {
+                const uint32_t* nrow = src + (r + 1) * W;
+                bool dead_row = false;
+                if (!WRAP) {
                     const int gy = y0 - k + r;
-                    if (gy < 0 || gy >= p.n1) nx = 0u;   // rows outside the grid stay dead
+                    dead_row = gy < 0 || gy >= p.n1;   // rows outside the grid stay dead
                 }
-                dst[r * W + w] = nx;
-                su = sc;
-                sc = sd;
-                c = C_;
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    if (j >= cols) break;
+                    const Sum3 sd = load_sum3<WRAP>(nrow, w[j], wl[j], wr[j], W);
+                    const uint32_t cd = nrow[w[j]];
+                    uint32_t nx = rule_from_total<CONWAY>(total9(st[j].su, st[j].sc, sd), st[j].c, p.birth, p.survive);
+                    if (dead_row) nx = 0u;
+                    dst[r * W + w[j]] = nx;
+                    st[j].su = st[j].sc;
+                    st[j].sc = sd;
+                    st[j].c = cd;
+                }
             }
         }
         __syncthreads();
@@ -162,6 +184,23 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
         const int gy = y0 + r;
         if (gy < p.n1) p.out[(size_t)gy * W + w] = fin[(size_t)(r + k) * W + w];
     }
+}
+
+// launch one k-generation pass (both entry points use this)
+static cudaError_t life_launch(const LifeParams& lp, bool conway, int grid, size_t smem, cudaStream_t s) {
+#define STC_LIFE_LAUNCH(C, WR)                                                                       \
+    {                                                                                                \
+        cudaError_t e = cudaFuncSetAttribute(life_block_kernel<C, WR>,                                \
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        if (e != cudaSuccess) return e;                                                              \
+        life_block_kernel<C, WR><<<grid, kLifeThreads, smem, s>>>(lp);                               \
+        return cudaGetLastError();                                                                   \
+    }
+    if (conway && lp.wrap) STC_LIFE_LAUNCH(true, true)
+    if (conway) STC_LIFE_LAUNCH(true, false)
+    if (lp.wrap) STC_LIFE_LAUNCH(false, true)
+    STC_LIFE_LAUNCH(false, false)
+#undef STC_LIFE_LAUNCH
 }
 
 // ------------------------------------------------------------------ pack / unpack
@@ -313,15 +352,8 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         const size_t smem = (size_t)2 * (TB + 2 * k) * W * 4;
         const int grid = (int)((n1 + TB - 1) / TB);
         void* prof = prof_begin(stream);
-        if (conway) {
-            cudaFuncSetAttribute(life_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            life_block_kernel<true><<<grid, kLifeThreads, smem, stream>>>(lp);
-        } else {
-            cudaFuncSetAttribute(life_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            life_block_kernel<false><<<grid, kLifeThreads, smem, stream>>>(lp);
-        }
+        e = life_launch(lp, conway, grid, smem, stream);
         prof_end(prof, stream, "life_block", 2.0 * n0 * n1 * k, (double)n0 * n1 * k);
-        e = cudaGetLastError();
         if (e != cudaSuccess) { cudaFreeAsync(P, stream); return cuda_fail(e); }
         cur = 1 - cur;
         left -= k;
@@ -459,14 +491,7 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
         lp.k = k;
         const size_t smem = (size_t)2 * (TB + 2 * k) * W * 4;
         const int grid = (int)((n1 + TB - 1) / TB);
-        if (conway) {
-            cudaFuncSetAttribute(life_block_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            life_block_kernel<true><<<grid, kLifeThreads, smem, s>>>(lp);
-        } else {
-            cudaFuncSetAttribute(life_block_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            life_block_kernel<false><<<grid, kLifeThreads, smem, s>>>(lp);
-        }
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e);
+        if ((e = life_launch(lp, conway, grid, smem, s)) != cudaSuccess) return cuda_fail(e);
         cur = 1 - cur;
         left -= k;
     }

@@ -56,6 +56,9 @@ struct MapParams {
     int32_t L;
     uint32_t birth, survive;
     float rcp_f;               // RN(1/L) in float, used when fastdiv_f (host-verified exact for this L)
+    float Lf;                  // L and alpha pre-converted, so kernels never convert per cell
+    double Ld;
+    float alpha_f;
     int32_t fastdiv_f;
     int8_t off[STC_MAX_LEN][3];
     float wf[STC_MAX_LEN];
@@ -74,15 +77,15 @@ struct MapParams {
 template <class P> __device__ __forceinline__ float div_by_len(float a, const P& p) {
     if (p.fastdiv_f && fabsf(a) >= 0x1p-90f && fabsf(a) <= 3.0e38f) {
         const float q = __fmul_rn(a, p.rcp_f);
-        const float e = __fmaf_rn(-q, (float)p.L, a);
+        const float e = __fmaf_rn(-q, p.Lf, a);
         return __fmaf_rn(e, p.rcp_f, q);
     }
-    return __fdiv_rn(a, (float)p.L);
+    return __fdiv_rn(a, p.Lf);
 }
 // Float64 uses the IEEE division: on GB300 every FP64 instruction is costly, and a verified FMA
 // quotient needs more of them than __ddiv_rn.
 template <class P> __device__ __forceinline__ double div_by_len(double a, const P& p) {
-    return __ddiv_rn(a, (double)p.L);
+    return __ddiv_rn(a, p.Ld);
 }
 
 template <class Tin, class Tout, class Acc> struct OpMean {
@@ -191,15 +194,15 @@ template <class Tin, class Tout, class Acc> struct OpDiffuse {
     template <class P> __device__ static Tout finish(A s, Tin cv, const P& p) {
         if constexpr (sizeof(A) == 8) {
             double c = cvt_d(cv);
-            double t = __dmul_rn((double)p.L, c);
+            double t = __dmul_rn(p.Ld, c);
             t = __dsub_rn(s, t);
             t = __dmul_rn(p.alpha, t);
             return from_f64<Tout>(__dadd_rn(c, t));
         } else {
             float c = cvt_f(cv);
-            float t = __fmul_rn((float)p.L, c);
+            float t = __fmul_rn(p.Lf, c);
             t = __fsub_rn(s, t);
-            t = __fmul_rn((float)p.alpha, t);
+            t = __fmul_rn(p.alpha_f, t);
             return from_f32<Tout>(__fadd_rn(c, t));
         }
     }

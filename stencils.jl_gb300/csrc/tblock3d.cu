@@ -52,6 +52,9 @@ struct TBParams {
     double alpha;
     float rcp_f;
     int32_t fastdiv_f;
+    float Lf;
+    double Ld;
+    float alpha_f;
     float wf[64];
     double w[64];
 };
@@ -311,6 +314,9 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     p.alpha = op->alpha;
     p.rcp_f = (float)(1.0 / (double)st->len);
     p.fastdiv_f = (opv == OPV_MEAN && a->dtype != STC_F64) ? (int)fastdiv_f_exact(st->len) : 0;
+    p.Lf = (float)st->len;
+    p.Ld = (double)st->len;
+    p.alpha_f = (float)op->alpha;
     p.TX = 64;
     p.TY = 16;
     const int smem_cap = 200 * 1024;
@@ -320,7 +326,7 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     p.ntx = (int)((p.n[0] + p.TX - 1) / p.TX);
     p.nty = (int)((p.n[1] + p.TY - 1) / p.TY);
     const int64_t xy = (int64_t)p.ntx * p.nty;
-    p.nzc = (int)std::max<int64_t>(1, std::min<int64_t>(p.n[2] / 16, (2 * ctx->num_sms + xy - 1) / xy));
+    p.nzc = (int)std::max<int64_t>(1, std::min<int64_t>(p.n[2] / 32, (4 * ctx->num_sms + xy - 1) / xy));
     p.ZC = (int)((p.n[2] + p.nzc - 1) / p.nzc);
     p.nzc = (int)((p.n[2] + p.ZC - 1) / p.ZC);
     // launches: the first nsteps-1 steps, split so that state nsteps-1 ends in the parent the reference
