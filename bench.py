@@ -111,6 +111,12 @@ class ClockSampler:
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
 
+    def wait_first(self, timeout_s: float):
+        """Block until the sampler has produced its first line (or timeout_s passes)."""
+        t0 = time.perf_counter()
+        while self.proc is not None and not self.lines and time.perf_counter() - t0 < timeout_s:
+            time.sleep(0.02)
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
@@ -172,9 +178,11 @@ def run_reference(args):
         return 0
     from oracle import oracle as orc
     orc.build()
-    # calibrate a bounded sample: generations per step so that one step takes about 3 s
+    # calibrate a bounded sample: generations per step so that one step takes about 3 s, less when many
+    # steps are asked for (the whole run stays near a minute)
+    per_step = min(3.0, max(0.2, 60.0 / max(1, args.warmup + args.steps)))
     _, threads, _, _ = cpu_life_rate(0.5)
-    rate1, _, gens, _ = cpu_life_rate(3.0, threads)
+    rate1, _, gens, _ = cpu_life_rate(per_step, threads)
     st = entry.load_package()
     A = __import__("stencils_gb300._abi", fromlist=["x"])
     a0 = initial_grid()
@@ -225,28 +233,37 @@ def run_gpu(args):
         S = st.mapstencil_(st.life, S, steps=GENERATIONS)
     torch.cuda.synchronize()
 
+    def timed_pass(profile: bool):
+        """K steps bracketed by barrier + synchronize; device seconds of the steps (CUDA events)."""
+        nonlocal S
+        barrier()
+        torch.cuda.synchronize()
+        _lib.profile_enable(profile)
+        evs = []
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            S = st.mapstencil_(st.life, S, steps=GENERATIONS)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        prof = _lib.profile_report() if profile else {}
+        _lib.profile_enable(False)
+        barrier()
+        return sum(a.elapsed_time(b) for a, b in evs) / 1e3, prof
+
+    # value: the timed region without per-launch events; the roofline's per-launch durations come from
+    # a second pass of the same K steps with an event pair around every library launch
     clocks = ClockSampler(local)
-    barrier()
-    torch.cuda.synchronize()
     clocks.start()
-    _lib.profile_enable(True)
-    evs = []
+    clocks.wait_first(3.0)
     t_wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        S = st.mapstencil_(st.life, S, steps=GENERATIONS)
-        e1.record(stream)
-        evs.append((e0, e1))
-    torch.cuda.synchronize()
+    dev_s, _ = timed_pass(False)
     wall = time.perf_counter() - t_wall0
-    prof = _lib.profile_report()
-    _lib.profile_enable(False)
+    _, prof = timed_pass(True)
     clk = clocks.stop()
-    barrier()
-    dev_s = sum(a.elapsed_time(b) for a, b in evs) / 1e3
     dev_s_max = max_over_ranks(dev_s, dev)
     value = ws * args.steps * updates_per_step / dev_s_max / 1e9
 
@@ -622,7 +639,7 @@ WORKLOADS = {"mean_blur": run_mean_blur, "gauss": run_gauss, "diffusion": run_di
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
