@@ -16,6 +16,7 @@
 // The neighbour count is the count of nonzero neighbours, exactly what the LIFE op counts, so the
 // result is bit-identical to the per-cell gather for any input values.
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -102,6 +103,88 @@ __device__ __forceinline__ Sum3 load_sum3(const uint32_t* row, int w, int wl, in
     return row_sum3(L, C, R);
 }
 
+// A thread's fixed share of a band: columns w and w + W/2 (two independent adder networks that
+// interleave; one column when W is odd) and strip s of `strips` row strips.  Computed once per kernel.
+struct LifeLane {
+    int cols;            // 0 (idle thread), 1 or 2
+    int w[2], wl[2], wr[2];
+    int s, strips;
+    float inv_strips;
+};
+
+__device__ __forceinline__ LifeLane life_lane(int W) {
+    LifeLane L;
+    const int cols = (W % 2 == 0) ? 2 : 1;
+    const int Wc = W / cols;
+    L.strips = max(1, (int)blockDim.x / Wc);
+    L.inv_strips = 1.0f / (float)L.strips;
+    const int item = threadIdx.x;
+    L.cols = item < Wc * L.strips ? cols : 0;
+    const int cb = item % Wc;
+    L.s = item / Wc;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        L.w[j] = cb + j * Wc;
+        L.wl[j] = L.w[j] == 0 ? W - 1 : L.w[j] - 1;
+        L.wr[j] = L.w[j] == W - 1 ? 0 : L.w[j] + 1;
+    }
+    return L;
+}
+
+// Advance a band kk generations in the shared ping-pong pair (cur, oth).  cur holds `rows` valid rows
+// of W words; row r is global row gy_first + r.  Generation g computes rows [g+1, rows-g-1) (the
+// rows whose three source rows are still valid) into the other buffer, split into the lanes' strips.
+// Returns the buffer holding the result.  Ends with a barrier.
+template <bool CONWAY, bool WRAP>
+__device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
+                                               int kk, int gy_first, int n1, uint32_t birth, uint32_t survive) {
+    for (int g = 0; g < kk; ++g) {
+        const uint32_t* src = cur;
+        uint32_t* dst = oth;
+        const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of src
+        const int nr = hi - lo;
+        // strip bounds: the same monotone expression for a strip's end and the next strip's start, so
+        // the strips tile [lo, hi) exactly whatever the float rounding
+        const int ra = lo + (int)((float)(nr * L.s) * L.inv_strips);
+        const int rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
+        if (L.cols > 0 && ra < rb) {
+            ColState st[2];
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                if (j >= L.cols) break;
+                st[j].su = load_sum3<WRAP>(src + (ra - 1) * W, L.w[j], L.wl[j], L.wr[j], W);
+                st[j].sc = load_sum3<WRAP>(src + ra * W, L.w[j], L.wl[j], L.wr[j], W);
+                st[j].c = src[ra * W + L.w[j]];
+            }
+            for (int r = ra; r < rb; ++r) {
+                const uint32_t* nrow = src + (r + 1) * W;
+                bool dead_row = false;
+                if (!WRAP) {
+                    const int gy = gy_first + r;
+                    dead_row = gy < 0 || gy >= n1;   // rows outside the grid stay dead
+                }
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    if (j >= L.cols) break;
+                    const Sum3 sd = load_sum3<WRAP>(nrow, L.w[j], L.wl[j], L.wr[j], W);
+                    const uint32_t cd = nrow[L.w[j]];
+                    uint32_t nx = rule_from_total<CONWAY>(total9(st[j].su, st[j].sc, sd), st[j].c, birth, survive);
+                    if (dead_row) nx = 0u;
+                    dst[r * W + L.w[j]] = nx;
+                    st[j].su = st[j].sc;
+                    st[j].sc = sd;
+                    st[j].c = cd;
+                }
+            }
+        }
+        __syncthreads();
+        uint32_t* t = cur;
+        cur = oth;
+        oth = t;
+    }
+    return cur;
+}
+
 template <bool CONWAY, bool WRAP>
 __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifeParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
@@ -125,64 +208,129 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
         buf0[i] = v;
     }
     __syncthreads();
-    // Thread -> (column pair, strip).  Each thread carries two independent columns (w and w + W/2
-    // when W is even) through its strip of rows, so the two adder networks interleave.  Strips split
-    // the valid row range of each generation.
-    const int cols = (W % 2 == 0) ? 2 : 1;
-    const int Wc = W / cols;
-    const int strips = max(1, (int)blockDim.x / Wc);
-    for (int g = 0; g < k; ++g) {
-        const uint32_t* src = (g & 1) ? buf1 : buf0;
-        uint32_t* dst = (g & 1) ? buf0 : buf1;
-        const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of src
-        const int nr = hi - lo;
-        for (int item = threadIdx.x; item < Wc * strips; item += blockDim.x) {
-            const int cb = item % Wc, s = item / Wc;
-            const int ra = lo + (nr * s) / strips, rb = lo + (nr * (s + 1)) / strips;
-            if (ra >= rb) continue;
-            int w[2], wl[2], wr[2];
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                w[j] = cb + j * Wc;
-                wl[j] = w[j] == 0 ? W - 1 : w[j] - 1;
-                wr[j] = w[j] == W - 1 ? 0 : w[j] + 1;
-            }
-            ColState st[2];
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                if (j >= cols) break;
-                st[j].su = load_sum3<WRAP>(src + (ra - 1) * W, w[j], wl[j], wr[j], W);
-                st[j].sc = load_sum3<WRAP>(src + ra * W, w[j], wl[j], wr[j], W);
-                st[j].c = src[ra * W + w[j]];
-            }
-            for (int r = ra; r < rb; ++r) {
-                const uint32_t* nrow = src + (r + 1) * W;
-                bool dead_row = false;
-                if (!WRAP) {
-                    const int gy = y0 - k + r;
-                    dead_row = gy < 0 || gy >= p.n1;   // rows outside the grid stay dead
-                }
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    if (j >= cols) break;
-                    const Sum3 sd = load_sum3<WRAP>(nrow, w[j], wl[j], wr[j], W);
-                    const uint32_t cd = nrow[w[j]];
-                    uint32_t nx = rule_from_total<CONWAY>(total9(st[j].su, st[j].sc, sd), st[j].c, p.birth, p.survive);
-                    if (dead_row) nx = 0u;
-                    dst[r * W + w[j]] = nx;
-                    st[j].su = st[j].sc;
-                    st[j].sc = sd;
-                    st[j].c = cd;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    const uint32_t* fin = (k & 1) ? buf1 : buf0;
+    const LifeLane lane = life_lane(W);
+    const uint32_t* fin = life_gens<CONWAY, WRAP>(lane, buf0, buf1, rows, W, k, y0 - k, p.n1, p.birth, p.survive);
     for (int i = threadIdx.x; i < p.TB * W; i += blockDim.x) {
         const int r = i / W, w = i - r * W;
         const int gy = y0 + r;
         if (gy < p.n1) p.out[(size_t)gy * W + w] = fin[(size_t)(r + k) * W + w];
+    }
+}
+
+// ------------------------------------------------------------------ persistent (cooperative) variant
+// One launch runs every generation.  CTA b keeps its band (rows [y0, y1), balanced split of n1) in
+// shared memory for the whole run, with k ghost rows above and below.  A super-step advances the band
+// kk <= k generations; then the CTA publishes its first and last k band rows to an exchange slot in
+// global memory, each word as a 64-bit (super-step tag, word) pair written with a single relaxed
+// gpu-scope store.  Before the next super-step every thread reloads its share of the neighbours'
+// rows until each pair carries the expected tag (bounded) and copies the words in as ghost rows.  No
+// fence or flag sits on the critical path: a pair is atomic, so a matching tag means the word is the
+// one published for that super-step.  Two slots alternate: a neighbour overwrites a slot only after
+// it has read this CTA's following publication, which this CTA makes after reading that slot.
+// Every CTA must be resident at once (cooperative launch), and each band holds at least k rows, so
+// ghost rows come only from the adjacent bands.
+struct LifeCoopParams {
+    const uint32_t* in;   // generation 0; receives generation n-1 (n > 1) once neighbours stopped reading it
+    uint32_t* prev;       // == in
+    uint32_t* last;       // generation n
+    uint64_t* xbuf;       // [2 slots][grid][2 (first, last rows)][k][W] tagged words, zero before launch
+    int* status;
+    int W, n1, k;
+    int64_t nsteps;
+    uint32_t birth, survive;
+};
+
+__device__ __forceinline__ uint64_t ld_relaxed_gpu(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// the word of a tagged pair once its tag equals `tag`; false after ~limit SM clocks
+__device__ __forceinline__ bool take_tagged(const uint64_t* p, uint32_t tag, uint32_t* out,
+                                            long long limit = 4000000000ll) {
+    uint64_t v = ld_relaxed_gpu(p);
+    if ((uint32_t)(v >> 32) != tag) {
+        const long long t0 = clock64();
+        do {
+            if (clock64() - t0 > limit) return false;
+            v = ld_relaxed_gpu(p);
+        } while ((uint32_t)(v >> 32) != tag);
+    }
+    *out = (uint32_t)v;
+    return true;
+}
+
+template <bool CONWAY, bool WRAP>
+__global__ void __launch_bounds__(kLifeThreads) life_coop_kernel(const LifeCoopParams p) {
+    extern __shared__ __align__(16) uint32_t lsm[];
+    const int W = p.W, k = p.k, G = gridDim.x, b = blockIdx.x;
+    const int y0 = (int)(((int64_t)b * p.n1) / G), y1 = (int)(((int64_t)(b + 1) * p.n1) / G);
+    const int TB = y1 - y0, rows = TB + 2 * k;
+    const int TBmax = (p.n1 + G - 1) / G;
+    uint32_t* cur = lsm;
+    uint32_t* oth = lsm + (size_t)(TBmax + 2 * k) * W;
+    for (int i = threadIdx.x; i < rows * W; i += blockDim.x) {
+        const int r = i / W, w = i - r * W;
+        int gy = y0 - k + r;
+        uint32_t v = 0;
+        if (WRAP) {
+            gy = gy < 0 ? gy + p.n1 : (gy >= p.n1 ? gy - p.n1 : gy);
+            v = p.in[(size_t)gy * W + w];
+        } else if (gy >= 0 && gy < p.n1) {
+            v = p.in[(size_t)gy * W + w];
+        }
+        cur[i] = v;
+    }
+    __syncthreads();
+    const int up = b == 0 ? G - 1 : b - 1, dn = b == G - 1 ? 0 : b + 1;
+    const bool has_up = WRAP || b > 0, has_dn = WRAP || b < G - 1;
+    const size_t slab = (size_t)k * W;                 // one published row block
+    const int64_t nmain = p.nsteps - 1;                // generations before the last one
+    const LifeLane lane = life_lane(W);
+    int64_t gen = 0;
+    for (int step = 0;; ++step) {
+        const bool final = gen >= nmain;
+        const int kk = final ? 1 : (int)min((int64_t)k, nmain - gen);
+        if (step > 0) {
+            // ghost rows: the neighbours' publication of super-step step-1 (tag step)
+            const uint64_t* xs = p.xbuf + (size_t)((step - 1) & 1) * G * 2 * slab;
+            const uint64_t* from_up = xs + ((size_t)up * 2 + 1) * slab;   // neighbour's last k rows
+            const uint64_t* from_dn = xs + ((size_t)dn * 2 + 0) * slab;   // neighbour's first k rows
+            bool ok = true;
+            for (int i = threadIdx.x; i < (int)slab; i += blockDim.x) {
+                uint32_t u = 0u, d = 0u;
+                if (has_up && ok) ok = take_tagged(from_up + i, (uint32_t)step, &u);
+                if (has_dn && ok) ok = take_tagged(from_dn + i, (uint32_t)step, &d);
+                cur[i] = u;
+                cur[(size_t)(k + TB) * W + i] = d;
+            }
+            if (!__syncthreads_and(ok)) {
+                if (threadIdx.x == 0 && p.status) atomicOr(p.status, DEV_ERR_TIMEOUT);
+                return;
+            }
+            if (final && p.nsteps > 1) {
+                // generation n-1: every thread has seen both neighbours' publications (so they are past
+                // their initial load), and nobody reads `in` any more
+                for (int i = threadIdx.x; i < TB * W; i += blockDim.x) p.prev[(size_t)y0 * W + i] = cur[(size_t)k * W + i];
+            }
+        }
+        cur = life_gens<CONWAY, WRAP>(lane, cur, oth, rows, W, kk, y0 - k, p.n1, p.birth, p.survive);
+        oth = (cur == lsm) ? lsm + (size_t)(TBmax + 2 * k) * W : lsm;
+        gen += kk;
+        if (final) {
+            for (int i = threadIdx.x; i < TB * W; i += blockDim.x) p.last[(size_t)y0 * W + i] = cur[(size_t)k * W + i];
+            return;
+        }
+        uint64_t* xd = p.xbuf + (size_t)(step & 1) * G * 2 * slab + (size_t)b * 2 * slab;
+        const uint64_t tag = (uint64_t)(uint32_t)(step + 1) << 32;
+        for (int i = threadIdx.x; i < (int)slab; i += blockDim.x) {
+            st_relaxed_gpu(xd + i, tag | cur[(size_t)k * W + i]);            // band rows y0 .. y0+k-1
+            st_relaxed_gpu(xd + slab + i, tag | cur[(size_t)TB * W + i]);    // band rows y1-k .. y1-1
+        }
     }
 }
 
@@ -306,6 +454,120 @@ void life_plan(int W, int n1, int64_t steps_left, int smem_cap, int num_sms, int
     *k = kk;
 }
 
+// Generations per super-step of the persistent kernel (ghost depth).  Tuning overrides, read per call:
+// STC_LIFE_K = depth (1..32), STC_LIFE_COOP = 0 keeps the multi-launch kernel.
+static int life_coop_depth() {
+    const char* e = getenv("STC_LIFE_K");
+    const int v = e ? atoi(e) : 0;
+    return (v >= 1 && v <= 32) ? v : 8;
+}
+static bool life_coop_enabled() {
+    const char* e = getenv("STC_LIFE_COOP");
+    return !(e && e[0] == '0');
+}
+
+template <bool C, bool WR>
+static cudaError_t coop_fits_t(int grid, size_t smem, int num_sms, bool* fits) {
+    auto fn = life_coop_kernel<C, WR>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kLifeThreads, smem);
+    *fits = e == cudaSuccess && (int64_t)nb * num_sms >= grid;
+    return e;
+}
+
+template <bool C, bool WR>
+static cudaError_t coop_launch_t(const LifeCoopParams& cp, int grid, size_t smem, cudaStream_t s) {
+    LifeCoopParams arg = cp;
+    void* args[] = {&arg};
+    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR>, dim3(grid), dim3(kLifeThreads), args,
+                                       smem, s);
+}
+
+// The persistent path: every generation in one cooperative launch.  Returns STC_OK with *done = nsteps
+// when it ran, STC_OK with *done = 0 when the grid does not suit it (caller falls back).
+static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* op, bool halo, bool wrap, int64_t n0,
+                           int64_t n1, int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx,
+                           int64_t* done) {
+    *done = 0;
+    if (!life_coop_enabled()) return STC_OK;
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop) {
+        cudaGetLastError();
+        return STC_OK;
+    }
+    const int W = (int)(n0 / 32);
+    int k = (int)std::min<int64_t>(life_coop_depth(), std::max<int64_t>(1, nsteps - 1));
+    int G = (int)std::min<int64_t>(ctx->num_sms, n1 / k);
+    if (G < 1) {
+        G = 1;
+        k = (int)n1;
+    }
+    const int TBmax = (int)((n1 + G - 1) / G);
+    const size_t smem = (size_t)2 * (TBmax + 2 * k) * W * 4;
+    if ((int64_t)smem > ctx->max_smem_optin - 1024) return STC_OK;
+
+    const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
+    bool fits = false;
+    cudaError_t e;
+    if (conway && wrap) e = coop_fits_t<true, true>(G, smem, ctx->num_sms, &fits);
+    else if (conway) e = coop_fits_t<true, false>(G, smem, ctx->num_sms, &fits);
+    else if (wrap) e = coop_fits_t<false, true>(G, smem, ctx->num_sms, &fits);
+    else e = coop_fits_t<false, false>(G, smem, ctx->num_sms, &fits);
+    if (e != cudaSuccess) return cuda_fail(e);
+    if (!fits) return STC_OK;   // not enough co-resident CTAs: the caller uses the multi-launch kernel
+
+    const size_t words = (size_t)W * n1;
+    const size_t xwords = (size_t)2 * G * 2 * k * W;
+    char* mem = nullptr;
+    const size_t bytes = xwords * sizeof(uint64_t) + 2 * words * sizeof(uint32_t);
+    e = cudaMallocAsync((void**)&mem, bytes, stream);
+    if (e != cudaSuccess) return cuda_fail(e);
+    uint64_t* X = (uint64_t*)mem;
+    uint32_t* P0 = (uint32_t*)(X + xwords);
+    uint32_t* P1 = P0 + words;
+    const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
+    int rc = launch_pack(true, a, org_a, W, (int)n1, P0, stream, ctx->num_sms);
+    if (!rc) rc = cuda_fail(cudaMemsetAsync(X, 0, xwords * sizeof(uint64_t), stream));   // no stale tags
+    if (rc) { cudaFreeAsync(mem, stream); return rc; }
+    LifeCoopParams cp{};
+    cp.in = P0;
+    cp.prev = P0;
+    cp.last = P1;
+    cp.xbuf = X;
+    cp.status = ctx->status;
+    cp.W = W;
+    cp.n1 = (int)n1;
+    cp.k = k;
+    cp.nsteps = nsteps;
+    cp.birth = op->birth_mask;
+    cp.survive = op->survive_mask;
+    void* prof = prof_begin(stream);
+    if (conway && wrap) e = coop_launch_t<true, true>(cp, G, smem, stream);
+    else if (conway) e = coop_launch_t<true, false>(cp, G, smem, stream);
+    else if (wrap) e = coop_launch_t<false, true>(cp, G, smem, stream);
+    else e = coop_launch_t<false, false>(cp, G, smem, stream);
+    if (e != cudaSuccess) {
+        prof_end(prof, stream, "life_coop", 0.0, 0.0);
+        cudaFreeAsync(mem, stream);
+        return cuda_fail(e);
+    }
+    prof_end(prof, stream, "life_coop", 2.0 * n0 * n1 * nsteps, (double)n0 * n1 * nsteps);
+    // P1 holds generation nsteps, P0 generation nsteps-1 (the input when nsteps == 1).  The reference
+    // leaves the result in b after an odd number of steps, in a after an even number.
+    const bool res_in_b = (nsteps & 1) != 0;
+    const stc_grid* res = res_in_b ? b : a;
+    const stc_grid* prev = res_in_b ? a : b;
+    rc = launch_pack(false, res, res_in_b ? org_b : org_a, W, (int)n1, P1, stream, ctx->num_sms);
+    if (!rc && nsteps > 1) rc = launch_pack(false, prev, res_in_b ? org_a : org_b, W, (int)n1, P0, stream, ctx->num_sms);
+    cudaFreeAsync(mem, stream);
+    if (rc) return rc;
+    *src_is_b = res_in_b ? 1 : 0;
+    *done = nsteps;
+    return STC_OK;
+}
+
 int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
                    int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx, int64_t* done) {
     *done = 0;
@@ -317,6 +579,8 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     if (!wrap && !remove0) return STC_OK;   // Reflect / Use / nonzero padval take the per-step kernel
     const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
     if (n0 < 32 || n0 % 32 != 0 || n1 < 1 || n0 / 32 > 512 || n1 > (1 << 30)) return STC_OK;
+    int rc = life_coop_steps(a, b, op, halo, wrap, n0, n1, nsteps, src_is_b, stream, ctx, done);
+    if (rc || *done) return rc;
     const int W = (int)(n0 / 32);
     const int smem_cap = ctx->max_smem_optin - 1024;
     int TB, k;
@@ -329,7 +593,7 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     if (e != cudaSuccess) return cuda_fail(e);
     uint32_t* Pbuf[2] = {P, P + words};
     const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
-    int rc = launch_pack(true, a, org_a, W, (int)n1, Pbuf[0], stream, ctx->num_sms);
+    rc = launch_pack(true, a, org_a, W, (int)n1, Pbuf[0], stream, ctx->num_sms);
     if (rc) { cudaFreeAsync(P, stream); return rc; }
 
     LifeParams lp{};

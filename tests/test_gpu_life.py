@@ -59,7 +59,7 @@ def test_life_4096_every_100_steps(cuda, st, orc, abi):
         S = st.mapstencil_(st.life, S, steps=100)
         kern = _lib.profile_report()
         _lib.profile_enable(False)
-        assert "life_block" in kern and "map_shape_ldg" not in kern
+        assert ("life_coop" in kern or "life_block" in kern) and "map_shape_ldg" not in kern
         ref, _, _ = _oracle_steps(orc, abi, st, ref, abi.U8, st.life, st.Wrap(), st.Conditional(), 100)
         got = _logical(S.source, pad, st)
         assert np.array_equal(got, ref), f"differs after {100 * (chunk + 1)} generations"
@@ -81,7 +81,7 @@ def test_life_variants(cuda, st, orc, abi, dtype, bname, pname, steps):
     pad = st.Halo("out") if pname == "halo_out" else st.Conditional()
     dev = st.to_device(a.astype(np.bool_)) if dtype == "bool" else st.to_device(a)
     S2, kern = _gpu_run(st, dev, st.life, bnd, pad, steps)
-    assert "life_block" in kern
+    assert "life_coop" in kern or "life_block" in kern
     res, prev, in_b = _oracle_steps(orc, abi, st, a, code, st.life, bnd, st.Conditional(), steps)
     assert np.array_equal(_logical(S2.source, pad, st).astype(npdt), res)
     if steps > 1:
@@ -97,7 +97,7 @@ def test_life_other_rule_and_small_grids(cuda, st, orc, abi):
         a = np.asfortranarray((rng.random(shape) < 0.4).astype(np.uint8))
         for bnd in (st.Wrap(), st.Remove(0)):
             S2, kern = _gpu_run(st, st.to_device(a), rule, bnd, st.Conditional(), 45)
-            assert "life_block" in kern
+            assert "life_coop" in kern or "life_block" in kern
             res, _, _ = _oracle_steps(orc, abi, st, a, abi.U8, rule, bnd, st.Conditional(), 45)
             assert np.array_equal(_logical(S2.source, st.Conditional(), st), res), (shape, rule.name, bnd)
 
@@ -111,3 +111,25 @@ def test_life_fallback_shapes_still_exact(cuda, st, orc, abi):
         assert "life_block" not in kern
         res, _, _ = _oracle_steps(orc, abi, st, a, abi.U8, st.life, bnd, st.Conditional(), 9)
         assert np.array_equal(_logical(S2.source, st.Conditional(), st), res)
+
+
+@pytest.mark.parametrize("depth", ["1", "2", "5", "8", "13", "multi-launch"])
+@pytest.mark.parametrize("bname", ["wrap", "remove0"])
+def test_life_persistent_depths(cuda, st, orc, abi, monkeypatch, depth, bname):
+    """The persistent kernel at several ghost depths (super-step lengths, including depths that do not
+    divide the step count) and the multi-launch kernel, on a grid split over many bands."""
+    from stencils_gb300 import _lib
+    if depth == "multi-launch":
+        monkeypatch.setenv("STC_LIFE_COOP", "0")
+    else:
+        monkeypatch.setenv("STC_LIFE_K", depth)
+    rng = np.random.default_rng(31 + len(depth))
+    a = np.asfortranarray((rng.random((1024, 700)) < 0.33).astype(np.uint8))
+    bnd = st.Wrap() if bname == "wrap" else st.Remove(0)
+    for steps in (1, 2, 29):
+        S2, kern = _gpu_run(st, st.to_device(a), st.life, bnd, st.Conditional(), steps)
+        assert ("life_block" if depth == "multi-launch" else "life_coop") in kern, kern
+        res, prev, _ = _oracle_steps(orc, abi, st, a, abi.U8, st.life, bnd, st.Conditional(), steps)
+        assert np.array_equal(_logical(S2.source, st.Conditional(), st), res), (depth, steps)
+        if steps > 1:
+            assert np.array_equal(_logical(S2.dest, st.Conditional(), st), prev), (depth, steps)
