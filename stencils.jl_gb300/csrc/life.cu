@@ -28,53 +28,50 @@ namespace stc {
 
 constexpr int kLifeThreads = 512;
 
-struct Count4 { uint32_t b0, b1, b2, b3; };
-
 __device__ __forceinline__ void full_add(uint32_t a, uint32_t b, uint32_t c, uint32_t& s, uint32_t& cy) {
     const uint32_t t = a ^ b;
     s = t ^ c;
     cy = (a & b) | (t & c);
 }
 
-// 3-cell horizontal sum of a row around every bit: (a, b) with L + C + R = a + 2b
-struct Sum3 { uint32_t a, b; };
-__device__ __forceinline__ Sum3 row_sum3(uint32_t wl, uint32_t c, uint32_t wr) {
+// One source row seen from one column word: its 3-cell sums around every bit (a3 + 2 b3 = L + C + R,
+// used when the row is above or below the output row), its 2-cell sums (a2 + 2 b2 = L + R, used when
+// it is the output's own row) and the centre word itself.
+struct RowV { uint32_t a3, b3, a2, b2, c; };
+
+__device__ __forceinline__ RowV row_v(uint32_t wl, uint32_t c, uint32_t wr) {
     const uint32_t L = __funnelshift_l(wl, c, 1), R = __funnelshift_r(c, wr, 1);
-    Sum3 s;
-    s.a = L ^ c ^ R;
-    s.b = (L & c) | (R & (L ^ c));
-    return s;
+    RowV v;
+    v.a3 = L ^ c ^ R;
+    v.b3 = (L & c) | (R & (L ^ c));
+    v.a2 = L ^ R;
+    v.b2 = L & R;
+    v.c = c;
+    return v;
 }
 
-// 4-bit total of the 3x3 block (centre included) from three rows' 3-cell sums
-__device__ __forceinline__ Count4 total9(const Sum3& u, const Sum3& c, const Sum3& d) {
-    Count4 t;
-    uint32_t k0, x1, k1;
-    full_add(u.a, c.a, d.a, t.b0, k0);     // weight 1 and its carry (weight 2)
-    full_add(u.b, c.b, d.b, x1, k1);       // weight 2 and its carry (weight 4)
-    t.b1 = x1 ^ k0;
-    const uint32_t k2 = x1 & k0;           // weight 4
-    t.b2 = k1 ^ k2;
-    t.b3 = k1 & k2;                         // weight 8
-    return t;
-}
-
-// next state from the 3x3 total (neighbour count n = total - centre)
+// next state of the middle row m from the neighbour count n = sum3(u) + sum2(m) + sum3(d), 0..8, held
+// as bit planes n0..n3
 template <bool CONWAY>
-__device__ __forceinline__ uint32_t rule_from_total(const Count4& t, uint32_t c, uint32_t birth, uint32_t survive) {
+__device__ __forceinline__ uint32_t next_state(const RowV& u, const RowV& m, const RowV& d, uint32_t birth,
+                                               uint32_t survive) {
+    uint32_t n0, k0, x1, k1;
+    full_add(u.a3, m.a2, d.a3, n0, k0);    // weight 1 and its carry (weight 2)
+    full_add(u.b3, m.b2, d.b3, x1, k1);    // weight 2 and its carry (weight 4)
+    const uint32_t n1 = x1 ^ k0;
+    const uint32_t n2 = k1 ^ (x1 & k0);
     if constexpr (CONWAY) {
-        // B3/S23: n == 3 (total 3 when dead, 4 when alive) or alive with n == 2 (total 3)
-        const uint32_t is3 = t.b0 & t.b1 & ~t.b2 & ~t.b3;
-        const uint32_t is4 = ~t.b0 & ~t.b1 & t.b2 & ~t.b3;
-        return is3 | (c & is4);
+        // B3/S23: n == 3, or alive with n == 2, i.e. n1 set, n2 clear and (n0 or alive); n == 8 has n1 clear
+        return n1 & ~n2 & (n0 | m.c);
     } else {
+        const uint32_t n3 = k1 & x1 & k0;
         uint32_t out = 0;
 #pragma unroll
-        for (int v = 0; v <= 9; ++v) {
-            const uint32_t m = ((v & 1) ? t.b0 : ~t.b0) & ((v & 2) ? t.b1 : ~t.b1) & ((v & 4) ? t.b2 : ~t.b2) &
-                               ((v & 8) ? t.b3 : ~t.b3);
-            if (v <= 8 && ((birth >> v) & 1u)) out |= m & ~c;             // dead: n = total
-            if (v >= 1 && ((survive >> (v - 1)) & 1u)) out |= m & c;     // alive: n = total - 1
+        for (int v = 0; v <= 8; ++v) {
+            const uint32_t eq = ((v & 1) ? n0 : ~n0) & ((v & 2) ? n1 : ~n1) & ((v & 4) ? n2 : ~n2) &
+                                ((v & 8) ? n3 : ~n3);
+            if ((birth >> v) & 1u) out |= eq & ~m.c;
+            if ((survive >> v) & 1u) out |= eq & m.c;
         }
         return out;
     }
@@ -91,23 +88,12 @@ struct LifeParams {
     uint32_t birth, survive;
 };
 
-// one column's rolling window: the 3-cell sums of the rows above and at the current row, and the
-// current row's own word
-struct ColState { Sum3 su, sc; uint32_t c; };
-
-template <bool WRAP>
-__device__ __forceinline__ Sum3 load_sum3(const uint32_t* row, int w, int wl, int wr, int W) {
-    const uint32_t C = row[w];
-    const uint32_t L = (!WRAP && w == 0) ? 0u : row[wl];
-    const uint32_t R = (!WRAP && w == W - 1) ? 0u : row[wr];
-    return row_sum3(L, C, R);
-}
-
 // A thread's fixed share of a band: columns w and w + W/2 (two independent adder networks that
 // interleave; one column when W is odd) and strip s of `strips` row strips.  Computed once per kernel.
 struct LifeLane {
     int cols;            // 0 (idle thread), 1 or 2
     int w[2], wl[2], wr[2];
+    bool ledge[2], redge[2];
     int s, strips;
     float inv_strips;
 };
@@ -125,57 +111,110 @@ __device__ __forceinline__ LifeLane life_lane(int W) {
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         L.w[j] = cb + j * Wc;
-        L.wl[j] = L.w[j] == 0 ? W - 1 : L.w[j] - 1;
-        L.wr[j] = L.w[j] == W - 1 ? 0 : L.w[j] + 1;
+        L.ledge[j] = L.w[j] == 0;
+        L.redge[j] = L.w[j] == W - 1;
+        L.wl[j] = L.ledge[j] ? W - 1 : L.w[j] - 1;
+        L.wr[j] = L.redge[j] ? 0 : L.w[j] + 1;
     }
     return L;
+}
+
+// Rows [ra, rb) of one strip for NC columns: source row q is read through per-column pointers to
+// its (w-1, w, w+1) words, each row's sums are formed once as it enters a three-row window, and the
+// row walk is unrolled by three with the window's roles rotating, so nothing is copied between
+// registers.  Remove(0) (WRAP false): words beyond the x edges read as zero, and rows outside the grid
+// stay dead.
+template <bool CONWAY, bool WRAP, int WT, int NC>
+__device__ __forceinline__ void life_strip(const LifeLane& L, const uint32_t* src, uint32_t* dst, int Wrt, int ra,
+                                           int rb, int gy_first, int n1, uint32_t birth, uint32_t survive) {
+    const int W = WT > 0 ? WT : Wrt;
+    const uint32_t *pl[NC], *pc[NC], *pr[NC];
+    uint32_t* pd[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        pl[j] = src + (size_t)(ra - 1) * W + L.wl[j];
+        pc[j] = src + (size_t)(ra - 1) * W + L.w[j];
+        pr[j] = src + (size_t)(ra - 1) * W + L.wr[j];
+        pd[j] = dst + (size_t)ra * W + L.w[j];
+    }
+    // row (ra - 1 + q) of column j
+    auto load = [&](int j, int q) -> RowV {
+        const uint32_t c = pc[j][q * W];
+        const uint32_t l = (!WRAP && L.ledge[j]) ? 0u : pl[j][q * W];
+        const uint32_t r = (!WRAP && L.redge[j]) ? 0u : pr[j][q * W];
+        return row_v(l, c, r);
+    };
+    // output row (ra + q) from the window (u, m, d)
+    auto emit = [&](int j, int q, int r, const RowV& u, const RowV& m, const RowV& d) {
+        uint32_t nx = next_state<CONWAY>(u, m, d, birth, survive);
+        if (!WRAP) {
+            const int gy = gy_first + r;
+            if (gy < 0 || gy >= n1) nx = 0u;   // rows outside the grid stay dead
+        }
+        pd[j][q * W] = nx;
+    };
+    RowV v0[NC], v1[NC], v2[NC];
+#pragma unroll
+    for (int j = 0; j < NC; ++j) {
+        v0[j] = load(j, 0);
+        v1[j] = load(j, 1);
+    }
+    int r = ra;
+    // invariant: v0 = row r-1, v1 = row r; pointers at row r-1 (sources) and row r (destination)
+    for (; r + 3 <= rb; r += 3) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) v2[j] = load(j, 2);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) emit(j, 0, r, v0[j], v1[j], v2[j]);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) v0[j] = load(j, 3);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) emit(j, 1, r + 1, v1[j], v2[j], v0[j]);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) v1[j] = load(j, 4);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) emit(j, 2, r + 2, v2[j], v0[j], v1[j]);
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            pl[j] += 3 * W;
+            pc[j] += 3 * W;
+            pr[j] += 3 * W;
+            pd[j] += 3 * W;
+        }
+    }
+    if (r < rb) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) {
+            v2[j] = load(j, 2);
+            emit(j, 0, r, v0[j], v1[j], v2[j]);
+        }
+        if (r + 1 < rb) {
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+                v0[j] = load(j, 3);
+                emit(j, 1, r + 1, v1[j], v2[j], v0[j]);
+            }
+        }
+    }
 }
 
 // Advance a band kk generations in the shared ping-pong pair (cur, oth).  cur holds `rows` valid rows
 // of W words; row r is global row gy_first + r.  Generation g computes rows [g+1, rows-g-1) (the
 // rows whose three source rows are still valid) into the other buffer, split into the lanes' strips.
 // Returns the buffer holding the result.  Ends with a barrier.
-template <bool CONWAY, bool WRAP>
+template <bool CONWAY, bool WRAP, int WT>
 __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
                                                int kk, int gy_first, int n1, uint32_t birth, uint32_t survive) {
     for (int g = 0; g < kk; ++g) {
-        const uint32_t* src = cur;
-        uint32_t* dst = oth;
-        const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of src
+        const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of cur
         const int nr = hi - lo;
         // strip bounds: the same monotone expression for a strip's end and the next strip's start, so
         // the strips tile [lo, hi) exactly whatever the float rounding
         const int ra = lo + (int)((float)(nr * L.s) * L.inv_strips);
         const int rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
-        if (L.cols > 0 && ra < rb) {
-            ColState st[2];
-#pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                if (j >= L.cols) break;
-                st[j].su = load_sum3<WRAP>(src + (ra - 1) * W, L.w[j], L.wl[j], L.wr[j], W);
-                st[j].sc = load_sum3<WRAP>(src + ra * W, L.w[j], L.wl[j], L.wr[j], W);
-                st[j].c = src[ra * W + L.w[j]];
-            }
-            for (int r = ra; r < rb; ++r) {
-                const uint32_t* nrow = src + (r + 1) * W;
-                bool dead_row = false;
-                if (!WRAP) {
-                    const int gy = gy_first + r;
-                    dead_row = gy < 0 || gy >= n1;   // rows outside the grid stay dead
-                }
-#pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    if (j >= L.cols) break;
-                    const Sum3 sd = load_sum3<WRAP>(nrow, L.w[j], L.wl[j], L.wr[j], W);
-                    const uint32_t cd = nrow[L.w[j]];
-                    uint32_t nx = rule_from_total<CONWAY>(total9(st[j].su, st[j].sc, sd), st[j].c, birth, survive);
-                    if (dead_row) nx = 0u;
-                    dst[r * W + L.w[j]] = nx;
-                    st[j].su = st[j].sc;
-                    st[j].sc = sd;
-                    st[j].c = cd;
-                }
-            }
+        if (ra < rb) {
+            if (L.cols == 2) life_strip<CONWAY, WRAP, WT, 2>(L, cur, oth, W, ra, rb, gy_first, n1, birth, survive);
+            else if (L.cols == 1) life_strip<CONWAY, WRAP, WT, 1>(L, cur, oth, W, ra, rb, gy_first, n1, birth, survive);
         }
         __syncthreads();
         uint32_t* t = cur;
@@ -185,10 +224,10 @@ __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur,
     return cur;
 }
 
-template <bool CONWAY, bool WRAP>
+template <bool CONWAY, bool WRAP, int WT>
 __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifeParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
-    const int W = p.W, k = p.k;
+    const int W = WT > 0 ? WT : p.W, k = p.k;
     const int rows = p.TB + 2 * k;
     uint32_t* buf0 = lsm;
     uint32_t* buf1 = lsm + (size_t)rows * W;
@@ -209,7 +248,7 @@ __global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifePara
     }
     __syncthreads();
     const LifeLane lane = life_lane(W);
-    const uint32_t* fin = life_gens<CONWAY, WRAP>(lane, buf0, buf1, rows, W, k, y0 - k, p.n1, p.birth, p.survive);
+    const uint32_t* fin = life_gens<CONWAY, WRAP, WT>(lane, buf0, buf1, rows, W, k, y0 - k, p.n1, p.birth, p.survive);
     for (int i = threadIdx.x; i < p.TB * W; i += blockDim.x) {
         const int r = i / W, w = i - r * W;
         const int gy = y0 + r;
@@ -264,10 +303,10 @@ __device__ __forceinline__ bool take_tagged(const uint64_t* p, uint32_t tag, uin
     return true;
 }
 
-template <bool CONWAY, bool WRAP>
+template <bool CONWAY, bool WRAP, int WT>
 __global__ void __launch_bounds__(kLifeThreads) life_coop_kernel(const LifeCoopParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
-    const int W = p.W, k = p.k, G = gridDim.x, b = blockIdx.x;
+    const int W = WT > 0 ? WT : p.W, k = p.k, G = gridDim.x, b = blockIdx.x;
     const int y0 = (int)(((int64_t)b * p.n1) / G), y1 = (int)(((int64_t)(b + 1) * p.n1) / G);
     const int TB = y1 - y0, rows = TB + 2 * k;
     const int TBmax = (p.n1 + G - 1) / G;
@@ -318,7 +357,7 @@ __global__ void __launch_bounds__(kLifeThreads) life_coop_kernel(const LifeCoopP
                 for (int i = threadIdx.x; i < TB * W; i += blockDim.x) p.prev[(size_t)y0 * W + i] = cur[(size_t)k * W + i];
             }
         }
-        cur = life_gens<CONWAY, WRAP>(lane, cur, oth, rows, W, kk, y0 - k, p.n1, p.birth, p.survive);
+        cur = life_gens<CONWAY, WRAP, WT>(lane, cur, oth, rows, W, kk, y0 - k, p.n1, p.birth, p.survive);
         oth = (cur == lsm) ? lsm + (size_t)(TBmax + 2 * k) * W : lsm;
         gen += kk;
         if (final) {
@@ -334,21 +373,29 @@ __global__ void __launch_bounds__(kLifeThreads) life_coop_kernel(const LifeCoopP
     }
 }
 
+// Row width specialised at compile time (128 words = 4096 cells); other widths use the run-time path.
+constexpr int kLifeWT = 128;
+
 // launch one k-generation pass (both entry points use this)
+template <bool C, bool WR, int WT>
+static cudaError_t life_launch_t(const LifeParams& lp, int grid, size_t smem, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(life_block_kernel<C, WR, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    life_block_kernel<C, WR, WT><<<grid, kLifeThreads, smem, s>>>(lp);
+    return cudaGetLastError();
+}
+
+template <int WT>
+static cudaError_t life_launch_w(const LifeParams& lp, bool conway, int grid, size_t smem, cudaStream_t s) {
+    if (conway && lp.wrap) return life_launch_t<true, true, WT>(lp, grid, smem, s);
+    if (conway) return life_launch_t<true, false, WT>(lp, grid, smem, s);
+    if (lp.wrap) return life_launch_t<false, true, WT>(lp, grid, smem, s);
+    return life_launch_t<false, false, WT>(lp, grid, smem, s);
+}
+
 static cudaError_t life_launch(const LifeParams& lp, bool conway, int grid, size_t smem, cudaStream_t s) {
-#define STC_LIFE_LAUNCH(C, WR)                                                                       \
-    {                                                                                                \
-        cudaError_t e = cudaFuncSetAttribute(life_block_kernel<C, WR>,                                \
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        if (e != cudaSuccess) return e;                                                              \
-        life_block_kernel<C, WR><<<grid, kLifeThreads, smem, s>>>(lp);                               \
-        return cudaGetLastError();                                                                   \
-    }
-    if (conway && lp.wrap) STC_LIFE_LAUNCH(true, true)
-    if (conway) STC_LIFE_LAUNCH(true, false)
-    if (lp.wrap) STC_LIFE_LAUNCH(false, true)
-    STC_LIFE_LAUNCH(false, false)
-#undef STC_LIFE_LAUNCH
+    return lp.W == kLifeWT ? life_launch_w<kLifeWT>(lp, conway, grid, smem, s) : life_launch_w<0>(lp, conway, grid, smem, s);
 }
 
 // ------------------------------------------------------------------ pack / unpack
@@ -466,9 +513,9 @@ static bool life_coop_enabled() {
     return !(e && e[0] == '0');
 }
 
-template <bool C, bool WR>
+template <bool C, bool WR, int WT>
 static cudaError_t coop_fits_t(int grid, size_t smem, int num_sms, bool* fits) {
-    auto fn = life_coop_kernel<C, WR>;
+    auto fn = life_coop_kernel<C, WR, WT>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int nb = 0;
@@ -477,12 +524,28 @@ static cudaError_t coop_fits_t(int grid, size_t smem, int num_sms, bool* fits) {
     return e;
 }
 
-template <bool C, bool WR>
+template <bool C, bool WR, int WT>
 static cudaError_t coop_launch_t(const LifeCoopParams& cp, int grid, size_t smem, cudaStream_t s) {
     LifeCoopParams arg = cp;
     void* args[] = {&arg};
-    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR>, dim3(grid), dim3(kLifeThreads), args,
+    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR, WT>, dim3(grid), dim3(kLifeThreads), args,
                                        smem, s);
+}
+
+// (fits = true: occupancy query; false: launch) for the instantiation matching (conway, wrap, W)
+template <int WT>
+static cudaError_t coop_dispatch_w(bool query, bool conway, bool wrap, const LifeCoopParams& cp, int grid, size_t smem,
+                                   cudaStream_t s, int num_sms, bool* fits) {
+    if (conway && wrap) return query ? coop_fits_t<true, true, WT>(grid, smem, num_sms, fits) : coop_launch_t<true, true, WT>(cp, grid, smem, s);
+    if (conway) return query ? coop_fits_t<true, false, WT>(grid, smem, num_sms, fits) : coop_launch_t<true, false, WT>(cp, grid, smem, s);
+    if (wrap) return query ? coop_fits_t<false, true, WT>(grid, smem, num_sms, fits) : coop_launch_t<false, true, WT>(cp, grid, smem, s);
+    return query ? coop_fits_t<false, false, WT>(grid, smem, num_sms, fits) : coop_launch_t<false, false, WT>(cp, grid, smem, s);
+}
+
+static cudaError_t coop_dispatch(bool query, bool conway, bool wrap, const LifeCoopParams& cp, int grid, size_t smem,
+                                 cudaStream_t s, int num_sms, bool* fits) {
+    return cp.W == kLifeWT ? coop_dispatch_w<kLifeWT>(query, conway, wrap, cp, grid, smem, s, num_sms, fits)
+                           : coop_dispatch_w<0>(query, conway, wrap, cp, grid, smem, s, num_sms, fits);
 }
 
 // The persistent path: every generation in one cooperative launch.  Returns STC_OK with *done = nsteps
@@ -510,11 +573,9 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
 
     const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
     bool fits = false;
-    cudaError_t e;
-    if (conway && wrap) e = coop_fits_t<true, true>(G, smem, ctx->num_sms, &fits);
-    else if (conway) e = coop_fits_t<true, false>(G, smem, ctx->num_sms, &fits);
-    else if (wrap) e = coop_fits_t<false, true>(G, smem, ctx->num_sms, &fits);
-    else e = coop_fits_t<false, false>(G, smem, ctx->num_sms, &fits);
+    LifeCoopParams q{};
+    q.W = W;
+    cudaError_t e = coop_dispatch(true, conway, wrap, q, G, smem, stream, ctx->num_sms, &fits);
     if (e != cudaSuccess) return cuda_fail(e);
     if (!fits) return STC_OK;   // not enough co-resident CTAs: the caller uses the multi-launch kernel
 
@@ -544,10 +605,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
     cp.birth = op->birth_mask;
     cp.survive = op->survive_mask;
     void* prof = prof_begin(stream);
-    if (conway && wrap) e = coop_launch_t<true, true>(cp, G, smem, stream);
-    else if (conway) e = coop_launch_t<true, false>(cp, G, smem, stream);
-    else if (wrap) e = coop_launch_t<false, true>(cp, G, smem, stream);
-    else e = coop_launch_t<false, false>(cp, G, smem, stream);
+    e = coop_dispatch(false, conway, wrap, cp, G, smem, stream, ctx->num_sms, &fits);
     if (e != cudaSuccess) {
         prof_end(prof, stream, "life_coop", 0.0, 0.0);
         cudaFreeAsync(mem, stream);
