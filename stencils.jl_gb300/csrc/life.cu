@@ -88,8 +88,10 @@ struct LifeParams {
     uint32_t birth, survive;
 };
 
-// A thread's fixed share of a band: columns w and w + W/2 (two independent adder networks that
-// interleave; one column when W is odd) and strip s of `strips` row strips.  Computed once per kernel.
+// A thread's fixed share of a band: one column w (or two, w and w + W/2, for narrow rows) and strip s
+// of `strips` row strips.  One column per thread means fewer, longer strips, so the two rows each
+// strip reads before its first output are a smaller share of the work; the unrolled row walk gives
+// the thread its independent instructions.  Computed once per kernel.
 struct LifeLane {
     int cols;            // 0 (idle thread), 1 or 2
     int w[2], wl[2], wr[2];
@@ -100,7 +102,7 @@ struct LifeLane {
 
 __device__ __forceinline__ LifeLane life_lane(int W) {
     LifeLane L;
-    const int cols = (W % 2 == 0) ? 2 : 1;
+    const int cols = (W % 2 == 0 && W < 64) ? 2 : 1;
     const int Wc = W / cols;
     L.strips = max(1, (int)blockDim.x / Wc);
     L.inv_strips = 1.0f / (float)L.strips;
@@ -421,9 +423,21 @@ __global__ void life_pack_kernel(const PackParams p) {
         const T* row = base + p.org + (int64_t)y * p.sy;
         uint32_t mine = 0;
         const int nw = min(32, p.W - w0);
-        for (int i = 0; i < nw; ++i) {
-            const uint32_t b = __ballot_sync(0xffffffffu, row[(int64_t)(w0 + i) * 32 + lane] != (T)0);
-            if (lane == i) mine = b;
+        if (nw == 32) {
+            // all 32 loads issued before the first ballot, so the group costs one memory latency
+            bool nz[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) nz[i] = row[(int64_t)(w0 + i) * 32 + lane] != (T)0;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const uint32_t b = __ballot_sync(0xffffffffu, nz[i]);
+                if (lane == i) mine = b;
+            }
+        } else {
+            for (int i = 0; i < nw; ++i) {
+                const uint32_t b = __ballot_sync(0xffffffffu, row[(int64_t)(w0 + i) * 32 + lane] != (T)0);
+                if (lane == i) mine = b;
+            }
         }
         if (lane < nw) p.P[(size_t)y * p.W + w0 + lane] = mine;
     }
@@ -442,9 +456,17 @@ __global__ void life_unpack_kernel(const PackParams p) {
         T* row = base + p.org + (int64_t)y * p.sy;
         const int nw = min(32, p.W - w0);
         const uint32_t mine = lane < nw ? p.P[(size_t)y * p.W + w0 + lane] : 0u;
-        for (int i = 0; i < nw; ++i) {
-            const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-            row[(int64_t)(w0 + i) * 32 + lane] = (T)((word >> lane) & 1u);
+        if (nw == 32) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+                const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+                row[(int64_t)(w0 + i) * 32 + lane] = (T)((word >> lane) & 1u);
+            }
+        } else {
+            for (int i = 0; i < nw; ++i) {
+                const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
+                row[(int64_t)(w0 + i) * 32 + lane] = (T)((word >> lane) & 1u);
+            }
         }
     }
 }
@@ -506,7 +528,7 @@ void life_plan(int W, int n1, int64_t steps_left, int smem_cap, int num_sms, int
 static int life_coop_depth() {
     const char* e = getenv("STC_LIFE_K");
     const int v = e ? atoi(e) : 0;
-    return (v >= 1 && v <= 32) ? v : 8;
+    return (v >= 1 && v <= 32) ? v : 4;
 }
 static bool life_coop_enabled() {
     const char* e = getenv("STC_LIFE_COOP");
