@@ -26,7 +26,13 @@
 
 namespace stc {
 
-constexpr int kLifeThreads = 512;
+constexpr int kLifeMaxThreads = 1024;
+
+// CTA size of the Life kernels: 512 threads (STC_LIFE_THREADS = 1024 overrides, a tuning knob)
+static int life_threads() {
+    const char* e = getenv("STC_LIFE_THREADS");
+    return (e && atoi(e) == 1024) ? 1024 : 512;
+}
 
 __device__ __forceinline__ void full_add(uint32_t a, uint32_t b, uint32_t c, uint32_t& s, uint32_t& cy) {
     const uint32_t t = a ^ b;
@@ -51,19 +57,26 @@ __device__ __forceinline__ RowV row_v(uint32_t wl, uint32_t c, uint32_t wr) {
 }
 
 // next state of the middle row m from the neighbour count n = sum3(u) + sum2(m) + sum3(d), 0..8, held
-// as bit planes n0..n3
+// as bit planes n0..n3 (B3/S23 uses the 3x3 total instead)
 template <bool CONWAY>
 __device__ __forceinline__ uint32_t next_state(const RowV& u, const RowV& m, const RowV& d, uint32_t birth,
                                                uint32_t survive) {
-    uint32_t n0, k0, x1, k1;
-    full_add(u.a3, m.a2, d.a3, n0, k0);    // weight 1 and its carry (weight 2)
-    full_add(u.b3, m.b2, d.b3, x1, k1);    // weight 2 and its carry (weight 4)
-    const uint32_t n1 = x1 ^ k0;
-    const uint32_t n2 = k1 ^ (x1 & k0);
     if constexpr (CONWAY) {
-        // B3/S23: n == 3, or alive with n == 2, i.e. n1 set, n2 clear and (n0 or alive); n == 8 has n1 clear
-        return n1 & ~n2 & (n0 | m.c);
+        // B3/S23 from the 3x3 total t = n + centre (0..9): alive next iff t == 3, or t == 4 and alive.
+        // Only t's low three bits are formed: t in {3, 4} is exactly (t0^t2) & (t1^t2) (8 and 9 fail
+        // it), and t2 tells the two apart.
+        uint32_t t0, k0, x1, k1;
+        full_add(u.a3, m.a3, d.a3, t0, k0);
+        full_add(u.b3, m.b3, d.b3, x1, k1);
+        const uint32_t t1 = x1 ^ k0;
+        const uint32_t t2 = k1 ^ (x1 & k0);
+        return ((t0 ^ t2) & (t1 ^ t2)) & (~t2 | m.c);
     } else {
+        uint32_t n0, k0, x1, k1;
+        full_add(u.a3, m.a2, d.a3, n0, k0);    // weight 1 and its carry (weight 2)
+        full_add(u.b3, m.b2, d.b3, x1, k1);    // weight 2 and its carry (weight 4)
+        const uint32_t n1 = x1 ^ k0;
+        const uint32_t n2 = k1 ^ (x1 & k0);
         const uint32_t n3 = k1 & x1 & k0;
         uint32_t out = 0;
 #pragma unroll
@@ -227,7 +240,7 @@ __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur,
 }
 
 template <bool CONWAY, bool WRAP, int WT>
-__global__ void __launch_bounds__(kLifeThreads) life_block_kernel(const LifeParams p) {
+__global__ void __launch_bounds__(kLifeMaxThreads) life_block_kernel(const LifeParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
     const int W = WT > 0 ? WT : p.W, k = p.k;
     const int rows = p.TB + 2 * k;
@@ -306,7 +319,7 @@ __device__ __forceinline__ bool take_tagged(const uint64_t* p, uint32_t tag, uin
 }
 
 template <bool CONWAY, bool WRAP, int WT>
-__global__ void __launch_bounds__(kLifeThreads) life_coop_kernel(const LifeCoopParams p) {
+__global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCoopParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
     const int W = WT > 0 ? WT : p.W, k = p.k, G = gridDim.x, b = blockIdx.x;
     const int y0 = (int)(((int64_t)b * p.n1) / G), y1 = (int)(((int64_t)(b + 1) * p.n1) / G);
@@ -384,7 +397,7 @@ static cudaError_t life_launch_t(const LifeParams& lp, int grid, size_t smem, cu
     cudaError_t e = cudaFuncSetAttribute(life_block_kernel<C, WR, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    life_block_kernel<C, WR, WT><<<grid, kLifeThreads, smem, s>>>(lp);
+    life_block_kernel<C, WR, WT><<<grid, life_threads(), smem, s>>>(lp);
     return cudaGetLastError();
 }
 
@@ -541,7 +554,7 @@ static cudaError_t coop_fits_t(int grid, size_t smem, int num_sms, bool* fits) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kLifeThreads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, life_threads(), smem);
     *fits = e == cudaSuccess && (int64_t)nb * num_sms >= grid;
     return e;
 }
@@ -550,7 +563,7 @@ template <bool C, bool WR, int WT>
 static cudaError_t coop_launch_t(const LifeCoopParams& cp, int grid, size_t smem, cudaStream_t s) {
     LifeCoopParams arg = cp;
     void* args[] = {&arg};
-    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR, WT>, dim3(grid), dim3(kLifeThreads), args,
+    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR, WT>, dim3(grid), dim3(life_threads()), args,
                                        smem, s);
 }
 
