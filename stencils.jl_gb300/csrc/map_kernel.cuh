@@ -316,10 +316,9 @@ __device__ __forceinline__ int box_index(const MapParams& p, const TileOrigin& o
     return ((int)(z - o.z0 + p.rz) * p.bh + (int)(y - o.y0 + p.ry)) * p.bw + (int)(x - o.x0 + p.padl);
 }
 
-// Cooperative load (or patch) of the needed region, one warp per box row.  only_outside: patch just
-// the cells outside [0, n) (after a TMA copy); otherwise load every needed cell.
+// Cooperative load of the needed region, one warp per box row.
 template <class Tin>
-__device__ void load_region(const MapParams& p, const TileOrigin& o, Tin* box, bool only_outside) {
+__device__ void load_region(const MapParams& p, const TileOrigin& o, Tin* box) {
     const Region g = needed_region(p, o);
     const int wy = (int)(g.yb - g.ya), wz = (int)(g.zb - g.za);
     const int nrows = wy * wz;
@@ -330,16 +329,52 @@ __device__ void load_region(const MapParams& p, const TileOrigin& o, Tin* box, b
         Tin* brow = box + ((int)(z - o.z0 + p.rz) * p.bh + (int)(y - o.y0 + p.ry)) * p.bw + p.padl;
         const bool row_in = y >= 0 && y < p.n[1] && z >= 0 && z < p.n[2];
         if (p.halo || (row_in && g.xa >= 0 && g.xb <= p.n[0])) {
-            if (only_outside) continue;   // (fixups never run for Halo padding)
             // the whole row lies in memory: straight copy
             const Tin* srow = src + p.src_org + y * p.sst[1] + z * p.sst[2];
             for (int64_t x = g.xa + lane; x < g.xb; x += 32) brow[x - o.x0] = srow[x];
             continue;
         }
-        for (int64_t x = g.xa + lane; x < g.xb; x += 32) {
-            if (only_outside && row_in && x >= 0 && x < p.n[0]) continue;
-            brow[x - o.x0] = load_bounded<Tin>(p, x, y, z);
+        for (int64_t x = g.xa + lane; x < g.xb; x += 32) brow[x - o.x0] = load_bounded<Tin>(p, x, y, z);
+    }
+}
+
+// Patch of an edge tile after its TMA copy: only the needed cells outside [0, n) are written
+// (Conditional rules), so the work is proportional to the outside cells.  Whole rows whose y or z
+// lies outside: a warp per row.  Rows inside in y and z: only their x-halo cells beyond either end,
+// one cell per thread, so those loads are all in flight together.
+template <class Tin>
+__device__ void patch_outside(const MapParams& p, const TileOrigin& o, Tin* box) {
+    const Region g = needed_region(p, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int wy = (int)(g.yb - g.ya), wz = (int)(g.zb - g.za);
+    // rows with y inside, per plane: y in [yi0, yi1)
+    const int64_t yi0 = max(g.ya, (int64_t)0), yi1 = min(g.yb, p.n[1]);
+    const int nyi = (int)max((int64_t)0, yi1 - yi0);
+    const int ylo = (int)(yi0 - g.ya);               // rows below 0 (or every row when none is inside)
+    for (int zi = 0; zi < wz; ++zi) {
+        const int64_t z = g.za + zi;
+        const bool zin = z >= 0 && z < p.n[2];
+        const int nout = zin ? wy - nyi : wy;        // rows of this plane to load whole
+        for (int j = warp; j < nout; j += nwarps) {
+            const int64_t y = zin ? (j < ylo ? g.ya + j : yi1 + (j - ylo)) : g.ya + j;
+            Tin* brow = box + ((int)(z - o.z0 + p.rz) * p.bh + (int)(y - o.y0 + p.ry)) * p.bw + p.padl;
+            for (int64_t x = g.xa + lane; x < g.xb; x += 32) brow[x - o.x0] = load_bounded<Tin>(p, x, y, z);
         }
+    }
+    // x-halo cells of the rows inside in y and z: [xa, 0) on the left, [n0, xb) on the right
+    const int xl = (int)max((int64_t)0, min(g.xb, (int64_t)0) - g.xa);
+    const int xr = (int)max((int64_t)0, g.xb - max(g.xa, p.n[0]));
+    const int nx = xl + xr;
+    if (nx == 0 || nyi == 0) return;
+    const int64_t zi0 = max(g.za, (int64_t)0), zi1 = min(g.zb, p.n[2]);
+    const int nzi = (int)max((int64_t)0, zi1 - zi0);
+    const int items = nyi * nzi * nx;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int row = it / nx, c = it - row * nx;
+        const int ry = row % nyi, rz = row / nyi;
+        const int64_t y = yi0 + ry, z = zi0 + rz;
+        const int64_t x = c < xl ? g.xa + c : p.n[0] + (c - xl);
+        box[box_index(p, o, x, y, z)] = load_bounded<Tin>(p, x, y, z);
     }
 }
 
@@ -398,14 +433,18 @@ __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOr
 // thread owns XT columns (lane + 32 i) and VS consecutive outputs along the stream axis.  Input rows
 // r = 0 .. VS + 2R - 1 are visited once each, in increasing order; row r feeds the outputs
 // s = r - q for q = 0 .. D-1 (D = 2R+1, q = offset row + R).  Output s lives in accumulator slot
-// s mod D; the row loop is a run-time loop unrolled by D, so every slot index, offset and weight is a
-// compile-time constant.  Because rows ascend and the generated tables are sorted by (z, y, x), each
-// output folds its neighbours in table order; it is finished and stored right after its last row.
+// s mod D.  When the whole stream is small (rows x offsets) it is unrolled completely, so every
+// slot, bound and address offset is a compile-time constant; otherwise the row loop is a run-time
+// loop unrolled by D, which keeps slots, offsets and weights constant.  Because rows ascend and the
+// generated tables are sorted by (z, y, x), each output folds its neighbours in table order; it is
+// finished and stored right after its last row.
 template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
 __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrigin& o, const Tin* box) {
     constexpr int N = Sh::kN, R = Sh::kR, L = Sh::L;
     constexpr int D = 2 * R + 1;
     constexpr int RY = (N == 3) ? R : 0;    // in-plane y halo for 3D shapes
+    constexpr int NROW = VS + 2 * R;
+    constexpr bool FULL = NROW * L <= 600;
     constexpr auto T = Sh::table;
     static_assert(((N == 3) ? T.o[0].z : T.o[0].y) == -R, "tables start at the lowest stream offset");
     using A = typename Op::A;
@@ -416,66 +455,71 @@ __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrig
     for (int i = 0; i < XT; ++i)
 #pragma unroll
         for (int q = 0; q < D; ++q) { acc[i][q] = A(0); ctr[i][q] = Tin(0); }
-    // box coordinates of the thread's first stream row and its row within a plane
-    const int by0 = (N == 3) ? (warp + p.ry) : (warp * VS);   // 2D: box row of stream row 0; 3D: fixed row
-    const int bz0 = (N == 3) ? 0 : p.rz;
-    const int nrow = VS + 2 * R;
+    // box element (row r, in-plane row offset yy - RY, column lane + 32 i + xx - R) is
+    // bb[r * sr + yy * p.bw + xx + 32 i]
+    const int sr = (N == 3) ? p.bh * p.bw : p.bw;
+    const Tin* bb = box + ((N == 3) ? (warp + p.ry - RY) * p.bw : p.rz * p.bh * p.bw + warp * VS * p.bw) + lane + p.padl - R;
     // tile-local extents that hold real outputs (ragged last tiles)
     const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0);
     const int nvs = (N == 3) ? (int)min((int64_t)VS, p.n[2] - o.z0) : (int)min((int64_t)VS, p.n[1] - o.y0 - warp * VS);
     const bool row_ok = (N == 3) ? (o.y0 + warp < p.n[1]) : true;
-    Tout* dst = (Tout*)p.dst;
-    for (int r0 = 0; r0 < nrow; r0 += D) {
+    // output s of this thread is dbase[s * dstep + lane + 32 i]
+    Tout* dbase = (Tout*)p.dst + p.dst_org + o.x0 + lane +
+                  ((N == 3) ? (o.y0 + warp) * p.dstr[1] + o.z0 * p.dstr[2] : (o.y0 + warp * VS) * p.dstr[1]);
+    const int64_t dstep = (N == 3) ? p.dstr[2] : p.dstr[1];
+    auto row = [&](const int r, const int u) {
+        Tin v[XT][2 * RY + 1][D];
 #pragma unroll
-        for (int u = 0; u < D; ++u) {
-            const int r = r0 + u;
-            if (r >= nrow) break;
-            const int by = (N == 3) ? by0 : by0 + r;
-            const int bz = (N == 3) ? r : bz0;
-            Tin v[XT][2 * RY + 1][D];
+        for (int i = 0; i < XT; ++i)
 #pragma unroll
-            for (int i = 0; i < XT; ++i)
+            for (int yy = 0; yy < 2 * RY + 1; ++yy)
 #pragma unroll
-                for (int yy = 0; yy < 2 * RY + 1; ++yy)
+                for (int xx = 0; xx < D; ++xx) v[i][yy][xx] = bb[r * sr + yy * p.bw + xx + 32 * i];
 #pragma unroll
-                    for (int xx = 0; xx < D; ++xx)
-                        v[i][yy][xx] = box[(bz * p.bh + by + yy - RY) * p.bw + lane + 32 * i + p.padl + xx - R];
+        for (int q = 0; q < D; ++q) {
+            const int sidx = r - q;               // output fed by this row at offset row q - R
+            if (sidx < 0 || sidx >= VS) continue;
+            const int slot = ((u - q) % D + D) % D;   // == sidx mod D (r - u is a multiple of D)
+            if (Op::kZeroInit && q == 0) {
 #pragma unroll
-            for (int q = 0; q < D; ++q) {
-                const int sidx = r - q;               // output fed by this row at offset row q - R
-                if (sidx < 0 || sidx >= VS) continue;
-                const int slot = ((u - q) % D + D) % D;   // == sidx mod D (r0 is a multiple of D)
-                if (Op::kZeroInit && q == 0) {
+                for (int i = 0; i < XT; ++i) acc[i][slot] = Op::first(Tin(0), 0);
+            }
 #pragma unroll
-                    for (int i = 0; i < XT; ++i) acc[i][slot] = Op::first(Tin(0), 0);
+            for (int k = 0; k < L; ++k) {
+                const int ko = (N == 3) ? T.o[k].z : T.o[k].y;
+                if (ko != q - R) continue;
+                const int oy = (N == 3) ? T.o[k].y : 0;
+#pragma unroll
+                for (int i = 0; i < XT; ++i) {
+                    const Tin val = v[i][oy + RY][T.o[k].x + R];
+                    if (!Op::kZeroInit && k == 0) acc[i][slot] = Op::first(val, 0);
+                    else acc[i][slot] = Op::step(acc[i][slot], val, k, p);
                 }
+            }
+            if (Op::kNeedsCentre && q == R) {
 #pragma unroll
-                for (int k = 0; k < L; ++k) {
-                    const int ko = (N == 3) ? T.o[k].z : T.o[k].y;
-                    if (ko != q - R) continue;
-                    const int oy = (N == 3) ? T.o[k].y : 0;
+                for (int i = 0; i < XT; ++i) ctr[i][slot] = v[i][RY][R];
+            }
+            if (q == D - 1 && sidx < nvs && row_ok) {
+                // last row of output sidx: finish and store
+                Tout* drow = dbase + sidx * dstep;
 #pragma unroll
-                    for (int i = 0; i < XT; ++i) {
-                        const Tin val = v[i][oy + RY][T.o[k].x + R];
-                        if (!Op::kZeroInit && k == 0) acc[i][slot] = Op::first(val, 0);
-                        else acc[i][slot] = Op::step(acc[i][slot], val, k, p);
-                    }
+                for (int i = 0; i < XT; ++i) {
+                    if (lane + 32 * i < nvx) drow[32 * i] = Op::finish(acc[i][slot], ctr[i][slot], p);
                 }
-                if (Op::kNeedsCentre && q == R) {
+            }
+        }
+    };
+    if constexpr (FULL) {
 #pragma unroll
-                    for (int i = 0; i < XT; ++i) ctr[i][slot] = v[i][RY][R];
-                }
-                if (q == D - 1 && sidx < nvs && row_ok) {
-                    // last row of output sidx: finish and store
-                    const int64_t y = o.y0 + ((N == 3) ? warp : warp * VS + sidx);
-                    const int64_t z = o.z0 + ((N == 3) ? sidx : 0);
-                    Tout* drow = dst + p.dst_org + y * p.dstr[1] + z * p.dstr[2] + o.x0;
+        for (int r = 0; r < NROW; ++r) row(r, r % D);
+    } else {
+        for (int r0 = 0; r0 < NROW; r0 += D) {
 #pragma unroll
-                    for (int i = 0; i < XT; ++i) {
-                        const int lx = lane + 32 * i;
-                        if (lx < nvx) drow[lx] = Op::finish(acc[i][slot], ctr[i][slot], p);
-                    }
-                }
+            for (int u = 0; u < D; ++u) {
+                const int r = r0 + u;
+                if (r >= NROW) break;
+                row(r, u);
             }
         }
     }
@@ -496,7 +540,7 @@ __global__ void __launch_bounds__(kMapThreads) map_kernel(const __grid_constant_
         Tin* box = stage_box(0);
         for (int64_t t = blockIdx.x; t < p.ntiles; t += step) {
             const TileOrigin o = tile_origin(p, t);
-            load_region<Tin>(p, o, box, false);
+            load_region<Tin>(p, o, box);
             __syncthreads();
             compute(o, box);
             __syncthreads();
@@ -538,7 +582,7 @@ __global__ void __launch_bounds__(kMapThreads) map_kernel(const __grid_constant_
         const TileOrigin o = tile_origin(p, t);
         Tin* box = stage_box(s);
         if (p.fixup && !region_inside(p, needed_region(p, o))) {
-            load_region<Tin>(p, o, box, true);
+            patch_outside<Tin>(p, o, box);
             fence_proxy_async();
             __syncthreads();
         }

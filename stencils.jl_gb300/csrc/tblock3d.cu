@@ -66,9 +66,15 @@ template <> __device__ __forceinline__ __nv_bfloat16 tb_pad<__nv_bfloat16>(const
 }
 template <> __device__ __forceinline__ double tb_pad<double>(const TBParams& p) { return p.padf; }
 
+// i mod n for the coordinates a plane box can hold (within one period of the grid almost always)
 __device__ __forceinline__ int64_t tb_wrap(int64_t i, int64_t n) {
-    i %= n;
-    return i < 0 ? i + n : i;
+    if (i < 0) i += n;
+    else if (i >= n) i -= n;
+    if (i < 0 || i >= n) {
+        i %= n;
+        if (i < 0) i += n;
+    }
+    return i;
 }
 
 // value of logical cell (x, y, z) for the plane fix-up (Conditional rules: Wrap or Remove)
@@ -179,13 +185,23 @@ __global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant_
                 fence_proxy_async();   // generic writes before a later TMA refill of this slot
                 __syncthreads();
             } else if (p.fixup && edge_xy) {
+                // rows outside in y: every cell (a warp per row); rows inside: only the x cells beyond
+                // either end, one per thread so that their loads are in flight together
+                const int64_t gx0 = x0 - p.padl;
+                const int xl = (int)max((int64_t)0, min((int64_t)PX, -gx0));             // bx < xl: gx < 0
+                const int xr0 = (int)max((int64_t)xl, min((int64_t)PX, p.n[0] - gx0));   // bx >= xr0: gx >= n0
+                const int nxo = xl + (PX - xr0);
+                for (int it = threadIdx.x; it < PY * nxo; it += blockDim.x) {
+                    const int by = it / nxo, c = it - by * nxo;
+                    const int64_t gy = y0 - k + by;
+                    if (gy < 0 || gy >= p.n[1]) continue;
+                    const int bx = c < xl ? c : xr0 + (c - xl);
+                    P0[by * PX + bx] = tb_load<T>(p, gx0 + bx, gy, z);
+                }
                 for (int by = warp; by < PY; by += nwarps) {
                     const int64_t gy = y0 - k + by;
-                    const bool row_in = gy >= 0 && gy < p.n[1];
-                    for (int bx = lane; bx < PX; bx += 32) {
-                        const int64_t gx = x0 - p.padl + bx;
-                        if (!row_in || gx < 0 || gx >= p.n[0]) P0[by * PX + bx] = tb_load<T>(p, gx, gy, z);
-                    }
+                    if (gy >= 0 && gy < p.n[1]) continue;
+                    for (int bx = lane; bx < PX; bx += 32) P0[by * PX + bx] = tb_load<T>(p, gx0 + bx, gy, z);
                 }
                 fence_proxy_async();
                 __syncthreads();
