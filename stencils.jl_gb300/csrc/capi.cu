@@ -454,6 +454,75 @@ int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded, const 
     return rc;
 }
 
+}  // extern "C"
+
+namespace stc {
+// Wrap, Reflect or nonzero Remove on a Conditional 3D SwitchingStencilArray: the steps run on an
+// internal Halo-padded pair whose ring is refreshed (K2) before every step, so every tile's input box
+// arrives whole from TMA and no edge tile needs patching.  The ring holds exactly the values the
+// Conditional rules give (bounded_index / padval), so each step is bit-identical to the direct one.
+// Afterwards state n goes to the parent the reference leaves it in and state n-1 to the other.
+// Returns STC_OK with *done = 0 when it does not apply or scratch memory is not available.
+static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op,
+                        const stc_bc* bc, int64_t nsteps, int* src_is_b, cudaStream_t s, DeviceCtx* ctx,
+                        int64_t* done) {
+    *done = 0;
+    if (nsteps < 4 || a->ndims != 3 || bc->padding != STC_CONDITIONAL || bc->boundary == STC_USE) return STC_OK;
+    if (const char* e = getenv("STC_NO_PADDED")) if (e[0] == '1') return STC_OK;   // tuning / test override
+    const bool zero_pad = bc->boundary == STC_REMOVE &&
+                          (is_float_dtype(a->dtype) ? (bc->padval == 0.0 && !std::signbit(bc->padval)) : bc->padval_int == 0);
+    if (zero_pad) return STC_OK;   // TMA's zero fill already gives Remove(0) without patching
+    const int R = st->radius;
+    const int es = dtype_size(a->dtype);
+    int64_t P[3], n[3];
+    for (int d = 0; d < 3; ++d) {
+        n[d] = a->size[d];
+        P[d] = n[d] + 2 * R;
+    }
+    const int64_t pitch = (P[0] * es + 15) / 16 * 16 / es;   // row pitch a multiple of 16 bytes (TMA)
+    const size_t cells = (size_t)pitch * P[1] * P[2];
+    void* mem = nullptr;
+    if (cudaMallocAsync(&mem, 2 * cells * es, s) != cudaSuccess) {
+        cudaGetLastError();
+        return STC_OK;
+    }
+    stc_grid pg[2];
+    for (int i = 0; i < 2; ++i) {
+        pg[i].ndims = 3;
+        pg[i].dtype = a->dtype;
+        for (int d = 0; d < 3; ++d) pg[i].size[d] = P[d];
+        pg[i].stride[0] = 1;
+        pg[i].stride[1] = pitch;
+        pg[i].stride[2] = pitch * P[1];
+        pg[i].data = (char*)mem + i * cells * es;
+    }
+    stc_bc hb = *bc;
+    hb.padding = STC_HALO_OUT;
+    const int64_t inner = R + R * pitch + R * pitch * P[1];   // parent offset of logical (0, 0, 0)
+    // Remove(padval): the rings hold padval for good, filled once; Wrap / Reflect: refreshed every step
+    int rc = launch_grid_copy(a, 0, &pg[0], inner, n, s);
+    const bool fixed_ring = bc->boundary == STC_REMOVE;
+    if (!rc && fixed_ring) rc = launch_halo_fill(&pg[0], R, &hb, s);
+    if (!rc && fixed_ring) rc = launch_halo_fill(&pg[1], R, &hb, s);
+    int cur = 0;
+    for (int64_t k = 0; k < nsteps && !rc; ++k) {
+        if (!fixed_ring && (rc = launch_halo_fill(&pg[cur], R, &hb, s))) break;
+        if ((rc = launch_map(&pg[cur], &pg[1 - cur], 1, st, op, &hb, s, ctx))) break;
+        cur = 1 - cur;
+    }
+    const bool res_in_b = (nsteps & 1) != 0;
+    if (!rc) rc = launch_grid_copy(&pg[cur], inner, res_in_b ? b : a, 0, n, s);
+    if (!rc) rc = launch_grid_copy(&pg[1 - cur], inner, res_in_b ? a : b, 0, n, s);
+    cudaFreeAsync(mem, s);
+    if (rc) return rc;
+    *src_is_b = res_in_b ? 1 : 0;
+    *done = nsteps;
+    return STC_OK;
+}
+}  // namespace stc
+
+extern "C" {
+
 int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
                   int64_t nsteps, int32_t* out_src_is_b, void* stream, uint32_t flags) {
     if (nsteps < 0) return STC_ERR_INVALID;
@@ -470,6 +539,11 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
     // Cellular automata on bit-packable grids run temporally blocked on a packed copy.
     rc = life_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
     if (rc) return rc;
+    // 3D grids whose boundary needs edge patching: steps on an internal Halo-padded pair
+    if (done == 0) {
+        rc = padded_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
+        if (rc) return rc;
+    }
     // 3D radius-1 float maps: k steps per pass over HBM; the last step runs below
     if (done == 0) {
         rc = tb3d_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);

@@ -60,4 +60,8 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
 // halo fill (update_boundary!) of a Halo-padded parent
 int launch_halo_fill(const stc_grid* parent, int radius, const stc_bc* bc, cudaStream_t stream);
 
+// copy an n[0] x n[1] x n[2] box from src (element offset sorg) to dst (offset dorg), same dtype
+int launch_grid_copy(const stc_grid* src, int64_t sorg, const stc_grid* dst, int64_t dorg, const int64_t n[3],
+                     cudaStream_t stream);
+
 }  // namespace stc

@@ -5,6 +5,8 @@
 // a cell gets padval (Remove) or the interior value at bounded_index of its coordinates
 // (Wrap / Reflect, src/array.jl:154-179).  Every halo cell depends only on interior cells, so the
 // slabs are written in one launch; cells shared by two slabs receive the same value from both.
+#include <algorithm>
+
 #include "common.cuh"
 #include "dispatch.h"
 #include "profile.h"
@@ -40,38 +42,62 @@ template <> __device__ __forceinline__ int32_t halo_pad<int32_t>(const HaloParam
 }
 template <> __device__ __forceinline__ int64_t halo_pad<int64_t>(const HaloParams& p) { return p.padi; }
 
+// Every ring cell exactly once, in three parts (e = ring width on an axis, 0 beyond ndims):
+//   A  the z-ring planes, whole (rows y in [-e1, n1+e1), x along the threads);
+//   B  the y-ring rows of the interior planes (x along the threads);
+//   C  the x-ring cells of the interior rows (one cell per thread).
+// A ring cell holds padval (Remove) or the interior cell at bounded_index of its coordinates on every
+// axis (Wrap / Reflect).  Rows are indexed in 32-bit (axes < 2^31), so no per-cell 64-bit division.
+template <class T>
+__device__ __forceinline__ T halo_value(const HaloParams& p, const T* base, int64_t x, int64_t y, int64_t z) {
+    if (p.boundary == STC_REMOVE) return halo_pad<T>(p);
+    const int64_t bx = hb(p.boundary, x, p.n[0]);
+    const int64_t by = p.ndims > 1 ? hb(p.boundary, y, p.n[1]) : 0;
+    const int64_t bz = p.ndims > 2 ? hb(p.boundary, z, p.n[2]) : 0;
+    return base[(bx + p.R) + (p.ndims > 1 ? (by + p.R) * p.st[1] : 0) + (p.ndims > 2 ? (bz + p.R) * p.st[2] : 0)];
+}
+
 template <class T>
 __global__ void halo_fill_kernel(const HaloParams p) {
     T* base = (T*)p.base;
-    const int64_t R = p.R;
-    for (int64_t lin = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; lin < p.total;
-         lin += (int64_t)gridDim.x * blockDim.x) {
-        // locate the slab
-        int slab = 0;
-        int64_t r = lin;
-        while (slab < 2 * p.ndims - 1 && r >= p.slab_cells[slab]) r -= p.slab_cells[slab++];
-        const int ax = slab >> 1, side = slab & 1;
-        int64_t ext[3], J[3];
-        for (int d = 0; d < 3; ++d) ext[d] = d < p.ndims ? (d == ax ? R : p.n[d] + 2 * R) : 1;
-        J[0] = r % ext[0];
-        J[1] = (r / ext[0]) % ext[1];
-        J[2] = r / (ext[0] * ext[1]);
-        // to logical coordinates
-        for (int d = 0; d < p.ndims; ++d) {
-            if (d == ax) J[d] = side == 0 ? J[d] - R : p.n[d] + J[d];
-            else J[d] -= R;
-        }
-        const int64_t dsto = (J[0] + R) + (p.ndims > 1 ? (J[1] + R) * p.st[1] : 0) +
-                             (p.ndims > 2 ? (J[2] + R) * p.st[2] : 0);
-        T v;
-        if (p.boundary == STC_REMOVE) {
-            v = halo_pad<T>(p);
+    const int e0 = p.R, e1 = p.ndims > 1 ? p.R : 0, e2 = p.ndims > 2 ? p.R : 0;
+    const int n0 = (int)p.n[0], n1 = (int)p.n[1], n2 = (int)p.n[2];
+    const int wx = n0 + 2 * e0, wy = n1 + 2 * e1;
+    const int rowsA = 2 * e2 * wy, rowsB = n2 * 2 * e1;
+    const int64_t cellsC = (int64_t)n1 * n2 * 2 * e0;
+    auto put = [&](int64_t x, int64_t y, int64_t z) {
+        base[(x + p.R) + (y + e1) * p.st[1] + (z + e2) * p.st[2]] = halo_value<T>(p, base, x, y, z);
+    };
+    // parts A and B: a block per row, threads along x
+    for (int r = blockIdx.x; r < rowsA + rowsB; r += gridDim.x) {
+        int64_t y, z;
+        if (r < rowsA) {
+            const int zi = r / wy;
+            y = r - zi * wy - e1;
+            z = zi < e2 ? zi - e2 : n2 + (zi - e2);
         } else {
-            int64_t B[3] = {0, 0, 0};
-            for (int d = 0; d < p.ndims; ++d) B[d] = hb(p.boundary, J[d], p.n[d]);
-            v = base[(B[0] + R) + (p.ndims > 1 ? (B[1] + R) * p.st[1] : 0) + (p.ndims > 2 ? (B[2] + R) * p.st[2] : 0)];
+            const int q = r - rowsA;
+            const int zi = q / (2 * e1), yi = q - zi * 2 * e1;
+            z = zi;
+            y = yi < e1 ? yi - e1 : n1 + (yi - e1);
         }
-        base[dsto] = v;
+        for (int xi = threadIdx.x; xi < wx; xi += blockDim.x) put(xi - e0, y, z);
+    }
+    // part C: one x-ring cell per thread (32-bit indices while they fit)
+    if (cellsC < (1ll << 31)) {
+        const int cc = (int)cellsC, w = 2 * e0;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < cc; c += gridDim.x * blockDim.x) {
+            const int row = c / w, j = c - row * w;
+            const int z = row / n1, y = row - z * n1;
+            put(j < e0 ? j - e0 : n0 + (j - e0), y, z);
+        }
+        return;
+    }
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < cellsC; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = c / (2 * e0);
+        const int j = (int)(c - row * 2 * e0);
+        const int64_t y = row % n1, z = row / n1;
+        put(j < e0 ? j - e0 : n0 + (j - e0), y, z);
     }
 }
 
@@ -101,6 +127,8 @@ int launch_halo_fill(const stc_grid* g, int radius, const stc_bc* bc, cudaStream
         p.slab_cells[s] = c;
         p.total += c;
     }
+    for (int d = 0; d < 3; ++d)
+        if (p.n[d] + 2 * radius >= (1ll << 31)) return STC_ERR_UNSUPPORTED;
     const int threads = 256;
     int64_t blocks = (p.total + threads - 1) / threads;
     if (blocks > (int64_t)ctx->num_sms * 8) blocks = (int64_t)ctx->num_sms * 8;
@@ -117,6 +145,58 @@ int launch_halo_fill(const stc_grid* g, int radius, const stc_bc* bc, cudaStream
     default: return STC_ERR_UNSUPPORTED;
     }
     prof_end(prof, stream, "halo_fill", (double)p.total * 2 * dtype_size(g->dtype), (double)p.total);
+    return cuda_fail(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------ box copy between parents
+// dst[dorg + x + y*ds1 + z*ds2] = src[sorg + x + y*ss1 + z*ss2] over an n0 x n1 x n2 box: a block per
+// row (y, z), threads along x, so no per-element division.
+struct CopyParams {
+    const void* src;
+    void* dst;
+    int64_t sorg, ss1, ss2, dorg, ds1, ds2;
+    int64_t n0, n1, rows;
+};
+
+template <class T>
+__global__ void grid_copy_kernel(const CopyParams p) {
+    const T* src = (const T*)p.src;
+    T* dst = (T*)p.dst;
+    for (int64_t row = blockIdx.x; row < p.rows; row += gridDim.x) {
+        const int64_t y = row % p.n1, z = row / p.n1;
+        const T* s = src + p.sorg + y * p.ss1 + z * p.ss2;
+        T* d = dst + p.dorg + y * p.ds1 + z * p.ds2;
+        for (int64_t x = threadIdx.x; x < p.n0; x += blockDim.x) d[x] = s[x];
+    }
+}
+
+int launch_grid_copy(const stc_grid* src, int64_t sorg, const stc_grid* dst, int64_t dorg, const int64_t n[3],
+                     cudaStream_t stream) {
+    DeviceCtx* ctx = nullptr;
+    int rc = device_ctx(&ctx);
+    if (rc) return rc;
+    CopyParams p{};
+    p.src = src->data;
+    p.dst = dst->data;
+    p.sorg = sorg;
+    p.dorg = dorg;
+    p.ss1 = src->ndims > 1 ? src->stride[1] : 0;
+    p.ss2 = src->ndims > 2 ? src->stride[2] : 0;
+    p.ds1 = dst->ndims > 1 ? dst->stride[1] : 0;
+    p.ds2 = dst->ndims > 2 ? dst->stride[2] : 0;
+    p.n0 = n[0];
+    p.n1 = n[1];
+    p.rows = n[1] * n[2];
+    if (p.n0 < 1 || p.rows < 1) return STC_OK;
+    const int threads = p.n0 >= 256 ? 256 : 128;
+    const int blocks = (int)std::min<int64_t>(p.rows, (int64_t)ctx->num_sms * 16);
+    switch (dtype_size(src->dtype)) {
+    case 8: grid_copy_kernel<uint64_t><<<blocks, threads, 0, stream>>>(p); break;
+    case 4: grid_copy_kernel<uint32_t><<<blocks, threads, 0, stream>>>(p); break;
+    case 2: grid_copy_kernel<uint16_t><<<blocks, threads, 0, stream>>>(p); break;
+    case 1: grid_copy_kernel<uint8_t><<<blocks, threads, 0, stream>>>(p); break;
+    default: return STC_ERR_UNSUPPORTED;
+    }
     return cuda_fail(cudaGetLastError());
 }
 

@@ -14,6 +14,7 @@
 // update is the single-map fold (same op structs), so results are bit-identical to k separate maps.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -300,6 +301,10 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
                    int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx, int64_t* done) {
     *done = 0;
     if (nsteps < 3 || a->ndims != 3 || st->ndims != 3 || st->radius != 1) return STC_OK;
+    // Opt-in (STC_TBLOCK=1): at its present instruction count per cell update the blocked kernel is
+    // slower on GB300 than one K1 pass per step, which runs near the HBM roofline.
+    const char* e = getenv("STC_TBLOCK");
+    if (!(e && e[0] == '1')) return STC_OK;
     if (!(bc->boundary == STC_WRAP || bc->boundary == STC_REMOVE)) return STC_OK;
     int opv = op->code == STC_OP_DIFFUSE ? OPV_DIFFUSE : op->code == STC_OP_MEAN ? OPV_MEAN
               : op->code == STC_OP_SUM ? OPV_SUM : -1;
