@@ -322,6 +322,15 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
         cells *= p.n[d];
     }
     if (cells == 0) return STC_OK;
+    // A Halo parent whose base is not 16-byte aligned (its ring starts just before an aligned interior)
+    // gets its tensor map from the 16-byte boundary below the base: the extra leading columns are memory
+    // of the same allocation and only ever land in the box's unused left padding.  (Not for Conditional
+    // grids, whose x < 0 cells must read as TMA's zero fill.)
+    const int es_src = dtype_size(src->dtype);
+    int tma_shift = 0;
+    if (halo && ((uintptr_t)src->data % 16) != 0 && ((uintptr_t)src->data % es_src) == 0)
+        tma_shift = (int)(((uintptr_t)src->data % 16) / es_src);
+    p.hx[0] += tma_shift;   // from here on hx[0] is the tensor-map coordinate of logical x = 0
     // Remove's padval in the source element type
     p.padi = bc->padval_int;
     p.padf = bc->padval;
@@ -369,7 +378,8 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     p.stage_bytes = (uint32_t)align_up(p.box_bytes, 128);
     const int64_t smem_cap = (int64_t)ctx->max_smem_optin - 1024 - 8 * kMaxStages;
 
-    bool tma = nd >= 2 && encoder() != nullptr && ((uintptr_t)src->data % 16 == 0) && p.bw <= 256 &&
+    char* tma_base = (char*)src->data - (size_t)tma_shift * es;
+    bool tma = nd >= 2 && encoder() != nullptr && ((uintptr_t)tma_base % 16 == 0) && p.bw <= 256 &&
                p.bh <= 256 && p.bd <= 256 && 2 * (int64_t)p.stage_bytes <= smem_cap;
     for (int d = 1; d < nd; ++d)
         if ((src->stride[d] * es) % 16 != 0) tma = false;
@@ -378,9 +388,9 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
         while ((int64_t)p.stages * p.stage_bytes > smem_cap) --p.stages;
         cuuint64_t gdim[3], gstr[2];
         cuuint32_t box[3] = {(cuuint32_t)p.bw, (cuuint32_t)p.bh, (cuuint32_t)p.bd}, est[3] = {1, 1, 1};
-        for (int d = 0; d < nd; ++d) gdim[d] = (cuuint64_t)src->size[d];
+        for (int d = 0; d < nd; ++d) gdim[d] = (cuuint64_t)src->size[d] + (d == 0 ? tma_shift : 0);
         for (int d = 1; d < nd; ++d) gstr[d - 1] = (cuuint64_t)(src->stride[d] * es);
-        CUresult r = encoder()(&p.tmap, tma_dtype(src->dtype), (cuuint32_t)nd, src->data, gdim, gstr, box, est,
+        CUresult r = encoder()(&p.tmap, tma_dtype(src->dtype), (cuuint32_t)nd, tma_base, gdim, gstr, box, est,
                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) tma = false;
@@ -479,7 +489,12 @@ static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil*
         n[d] = a->size[d];
         P[d] = n[d] + 2 * R;
     }
-    const int64_t pitch = (P[0] * es + 15) / 16 * 16 / es;   // row pitch a multiple of 16 bytes (TMA)
+    // Rows: `lead` unused cells, the R ring cells, the interior, the R ring cells, padding; lead + R is a
+    // multiple of 128 bytes and so is the pitch, so every interior row starts on a 128-byte line (the
+    // map's row stores stay whole lines).
+    const int64_t line = 128 / es;
+    const int64_t lead = (R + line - 1) / line * line - R;
+    const int64_t pitch = (lead + P[0] + line - 1) / line * line;
     const size_t cells = (size_t)pitch * P[1] * P[2];
     void* mem = nullptr;
     if (cudaMallocAsync(&mem, 2 * cells * es, s) != cudaSuccess) {
@@ -494,7 +509,7 @@ static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil*
         pg[i].stride[0] = 1;
         pg[i].stride[1] = pitch;
         pg[i].stride[2] = pitch * P[1];
-        pg[i].data = (char*)mem + i * cells * es;
+        pg[i].data = (char*)mem + (i * cells + lead) * es;
     }
     stc_bc hb = *bc;
     hb.padding = STC_HALO_OUT;
