@@ -17,6 +17,8 @@
 //    all outputs of the thread that need it, while keeping each output's fold order.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace stc {
@@ -88,6 +90,37 @@ template <class P> __device__ __forceinline__ double div_by_len(double a, const 
     return __ddiv_rn(a, p.Ld);
 }
 
+// Correctly rounded a / LC for a compile-time 2 <= LC <= 512, in integer arithmetic (schoolbook
+// binary division with guard and sticky bits, IEEE 754 round to nearest even): the 53-bit significand
+// shifted left by 11 is divided by the constant (a multiply-high, no division instruction), the quotient
+// keeps at least 55 bits, its low bits and the remainder give the round and sticky bits.  Zero,
+// subnormal, infinite and NaN inputs and subnormal results use the IEEE division.  On GB300 this costs a
+// few dozen integer instructions instead of the FP64 instructions of a division.
+template <int LC>
+__device__ __forceinline__ double div_exact_const(double a) {
+    static_assert(LC >= 2 && LC <= 512, "constant divisor range");
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
+    if (ex == 0u || ex == 0x7ffu) return __ddiv_rn(a, (double)LC);
+    const unsigned long long N = ((b & 0xfffffffffffffull) | (1ull << 52)) << 11;
+    const unsigned long long Q = N / (unsigned long long)LC;
+    const unsigned long long rem = N - Q * (unsigned long long)LC;
+    const int t = 11 - __clzll((long long)Q);          // bits of Q beyond 53 (>= 2)
+    unsigned long long mant = Q >> t;
+    const unsigned long long low = Q & ((1ull << t) - 1ull);
+    const bool rnd = ((low >> (t - 1)) & 1ull) != 0ull;
+    const bool sticky = (low & ((1ull << (t - 1)) - 1ull)) != 0ull || rem != 0ull;
+    int E = (int)ex - 1023 + t - 11;                    // exponent of mant / 2^52
+    if (rnd && (sticky || (mant & 1ull))) mant += 1ull;
+    if (mant == (1ull << 53)) {
+        mant >>= 1;
+        E += 1;
+    }
+    if (E + 1023 <= 0) return __ddiv_rn(a, (double)LC);
+    return __longlong_as_double(
+        (long long)((b & (1ull << 63)) | ((unsigned long long)(E + 1023) << 52) | (mant - (1ull << 52))));
+}
+
 template <class Tin, class Tout, class Acc> struct OpMean {
     static constexpr bool kZeroInit = false, kNeedsCentre = false;
     using A = Acc;
@@ -96,6 +129,11 @@ template <class Tin, class Tout, class Acc> struct OpMean {
     template <class P> __device__ static Tout finish(A a, Tin, const P& p) {
         if constexpr (sizeof(A) == 8) return from_f64<Tout>(div_by_len(a, p));
         else return from_f32<Tout>(div_by_len(a, p));
+    }
+    // finish with the stencil length known at compile time (shape-specialised kernels)
+    template <int LC, class P> __device__ static Tout finish_c(A a, Tin c, const P& p) {
+        if constexpr (sizeof(A) == 8 && LC >= 2 && LC <= 512) return from_f64<Tout>(div_exact_const<LC>(a));
+        else return finish(a, c, p);
     }
     __device__ static A conv(Tin v) {
         if constexpr (sizeof(A) == 8) return cvt_d(v); else return cvt_f(v);
@@ -505,7 +543,12 @@ __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrig
                 Tout* drow = dbase + sidx * dstep;
 #pragma unroll
                 for (int i = 0; i < XT; ++i) {
-                    if (lane + 32 * i < nvx) drow[32 * i] = Op::finish(acc[i][slot], ctr[i][slot], p);
+                    if (lane + 32 * i < nvx) {
+                        if constexpr (std::is_same_v<Op, OpMean<Tin, Tout, A>>)
+                            drow[32 * i] = Op::template finish_c<L>(acc[i][slot], ctr[i][slot], p);
+                        else
+                            drow[32 * i] = Op::finish(acc[i][slot], ctr[i][slot], p);
+                    }
                 }
             }
         }

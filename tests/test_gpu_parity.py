@@ -212,6 +212,28 @@ def test_mean_blur_1000x1000_bit_exact(gpu, ora, st):
     assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
 
 
+def test_mean_division_all_binades(gpu, ora, st):
+    """Float64 mean of Window(1) (the specialised kernel divides by 9 in integer arithmetic) over values
+    spread across every binade, both signs, zeros and subnormals, so that sums land on tiny, huge and
+    subnormal quotients (those fall back to the IEEE division): bit-exact against the oracle's
+    division, for Window(1) (L = 9) and Window(2) as a table (L = 25, run-time IEEE division)."""
+    rng = np.random.default_rng(23)
+    shape = (257, 131)
+    e = rng.integers(-1074, 1000, size=shape).astype(np.float64)
+    a = rng.random(shape) * np.exp2(e) * np.where(rng.random(shape) < 0.5, -1.0, 1.0)
+    a[rng.random(shape) < 0.02] = 0.0
+    a[rng.random(shape) < 0.02] = 5e-324
+    # runs of similar magnitudes, so whole 3x3 blocks share a scale
+    blk = np.exp2(rng.integers(-1070, 1000, size=(shape[0] // 8 + 1, shape[1] // 8 + 1)).astype(np.float64))
+    a[: shape[0] // 2] = rng.random((shape[0] // 2, shape[1])) * np.kron(blk, np.ones((8, 8)))[: shape[0] // 2, : shape[1]]
+    a = np.asfortranarray(a)
+    for bnd in (st.Remove(0.0), st.Wrap()):
+        for stencil in (st.Window(1), st.Positional(*st.Window(2).offsets())):
+            got = gpu.map(a, stencil, st.mean, bnd, st.Conditional())
+            want = ora.map(a, stencil, st.mean, bnd, st.Conditional())
+            assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), (bnd, stencil)
+
+
 @pytest.mark.parametrize("pad", ["cond", "halo_out"])
 @pytest.mark.parametrize("what", ["life", "mean", "diffuse"])
 def test_switching_steps_match_oracle(gpu, ora, st, abi, what, pad):
