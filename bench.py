@@ -356,7 +356,8 @@ def _kernel_roofline(prof, peak_gbs):
     k = dom[1]
     ach = k["alg_bytes"] / (k["ms"] / 1e3) / 1e9
     return {"kernel": dom[0], "achieved_gbs": ach, "frac_of_measured_hbm": ach / peak_gbs,
-            "avg_launch_us": 1e3 * k["ms"] / k["launches"], "gcell_s": k["updates"] / (k["ms"] / 1e3) / 1e9}
+            "avg_launch_us": 1e3 * k["ms"] / k["launches"], "gcell_s": k["updates"] / (k["ms"] / 1e3) / 1e9,
+            "all_kernels_ms": {name: {"launches": v["launches"], "ms": round(v["ms"], 4)} for name, v in prof.items()}}
 
 
 def _peaks():
