@@ -458,7 +458,8 @@ def run_diffusion(args):
     A = __import__("stencils_gb300._abi", fromlist=["x"])
     rng = np.random.Generator(np.random.PCG64(4))
     steps = 200
-    a = np.asfortranarray(rng.random((512, 512, 512), dtype=np.float32))
+    side = args.side or 512
+    a = np.asfortranarray(rng.random((side, side, side), dtype=np.float32))
     small = np.asfortranarray(rng.random((96, 96, 96), dtype=np.float32))
     pa, pb = np.asfortranarray(small.astype(np.float64)), np.asfortranarray(small.astype(np.float64))
     in_b = orc.map_steps(pa, pb, A.F64, st.VonNeumann(1, 3), st.Diffusion(0.1), st.Wrap(), st.Conditional(), steps,
@@ -493,7 +494,7 @@ def run_diffusion(args):
         res[name] = {"gcell_s": a.size * steps / t / 1e9, "s_total": t, "mass_drift_rel": (m1 - m0) / m0,
                      "max_rel_err_vs_fp64_96cube": rel, "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"])}
         del S, Ss
-    line = {"workload": "7-point diffusion VonNeumann(1,3) 512^3, Wrap, 200 steps", "metric": METRIC, "unit": UNIT,
+    line = {"workload": f"7-point diffusion VonNeumann(1,3) {side}^3, Wrap, 200 steps", "metric": METRIC, "unit": UNIT,
             "value": res["f32"]["gcell_s"], "results": res}
     print(json.dumps(line), flush=True)
 
@@ -647,6 +648,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="life", choices=["life"] + sorted(WORKLOADS),
                     help="life (the headline line) or one of the other BASELINE configurations")
+    ap.add_argument("--side", type=int, default=0, help="diffusion: grid side (default 512)")
     ap.add_argument("--serve-jobs", type=int, default=120)
     ap.add_argument("--serve-rates", default="100,300,1000,3000,5000")
     ap.add_argument("--serve-tick", type=int, default=16)

@@ -25,6 +25,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "batch.h"
@@ -174,6 +175,97 @@ __device__ void batch_item(const BatchJob& j, const BatchItem& it, unsigned char
     }
 }
 
+// ---------------------------------------------------------------------------- vector-column tiles
+// Fields compute_shape_vec reads, for one tile of one job (weights held in registers: NW = L for
+// kernelproduct shapes).
+template <int NW> struct BatchTileP {
+    int32_t bw, bh, ry, rz, padl, tw, ring;
+    int64_t n[3];
+    void* dst;
+    int64_t dst_org;
+    int64_t dstr[3];
+    int32_t L;
+    uint32_t birth, survive;
+    double alpha;
+    float rcp_f;
+    int32_t fastdiv_f;
+    float Lf;
+    double Ld;
+    float alpha_f;
+    float wf[NW];
+    const double* w;
+};
+
+// Geometry of the vector-column tiles of the batched kernel (shared with the host planner).
+template <class T> struct BatchVecGeom {
+    static constexpr int XV = 4, VS = 8;
+    static constexpr int TW = 32 * XV, TH = (kBatchThreads / 32) * VS;
+};
+template <class T, int R> struct BatchVecBox {
+    using G = BatchVecGeom<T>;
+    static constexpr int PA = (R + G::XV - 1) / G::XV * G::XV;
+    static constexpr int V = 16 / (int)sizeof(T);
+    static constexpr int BW = (2 * PA + G::TW + V - 1) / V * V;
+    static constexpr int BH = G::TH + 2 * R;
+};
+
+// One step of one tile: the tile's box (tile + R, Conditional rules of the job's boundary) is read
+// through L2 into shared memory, then reduced by the single-map kernel's vector-column code straight
+// into the destination parent, so each cell's fold is the one stc_map_steps performs.
+template <class T, class Op, class Sh>
+__device__ void batch_tile_vec(const BatchJob& j, const BatchItem& it, unsigned char* smem, const float* sw,
+                               const OpArgs& oa) {
+    using G = BatchVecGeom<T>;
+    constexpr int R = Sh::kR;
+    using B = BatchVecBox<T, R>;
+    constexpr int BW = B::BW, BH = B::BH, PA = B::PA;
+    const int x0 = (it.tile % j.ntx) * G::TW, y0 = (it.tile / j.ntx) * G::TH;
+    const int src = it.round & 1, dstb = (it.round + 1) & 1;
+    const T* sp = (const T*)j.buf[src] + j.org[src];
+    const T pv = pad_of<T>(j);
+    T* box = (T*)smem;
+    const bool wr = j.boundary == STC_WRAP;
+    constexpr int TOTAL = BW * BH;
+    constexpr int UNR = 8;
+    for (int i0 = 0; i0 < TOTAL; i0 += kBatchThreads * UNR) {
+        T v[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int i = i0 + u * kBatchThreads + threadIdx.x;
+            v[u] = pv;
+            if (i < TOTAL) {
+                const int by = i / BW, bx = i - by * BW;
+                int gy = y0 - R + by, gx = x0 - PA + bx;
+                bool in = gy >= 0 && gy < j.n1 && gx >= 0 && gx < j.n0;
+                if (!in && wr) {
+                    gy = wrapi(gy, j.n1);
+                    gx = wrapi(gx, j.n0);
+                    in = true;
+                }
+                if (in) v[u] = ld_l2(sp + (int64_t)gy * j.sy[src] + gx);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+            const int i = i0 + u * kBatchThreads + threadIdx.x;
+            if (i < TOTAL) box[i] = v[u];
+        }
+    }
+    __syncthreads();
+    constexpr int NW = std::is_same_v<Op, OpKdotF<T, T>> ? Sh::L : 1;
+    BatchTileP<NW> p;
+    p.bw = BW; p.bh = BH; p.ry = R; p.rz = 0; p.padl = PA; p.tw = G::TW; p.ring = 0;
+    p.n[0] = j.n0; p.n[1] = j.n1; p.n[2] = 1;
+    p.dst = j.buf[dstb];
+    p.dst_org = j.org[dstb];
+    p.dstr[0] = 1; p.dstr[1] = j.sy[dstb]; p.dstr[2] = 0;
+    p.L = oa.L; p.birth = oa.birth; p.survive = oa.survive; p.alpha = oa.alpha; p.rcp_f = oa.rcp_f;
+    p.fastdiv_f = oa.fastdiv_f; p.Lf = oa.Lf; p.Ld = oa.Ld; p.alpha_f = oa.alpha_f; p.w = nullptr;
+#pragma unroll
+    for (int k = 0; k < NW; ++k) p.wf[k] = NW > 1 ? sw[k] : 0.f;
+    compute_shape_vec<T, T, Op, Sh, G::XV, G::VS>(p, TileOrigin{x0, y0, 0}, box);
+}
+
 // reduction types the batched kernel runs
 using OpF_Mean = OpMean<float, float, float>;
 using OpF_Sum = OpSumF<float, float, float>;
@@ -243,6 +335,20 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(const BatchDev d) 
         batch_item<T, OP, Shape<KIND, RR, 2>>(j, it, bsm, so, oa);                              \
         goto item_done;                                                                         \
     }
+#define STC_BV(DT, OPV, T, OP, KIND, RR)                                                        \
+    if (key == DT * 16 + OPV && j.shape == KIND && j.R == RR && j.vec) {                        \
+        batch_tile_vec<T, OP, Shape<KIND, RR, 2>>(j, it, bsm, sw, oa);                          \
+        goto item_done;                                                                         \
+    }
+        // vector-column tiles (one step per round) for the shapes batched workloads use
+        STC_BV(STC_F32, OPV_MEAN, float, OpF_Mean, STC_SHAPE_WINDOW, 1)
+        STC_BV(STC_F32, OPV_MEAN, float, OpF_Mean, STC_SHAPE_CIRCLE, 3)
+        STC_BV(STC_F32, OPV_SUM, float, OpF_Sum, STC_SHAPE_CROSS, 2)
+        STC_BV(STC_F32, OPV_KDOT_F, float, OpF_Kdot, STC_SHAPE_WINDOW, 2)
+        STC_BV(STC_BF16, OPV_MEAN, __nv_bfloat16, OpB_Mean, STC_SHAPE_WINDOW, 1)
+        STC_BV(STC_BF16, OPV_MEAN, __nv_bfloat16, OpB_Mean, STC_SHAPE_CIRCLE, 3)
+        STC_BV(STC_BF16, OPV_KDOT_F, __nv_bfloat16, OpB_Kdot, STC_SHAPE_WINDOW, 2)
+        STC_BV(STC_U8, OPV_LIFE, uint8_t, OpU_Life, STC_SHAPE_MOORE, 1)
         // compile-time tables for the shapes batched workloads use
         STC_BS(STC_F32, OPV_MEAN, float, OpF_Mean, STC_SHAPE_WINDOW, 1)
         STC_BS(STC_F32, OPV_MEAN, float, OpF_Mean, STC_SHAPE_CIRCLE, 3)
@@ -269,6 +375,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(const BatchDev d) 
         }
 #undef STC_B
 #undef STC_BS
+#undef STC_BV
     item_done:
         __syncthreads();
         if (!j.resident) {
@@ -302,6 +409,37 @@ constexpr size_t kTiledSmemCap = 200 * 1024;
 static size_t tiled_smem(const BatchSpec& s, const Geometry& g) {
     const size_t es = dtype_size(s.a.dtype);
     return 2 * (size_t)(g.tw + 2 * g.k * s.R) * (g.th + 2 * g.k * s.R) * es;
+}
+
+// Vector-column tile geometry for the (dtype, reduction, shape, R) the kernel has a vector path for
+// (the STC_BV list of batch_kernel); false otherwise.
+static bool vec_geometry(const BatchSpec& s, int shape, int* tw, int* th, size_t* smem) {
+    auto geo = [&](auto t, auto r) {
+        using T = decltype(t);
+        constexpr int R = decltype(r)::value;
+        *tw = BatchVecGeom<T>::TW;
+        *th = BatchVecGeom<T>::TH;
+        *smem = (size_t)BatchVecBox<T, R>::BW * BatchVecBox<T, R>::BH * sizeof(T);
+        return true;
+    };
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    using I3 = std::integral_constant<int, 3>;
+    const int dt = s.a.dtype, opv = s.opv, R = s.R;
+    if (dt == STC_F32) {
+        if (opv == OPV_MEAN && shape == STC_SHAPE_WINDOW && R == 1) return geo(0.f, I1{});
+        if (opv == OPV_MEAN && shape == STC_SHAPE_CIRCLE && R == 3) return geo(0.f, I3{});
+        if (opv == OPV_SUM && shape == STC_SHAPE_CROSS && R == 2) return geo(0.f, I2{});
+        if (opv == OPV_KDOT_F && shape == STC_SHAPE_WINDOW && R == 2) return geo(0.f, I2{});
+    } else if (dt == STC_BF16) {
+        const __nv_bfloat16 b{};
+        if (opv == OPV_MEAN && shape == STC_SHAPE_WINDOW && R == 1) return geo(b, I1{});
+        if (opv == OPV_MEAN && shape == STC_SHAPE_CIRCLE && R == 3) return geo(b, I3{});
+        if (opv == OPV_KDOT_F && shape == STC_SHAPE_WINDOW && R == 2) return geo(b, I2{});
+    } else if (dt == STC_U8) {
+        if (opv == OPV_LIFE && shape == STC_SHAPE_MOORE && R == 1) return geo((uint8_t)0, I1{});
+    }
+    return false;
 }
 
 static size_t resident_smem(const BatchSpec& s) {
@@ -471,6 +609,24 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
             smem = std::max(smem, resident_smem(s));
             resident_items.push_back(BatchItem{i, 0, 0, j.nsteps});
             b->result_in_b[i] = (int)(s.nsteps & 1);
+            continue;
+        }
+        int vtw = 0, vth = 0;
+        size_t vsmem = 0;
+        if (!forced && vec_geometry(s, j.shape, &vtw, &vth, &vsmem)) {
+            // one step per round on vector-column tiles
+            j.resident = 0;
+            j.vec = 1;
+            j.tw = vtw; j.th = vth; j.k = 1;
+            j.ntx = (j.n0 + vtw - 1) / vtw;
+            j.nty = (j.n1 + vth - 1) / vth;
+            j.tiles = j.ntx * j.nty;
+            j.rounds = (int32_t)s.nsteps;
+            j.counter_base = b->ncounters;
+            b->ncounters += j.rounds;
+            smem = std::max(smem, vsmem);
+            max_rounds = std::max(max_rounds, j.rounds);
+            b->result_in_b[i] = j.rounds & 1;
             continue;
         }
         Geometry g;

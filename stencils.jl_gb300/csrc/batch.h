@@ -38,6 +38,7 @@ struct BatchJob {
     int32_t ntx, nty, tiles;
     int32_t rounds, nsteps;
     int32_t resident;
+    int32_t vec;            // tiled with the vector-column map (one step per round, tile 32*XV x 8*VS)
     int32_t shape;          // stc_shape when the job's table is that generated shape (radius R), else 0
     int32_t counter_base, off_base;
     float padf;

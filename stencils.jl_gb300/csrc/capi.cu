@@ -29,7 +29,21 @@ static std::map<std::tuple<int, int, int, int, int>, KernelEntry>& registry() {
 }
 
 void register_kernel(int dt, int opv, int kind, int R, int N, const KernelEntry& e) {
-    registry()[std::make_tuple(dt, opv, kind, R, N)] = e;
+    KernelEntry& x = registry()[std::make_tuple(dt, opv, kind, R, N)];
+    if (e.launch) {
+        x.launch = e.launch;
+        x.xt = e.xt;
+        x.vs = e.vs;
+    }
+    if (e.launch_direct) x.launch_direct = e.launch_direct;
+    if (e.launch_vec) {
+        x.launch_vec = e.launch_vec;
+        x.xv = e.xv;
+        x.vs_vec = e.vs_vec;
+    }
+    x.kind = e.kind;
+    x.R = e.R;
+    x.N = e.N;
 }
 
 const KernelEntry* find_kernel(int dt, int opv, int kind, int R, int N) {
@@ -361,13 +375,19 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
 
     // tile geometry
     const bool specialised = e->kind != STC_SHAPE_TABLE;
+    // The vector-column variant needs the tile's first column on an XV-aligned shared-memory index.
+    // padl (below) is congruent to the tensor-map x of logical 0 modulo 16 bytes, so that is hx[0] % XV.
+    const char* nv = getenv("STC_NO_VEC");   // tuning / test override: one column per lane
+    const bool vec = specialised && e->launch_vec && !(nv && nv[0] == '1') && (p.hx[0] % e->xv) == 0;
+    const int xcols = vec ? e->xv : e->xt, vslots = vec ? e->vs_vec : e->vs;
     p.tiles3d = specialised ? (e->N == 3) : (nd == 3);
-    p.tw = 32 * e->xt;
-    p.th = p.tiles3d ? kMapWarps : kMapWarps * e->vs;
-    p.tz = p.tiles3d ? e->vs : 1;
+    p.tw = 32 * xcols;
+    p.th = p.tiles3d ? kMapWarps : kMapWarps * vslots;
+    p.tz = p.tiles3d ? vslots : 1;
     const int V = 16 / es;
     p.padl = p.rx + (int)(((p.hx[0] - p.rx) % V + V) % V);
-    p.bw = (int)align_up(p.padl + p.tw + p.rx, V);
+    const int reach = vec ? (int)align_up(p.rx, e->xv) : p.rx;   // loaded columns right of the tile
+    p.bw = (int)align_up(p.padl + p.tw + reach, V);
     p.bh = p.th + 2 * p.ry;
     p.bd = p.tz + 2 * p.rz;
     p.ntx = cdiv(p.n[0], p.tw);
@@ -411,8 +431,9 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
         err = e->launch_direct(p, stream, ctx->num_sms);
         kname = "map_direct";
     } else {
-        err = e->launch(p, stream, ctx->num_sms);
-        kname = specialised ? (tma ? "map_shape_tma" : "map_shape_ldg") : (tma ? "map_table_tma" : "map_table_ldg");
+        err = (vec ? e->launch_vec : e->launch)(p, stream, ctx->num_sms);
+        kname = vec ? (tma ? "map_vec_tma" : "map_vec_ldg")
+                    : specialised ? (tma ? "map_shape_tma" : "map_shape_ldg") : (tma ? "map_table_tma" : "map_table_ldg");
     }
     prof_end(prof, stream, kname, (double)cells * (es + dtype_size(dst->dtype)), (double)cells);
     return cuda_fail(err);
@@ -519,6 +540,8 @@ static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil*
     const bool fixed_ring = bc->boundary == STC_REMOVE;
     if (!rc && fixed_ring) rc = launch_halo_fill(&pg[0], R, &hb, s);
     if (!rc && fixed_ring) rc = launch_halo_fill(&pg[1], R, &hb, s);
+    // Wrap / Reflect: the ring is refreshed (K2) before every step.  (Writing each output's ring images
+    // from the map kernel instead measured slower on 512^3: 384 us per step against 188 + 41 us.)
     int cur = 0;
     for (int64_t k = 0; k < nsteps && !rc; ++k) {
         if (!fixed_ring && (rc = launch_halo_fill(&pg[cur], R, &hb, s))) break;

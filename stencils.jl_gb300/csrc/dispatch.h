@@ -22,10 +22,13 @@ struct KernelEntry {
     LaunchFn launch = nullptr;       // tiled kernel (TMA or cooperative loads)
     LaunchFn launch_direct = nullptr;  // per-output global gather, for boxes too large for shared memory
     int xt = 1, vs = 1;              // columns per thread, stream slots per thread
+    LaunchFn launch_vec = nullptr;   // shape kernels: XV adjacent columns per thread (vector loads)
+    int xv = 0, vs_vec = 1;
     int kind = STC_SHAPE_TABLE, R = 0, N = 0;
 };
 
-// kind == STC_SHAPE_TABLE for the generic kernels (R, N ignored)
+// kind == STC_SHAPE_TABLE for the generic kernels (R, N ignored).  Registering the same key twice
+// merges the launchers given (tiled / direct / vector), so each variant registers on its own.
 void register_kernel(int src_dtype, int opv, int kind, int R, int N, const KernelEntry& e);
 const KernelEntry* find_kernel(int src_dtype, int opv, int kind, int R, int N);
 

@@ -131,7 +131,7 @@ int launch_halo_fill(const stc_grid* g, int radius, const stc_bc* bc, cudaStream
         if (p.n[d] + 2 * radius >= (1ll << 31)) return STC_ERR_UNSUPPORTED;
     const int threads = 256;
     int64_t blocks = (p.total + threads - 1) / threads;
-    if (blocks > (int64_t)ctx->num_sms * 8) blocks = (int64_t)ctx->num_sms * 8;
+    if (blocks > (int64_t)ctx->num_sms * 6) blocks = (int64_t)ctx->num_sms * 6;   // one wave (6 CTAs/SM resident)
     if (blocks < 1) blocks = 1;
     void* prof = prof_begin(stream);
     switch (g->dtype) {

@@ -17,6 +17,7 @@
 //    all outputs of the thread that need it, while keeping each output's fold order.
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #include "common.cuh"
@@ -568,14 +569,200 @@ __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrig
     }
 }
 
+// ---------------------------------------------------------------------------- compute: vector columns
+// Fold type of the vector path.  A 16-bit float source accumulated in Float32 is widened once per
+// loaded element (exact), and the op is the same op over Float32 inputs: for these ops
+// step(a, v) == step_f32(a, float(v)) and finish(a, c) == finish_f32(a, float(c)), so every output is
+// bit-identical to the one-column path.
+template <class Op> struct Widen { using type = Op; static constexpr bool kWide = false; };
+#define STC_WIDEN3(OPT)                                                                                    \
+    template <class Tout> struct Widen<OPT<__nv_bfloat16, Tout, float>> { using type = OPT<float, Tout, float>; static constexpr bool kWide = true; }; \
+    template <class Tout> struct Widen<OPT<__half, Tout, float>> { using type = OPT<float, Tout, float>; static constexpr bool kWide = true; };
+STC_WIDEN3(OpMean)
+STC_WIDEN3(OpSumF)
+STC_WIDEN3(OpDiffuse)
+#undef STC_WIDEN3
+template <class Tout> struct Widen<OpKdotF<__nv_bfloat16, Tout>> { using type = OpKdotF<float, Tout>; static constexpr bool kWide = true; };
+template <class Tout> struct Widen<OpKdotF<__half, Tout>> { using type = OpKdotF<float, Tout>; static constexpr bool kWide = true; };
+template <class Tout, bool MAX> struct Widen<OpMinMaxF<__nv_bfloat16, Tout, float, MAX>> { using type = OpMinMaxF<float, Tout, float, MAX>; static constexpr bool kWide = true; };
+template <class Tout, bool MAX> struct Widen<OpMinMaxF<__half, Tout, float, MAX>> { using type = OpMinMaxF<float, Tout, float, MAX>; static constexpr bool kWide = true; };
+
+// XV consecutive elements at an XV*sizeof(Tin)-aligned shared address, widened to V.
+template <class Tin, class V, int XV>
+__device__ __forceinline__ void ld_row_vec(const Tin* p, V* out) {
+    constexpr int B = XV * (int)sizeof(Tin);
+    static_assert(B == 2 || B == 4 || B == 8 || B == 16, "vector width");
+    uint32_t w[B >= 4 ? B / 4 : 1];
+    if constexpr (B == 16) { const uint4 u = *(const uint4*)p; w[0] = u.x; w[1] = u.y; w[2] = u.z; w[3] = u.w; }
+    else if constexpr (B == 8) { const uint2 u = *(const uint2*)p; w[0] = u.x; w[1] = u.y; }
+    else if constexpr (B == 4) { w[0] = *(const uint32_t*)p; }
+    else { w[0] = *(const uint16_t*)p; }
+    if constexpr (std::is_same_v<V, float> && std::is_same_v<Tin, __nv_bfloat16>) {
+        // bfloat16 -> float is the 16 bits placed on top of a zero low half
+#pragma unroll
+        for (int i = 0; i < XV / 2; ++i) {
+            out[2 * i] = __uint_as_float(w[i] << 16);
+            out[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+        }
+    } else if constexpr (std::is_same_v<V, float> && std::is_same_v<Tin, __half>) {
+#pragma unroll
+        for (int i = 0; i < XV / 2; ++i) {
+            __half2 h;
+            memcpy(&h, &w[i], 4);
+            const float2 f = __half22float2(h);
+            out[2 * i] = f.x;
+            out[2 * i + 1] = f.y;
+        }
+    } else {
+        static_assert(std::is_same_v<V, Tin>, "only 16-bit floats are widened");
+        memcpy(out, w, B);
+    }
+}
+
+// XV consecutive outputs to global memory: one or two vector stores when `aligned`, else per element
+// (with the ragged right edge masked by `nvalid`).
+template <class Tout, int XV>
+__device__ __forceinline__ void st_row_vec(Tout* d, const Tout* v, bool aligned, int nvalid) {
+    constexpr int B = XV * (int)sizeof(Tout);
+    if (aligned && nvalid >= XV) {
+        if constexpr (B == 32) {
+            uint4 u[2];
+            memcpy(u, v, 32);
+            ((uint4*)d)[0] = u[0];
+            ((uint4*)d)[1] = u[1];
+        } else if constexpr (B == 16) {
+            uint4 u;
+            memcpy(&u, v, 16);
+            *(uint4*)d = u;
+        } else if constexpr (B == 8) {
+            uint2 u;
+            memcpy(&u, v, 8);
+            *(uint2*)d = u;
+        } else if constexpr (B == 4) {
+            uint32_t u;
+            memcpy(&u, v, 4);
+            *(uint32_t*)d = u;
+        } else {
+#pragma unroll
+            for (int c = 0; c < XV; ++c) d[c] = v[c];
+        }
+        return;
+    }
+#pragma unroll
+    for (int c = 0; c < XV; ++c)
+        if (c < nvalid) d[c] = v[c];
+}
+
+// Register-rotation stream as compute_shape, but each thread owns XV adjacent columns
+// (lane*XV .. lane*XV + XV - 1), so one row of its box neighbourhood is NV aligned vector loads
+// (the reach PA = R rounded up to XV on each side) instead of one scalar load per tap column, and the
+// XV outputs of a row are stored together.  Requires the tile's first column at a shared-memory index
+// that is a multiple of XV (the host checks this).  Fold order per output: the table's, as above.
+// P: MapParams, or any struct with the same geometry, destination and reduction fields (the batched
+// kernel passes a per-tile one).
+template <class Tin, class Tout, class Op, class Sh, int XV, int VS, class P>
+__device__ __forceinline__ void compute_shape_vec(const P& p, const TileOrigin& o, const Tin* box) {
+    using OpV = typename Widen<Op>::type;
+    using V = std::conditional_t<Widen<Op>::kWide, float, Tin>;
+    constexpr int N = Sh::kN, R = Sh::kR, L = Sh::L;
+    constexpr int D = 2 * R + 1;
+    constexpr int RY = (N == 3) ? R : 0;
+    constexpr int PA = (R + XV - 1) / XV * XV;
+    constexpr int NV = 1 + 2 * PA / XV;
+    constexpr int NE = NV * XV;
+    constexpr int NROW = VS + 2 * R;
+    constexpr bool FULL = NROW * L * XV <= 700;
+    constexpr auto T = Sh::table;
+    static_assert(((N == 3) ? T.o[0].z : T.o[0].y) == -R, "tables start at the lowest stream offset");
+    using A = typename OpV::A;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    A acc[D][XV];
+    V ctr[D][XV];
+#pragma unroll
+    for (int q = 0; q < D; ++q)
+#pragma unroll
+        for (int c = 0; c < XV; ++c) { acc[q][c] = A(0); ctr[q][c] = V(0); }
+    const int sr = (N == 3) ? p.bh * p.bw : p.bw;
+    const Tin* bb = box + ((N == 3) ? (warp + p.ry - RY) * p.bw : p.rz * p.bh * p.bw + warp * VS * p.bw) +
+                    p.padl - PA + lane * XV;
+    const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0) - lane * XV;   // valid outputs of this thread's XV
+    const int nvs = (N == 3) ? (int)min((int64_t)VS, p.n[2] - o.z0) : (int)min((int64_t)VS, p.n[1] - o.y0 - warp * VS);
+    const bool row_ok = (N == 3) ? (o.y0 + warp < p.n[1]) : true;
+    Tout* dbase = (Tout*)p.dst + p.dst_org + o.x0 + lane * XV +
+                  ((N == 3) ? (o.y0 + warp) * p.dstr[1] + o.z0 * p.dstr[2] : (o.y0 + warp * VS) * p.dstr[1]);
+    const int64_t dstep = (N == 3) ? p.dstr[2] : p.dstr[1];
+    constexpr int VA = (XV * (int)sizeof(Tout)) < 16 ? XV * (int)sizeof(Tout) : 16;
+    const bool aligned = (((uintptr_t)((Tout*)p.dst + p.dst_org)) % VA) == 0 &&
+                         ((p.dstr[1] * (int64_t)sizeof(Tout)) % VA) == 0 && ((p.dstr[2] * (int64_t)sizeof(Tout)) % VA) == 0;
+    auto row = [&](const int r, const int u) {
+        V v[2 * RY + 1][NE];
+#pragma unroll
+        for (int yy = 0; yy < 2 * RY + 1; ++yy)
+#pragma unroll
+            for (int j = 0; j < NV; ++j) ld_row_vec<Tin, V, XV>(bb + r * sr + yy * p.bw + j * XV, &v[yy][j * XV]);
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            const int sidx = r - q;
+            if (sidx < 0 || sidx >= VS) continue;
+            const int slot = ((u - q) % D + D) % D;
+            if (OpV::kZeroInit && q == 0) {
+#pragma unroll
+                for (int c = 0; c < XV; ++c) acc[slot][c] = OpV::first(V(0), 0);
+            }
+#pragma unroll
+            for (int k = 0; k < L; ++k) {
+                const int ko = (N == 3) ? T.o[k].z : T.o[k].y;
+                if (ko != q - R) continue;
+                const int oy = (N == 3) ? T.o[k].y : 0;
+#pragma unroll
+                for (int c = 0; c < XV; ++c) {
+                    const V val = v[oy + RY][PA + c + T.o[k].x];
+                    if (!OpV::kZeroInit && k == 0) acc[slot][c] = OpV::first(val, 0);
+                    else acc[slot][c] = OpV::step(acc[slot][c], val, k, p);
+                }
+            }
+            if (OpV::kNeedsCentre && q == R) {
+#pragma unroll
+                for (int c = 0; c < XV; ++c) ctr[slot][c] = v[RY][PA + c];
+            }
+            if (q == D - 1 && sidx < nvs && row_ok && nvx > 0) {
+                Tout res[XV];
+#pragma unroll
+                for (int c = 0; c < XV; ++c) {
+                    if constexpr (std::is_same_v<OpV, OpMean<V, Tout, A>>)
+                        res[c] = OpV::template finish_c<L>(acc[slot][c], ctr[slot][c], p);
+                    else
+                        res[c] = OpV::finish(acc[slot][c], ctr[slot][c], p);
+                }
+                st_row_vec<Tout, XV>(dbase + sidx * dstep, res, aligned, nvx);
+            }
+        }
+    };
+    if constexpr (FULL) {
+#pragma unroll
+        for (int r = 0; r < NROW; ++r) row(r, r % D);
+    } else {
+        for (int r0 = 0; r0 < NROW; r0 += D) {
+#pragma unroll
+            for (int u = 0; u < D; ++u) {
+                const int r = r0 + u;
+                if (r >= NROW) break;
+                row(r, u);
+            }
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------- the kernel
-template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
-__global__ void __launch_bounds__(kMapThreads) map_kernel(const __grid_constant__ MapParams p) {
+// VEC selects compute_shape_vec, with XT then the number of adjacent columns per thread.
+template <class Tin, class Tout, class Op, class Sh, int XT, int VS, bool VEC>
+__device__ __forceinline__ void map_body(const MapParams& p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     uint64_t* bars = (uint64_t*)(smem_raw + (size_t)p.stages * p.stage_bytes);
     auto stage_box = [&](int s) { return (Tin*)(smem_raw + (size_t)s * p.stage_bytes); };
     auto compute = [&](const TileOrigin& o, const Tin* box) {
         if constexpr (Sh::kKind == STC_SHAPE_TABLE) compute_generic<Tin, Tout, Op, XT, VS>(p, o, box);
+        else if constexpr (VEC) compute_shape_vec<Tin, Tout, Op, Sh, XT, VS>(p, o, box);
         else compute_shape<Tin, Tout, Op, Sh, XT, VS>(p, o, box);
     };
     const int64_t step = gridDim.x;
@@ -632,6 +819,18 @@ __global__ void __launch_bounds__(kMapThreads) map_kernel(const __grid_constant_
         compute(o, box);
         __syncthreads();
     }
+}
+
+template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
+__global__ void __launch_bounds__(kMapThreads) map_kernel(const __grid_constant__ MapParams p) {
+    map_body<Tin, Tout, Op, Sh, XT, VS, false>(p);
+}
+
+// The vector-column variant keeps its XV x (2R+1) accumulators and loaded rows in registers; MINB
+// resident CTAs per SM bound its registers (two CTAs: up to 128 per thread).
+template <class Tin, class Tout, class Op, class Sh, int XV, int VS, int MINB>
+__global__ void __launch_bounds__(kMapThreads, MINB) map_vec_kernel(const __grid_constant__ MapParams p) {
+    map_body<Tin, Tout, Op, Sh, XV, VS, true>(p);
 }
 
 }  // namespace stc

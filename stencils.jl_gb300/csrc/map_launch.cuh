@@ -63,10 +63,10 @@ static cudaError_t prepare_launch(K kern, LaunchCache& c, size_t smem, int* per_
     return cudaSuccess;
 }
 
-template <class Tin, class Tout, class Op, class Sh, int XT, int VS>
+template <class Tin, class Tout, class Op, class Sh, int XT, int VS, bool VEC = false, int MINB = 2>
 cudaError_t launch_tiled(MapParams& p, cudaStream_t stream, int num_sms) {
     static LaunchCache cache;
-    auto kern = map_kernel<Tin, Tout, Op, Sh, XT, VS>;
+    auto kern = VEC ? map_vec_kernel<Tin, Tout, Op, Sh, XT, VS, MINB> : map_kernel<Tin, Tout, Op, Sh, XT, VS>;
     const size_t smem = (size_t)(p.use_tma ? p.stages : 1) * p.stage_bytes + (size_t)kMaxStages * 8;
     int per_sm = 0;
     cudaError_t e = prepare_launch(kern, cache, smem, &per_sm);
@@ -146,6 +146,24 @@ struct RegisterShape {
         e.launch = &launch_tiled<typename F::Tin, typename F::Tout, typename F::Op, Shape<KIND, R, N>, XT, VS>;
         e.xt = XT;
         e.vs = VS;
+        e.kind = KIND;
+        e.R = R;
+        e.N = N;
+        register_kernel(DT, OPV, KIND, R, N, e);
+    }
+};
+
+// The vector-column variant of a shape kernel (XV adjacent columns per thread); launch_map uses it
+// when the tile's first column lands on an XV-aligned shared-memory index, else the variant above.
+template <int DT, int OPV, int KIND, int R, int N, int XV, int VS, int MINB = 2>
+struct RegisterShapeVec {
+    RegisterShapeVec() {
+        using F = OpFor<DT, OPV>;
+        static_assert(XV * sizeof(typename F::Tin) <= 16, "one vector load per XV columns");
+        KernelEntry e;
+        e.launch_vec = &launch_tiled<typename F::Tin, typename F::Tout, typename F::Op, Shape<KIND, R, N>, XV, VS, true, MINB>;
+        e.xv = XV;
+        e.vs_vec = VS;
         e.kind = KIND;
         e.R = R;
         e.N = N;

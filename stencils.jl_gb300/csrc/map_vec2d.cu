@@ -1,0 +1,21 @@
+// Vector-column variants (XV adjacent columns per thread, aligned vector shared-memory loads and
+// global stores) of the 2D shape-specialised map kernels.  Template arguments: <source type,
+// reduction, shape, R, N, columns per thread, stream slots per thread>.
+#include "map_launch.cuh"
+
+namespace stc {
+// 7x7 and 5x5 kernels, f32 accumulation
+static RegisterShapeVec<STC_F32, OPV_KDOT_F, STC_SHAPE_WINDOW, 3, 2, 4, 8> v0;
+static RegisterShapeVec<STC_BF16, OPV_KDOT_F, STC_SHAPE_WINDOW, 3, 2, 4, 8> v1;
+static RegisterShapeVec<STC_F32, OPV_KDOT_F, STC_SHAPE_WINDOW, 2, 2, 4, 8> v2;
+// mean blur Window(1)
+static RegisterShapeVec<STC_F64, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 2, 8> v3;
+static RegisterShapeVec<STC_F32, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 4, 8> v4;
+static RegisterShapeVec<STC_BF16, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 4, 8> v5;
+// Circle(3) mean, Cross(2) sum
+static RegisterShapeVec<STC_F32, OPV_MEAN, STC_SHAPE_CIRCLE, 3, 2, 4, 8> v6;
+static RegisterShapeVec<STC_F32, OPV_SUM, STC_SHAPE_CROSS, 2, 2, 4, 8> v7;
+// Life on bytes, Moore(1)
+static RegisterShapeVec<STC_U8, OPV_LIFE, STC_SHAPE_MOORE, 1, 2, 4, 16> v8;
+static RegisterShapeVec<STC_BOOL, OPV_LIFE, STC_SHAPE_MOORE, 1, 2, 4, 16> v9;
+}  // namespace stc
