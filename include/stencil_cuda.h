@@ -14,6 +14,10 @@
  *                         (and gatherstencil(f, source), which allocates dest,   src/gatherstencil.jl:14-39)
  *   stc_map_steps         repeated  A = gatherstencil!(f, A::SwitchingStencilArray) src/gatherstencil.jl:77-83
  *                         with switch(A)                                        src/array.jl:610-611
+ *   stc_map_terms         gatherstencil!(f, dest, source, args...) with several arrays, f a
+ *                         registered sum of per-array terms                      src/gatherstencil.jl:84-113
+ *   stc_scatter           scatterstencil!(f, op, dest, source) for registered f and op
+ *                                                                                src/scatterstencil.jl:36-133
  *   stc_update_boundary   update_boundary!(A::AbstractStencilArray)              src/array.jl:195-233
  *   stc_mass              no counterpart: FP64 compensated total of a grid, used to report the mass
  *                         drift of long multi-step runs.
@@ -161,6 +165,62 @@ STC_API int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded
 STC_API int stc_map_steps(const stc_grid* a, const stc_grid* b,
                   const stc_stencil* stencil, const stc_op* op, const stc_bc* bc,
                   int64_t nsteps, int32_t* out_src_is_b, void* stream, uint32_t flags);
+
+/* ---- maps over several arrays: mapstencil(f, A, args...) (src/gatherstencil.jl:84-113) ----
+ * The reference passes f the stencil of every StencilArray argument at I and the value at I of every
+ * plain array (`_getarg`, src/gatherstencil.jl:111-112).  The registered f is a left-to-right sum of
+ * one term per argument, t_1 + t_2 + ... + t_n, each term
+ *     CENTER  center(hood)            VALUE   arg[I]               (a plain array: stencil/bc NULL)
+ *     SUM     sum(neighbors(hood))    MEAN    mean(neighbors(hood))   KDOT  kernelproduct(hood)
+ * optionally scaled, alpha * term (scaled != 0), as in `c + 0.1 * sum(neighbors(hood_r))`.  All
+ * arithmetic is in the element type of the grids (Float64 or Float32, all the same; alpha is applied
+ * in that type); sums fold in offset order exactly as stc_map.  Every StencilArray argument keeps its
+ * own stencil, boundary and padding, and Halo arguments get update_boundary! first.  All logical
+ * sizes must equal dest's (else STC_ERR_SIZE_MISMATCH, src/gatherstencil.jl:115-121). */
+typedef enum {
+    STC_TERM_CENTER = 0, STC_TERM_SUM = 1, STC_TERM_MEAN = 2, STC_TERM_KDOT = 3, STC_TERM_VALUE = 4
+} stc_term_kind;
+
+typedef struct {
+    int32_t kind;                 /* stc_term_kind */
+    int32_t scaled;               /* nonzero: alpha * term */
+    double  alpha;
+    const stc_grid* grid;         /* the argument's parent */
+    const stc_stencil* stencil;   /* its stencil (NULL for VALUE) */
+    const stc_bc* bc;             /* its boundary and padding (NULL for VALUE) */
+} stc_term;
+
+#define STC_MAX_TERMS 4
+#define STC_MAX_TERM_LEN 64
+
+/* dest[I] = t_1 + ... + t_n over dest's logical indices; dst_padded as in stc_map, relative to the
+ * first term's padding (the SwitchingStencilArray form writes the padded dest parent). */
+STC_API int stc_map_terms(const stc_term* terms, int32_t nterms, const stc_grid* dst, int32_t dst_padded,
+                          void* stream, uint32_t flags);
+
+/* ---- scatterstencil!(f, op, dest, source) (src/scatterstencil.jl:36-133) ----
+ * Each source cell s computes one value per stencil offset k, v_k = f(stencil(source, s))[k], and
+ * combines it into dest at s + offset_k: dest[t] = op(dest[t], v_k).  Out-of-range targets are skipped
+ * for Remove and Use, wrapped for Wrap and reflected for Reflect (src/scatterstencil.jl:76-112).
+ * Registered f: CONST (v_k = constant, as `map(_ -> c, neighbors(hood))`), CENTER
+ * (v_k = center(hood)) and WEIGHTED (v_k = center(hood) * kernel[k], a Kernel stencil's weights);
+ * registered op: ADD (+), MAX, MIN (Julia's max/min).  2D grids, Float64 or Float32, dest the
+ * logical size of source, combined in the element type.  Every dest cell receives its contributions
+ * in the order of the reference's pass schedule run on one thread (passes p = 1..2R+1 over the columns
+ * j = p, p + 2R + 1, ...; rows in order; offsets in order), so results are deterministic and bit-exact
+ * with it (the reference's threaded passes give that order too, except that with Wrap, columns of one
+ * pass meet at the seam when the column count is not a multiple of 2R + 1). */
+typedef enum { STC_SCATTER_CONST = 0, STC_SCATTER_CENTER = 1, STC_SCATTER_WEIGHTED = 2 } stc_scatter_value;
+typedef enum { STC_COMBINE_ADD = 0, STC_COMBINE_MAX = 1, STC_COMBINE_MIN = 2 } stc_combine;
+
+typedef struct {
+    int32_t value;       /* stc_scatter_value */
+    int32_t combine;     /* stc_combine */
+    double  constant;    /* CONST */
+} stc_scatter_op;
+
+STC_API int stc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* stencil, const stc_scatter_op* op,
+                        const stc_bc* bc, void* stream, uint32_t flags);
 
 /* update_boundary!: write the halo ring of a Halo-padded parent from its interior. */
 STC_API int stc_update_boundary(const stc_grid* parent, int32_t radius, const stc_bc* bc,

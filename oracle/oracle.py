@@ -39,6 +39,8 @@ def lib():
         _lib.orc_map_steps.argtypes = [P(A.Grid), P(A.Grid), P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc),
                                        C.c_int64, C.c_int, P(C.c_int)]
         _lib.orc_update_boundary.argtypes = [P(A.Grid), C.c_int, P(A.BcDesc)]
+        _lib.orc_map_terms.argtypes = [P(A.TermDesc), C.c_int, P(A.Grid), C.c_int, C.c_int]
+        _lib.orc_scatter.argtypes = [P(A.Grid), P(A.Grid), P(A.StencilDesc), C.c_void_p, P(A.BcDesc)]
         _lib.orc_mass.argtypes = [P(A.Grid), C.c_int, C.c_int]
         _lib.orc_mass.restype = C.c_double
         _lib.orc_result_dtype.argtypes = [C.c_int, C.c_int, C.c_int]
@@ -146,3 +148,41 @@ def mass(a: np.ndarray, code: int, radius: int = 0, padding_code: int = 0) -> fl
 
 def default_threads() -> int:
     return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def map_terms(f, args, code: int, *, dst_padded: bool = False, nthreads: int = 1) -> np.ndarray:
+    """mapstencil(f, args...) for a registered sum of terms `f` (stencils_gb300.Terms).
+
+    `args` are (parent, stencil, boundary, padding) tuples for StencilArray arguments or plain numpy
+    arrays; parents are updated in place like the reference's update_boundary!.  Returns the new dest.
+    """
+    from stencils_gb300 import _abi as A
+    descs, keep = f.lower(args, code, lambda a: _grid(a, code))
+    first = args[0]
+    if isinstance(first, tuple):
+        parent, stencil, _, padding = first
+        R = stencil.radius if padding.code != 0 else 0
+        shape = tuple(s - 2 * R + (2 * R if dst_padded else 0) for s in parent.shape)
+    else:
+        shape = first.shape
+    dst = alloc(shape, code)
+    gd = _grid(dst, code)
+    arr = (A.TermDesc * len(descs))(*descs)
+    _check(lib().orc_map_terms(arr, len(descs), C.byref(gd), int(dst_padded), nthreads), "map_terms")
+    del keep
+    return dst
+
+
+def scatter(f, op, dest: np.ndarray, src: np.ndarray, code: int, stencil, boundary, padding) -> np.ndarray:
+    """scatterstencil!(f, op, dest, StencilArray(src parent, ...)) in place on `dest` (returned)."""
+    from stencils_gb300 import _abi as A
+    from stencils_gb300.scatter import ScatterOpDesc, _combine_code
+    d = ScatterOpDesc()
+    d.value = f.code
+    d.combine = _combine_code(op)
+    d.constant = f.constant
+    lst = A.LoweredStencil(stencil)
+    bc = A.lower_bc(boundary, padding)
+    gs, gd = _grid(src, code), _grid(dest, code)
+    _check(lib().orc_scatter(C.byref(gs), C.byref(gd), C.byref(lst.desc), C.byref(d), C.byref(bc)), "scatter")
+    return dest

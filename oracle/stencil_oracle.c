@@ -529,3 +529,160 @@ int orc_max_threads(void) {
 }
 
 uint16_t orc_f32_to_bf16(float f) { return f32_to_bf16(f); }
+
+/* ---------------------------------------------------------------- maps over several arrays */
+/* mapstencil(f, A, args...) with f = t_1 + t_2 + ... (src/gatherstencil.jl:84-113): term m is
+ * center(hood), sum / mean / kernelproduct of the neighbours of argument m's stencil at I, or the
+ * value of a plain array at I (`_getarg`, src/gatherstencil.jl:111-112), optionally alpha * term.
+ * Arithmetic in the element type T (Float64 or Float32), each operation rounded, left to right. */
+#define ORC_TERM_BODY(T)                                                                               \
+    do {                                                                                               \
+        T acc = 0;                                                                                     \
+        for (int m = 0; m < nterms; ++m) {                                                             \
+            const stc_term* tm = &terms[m];                                                            \
+            T g;                                                                                       \
+            if (tm->kind == STC_TERM_VALUE) {                                                          \
+                g = (T)load_f(vw[m].data, vw[m].dt, poff(&vw[m], I));                                  \
+            } else {                                                                                   \
+                val_t centre;                                                                          \
+                gather(&gt[m], I, vals, &centre);                                                      \
+                const int L = tm->stencil->len;                                                        \
+                if (tm->kind == STC_TERM_CENTER) {                                                     \
+                    g = (T)centre.f;                                                                   \
+                } else if (tm->kind == STC_TERM_KDOT) {                                                \
+                    g = (T)0;                                                                          \
+                    for (int k = 0; k < L; ++k) {                                                      \
+                        T w = (T)tm->stencil->weights[k];                                              \
+                        T prod = (T)vals[k].f * w;                                                     \
+                        g = g + prod;                                                                  \
+                    }                                                                                  \
+                } else {                                                                               \
+                    g = (T)vals[0].f;                                                                  \
+                    for (int k = 1; k < L; ++k) g = g + (T)vals[k].f;                                  \
+                    if (tm->kind == STC_TERM_MEAN) g = g / (T)L;                                       \
+                }                                                                                      \
+            }                                                                                          \
+            if (tm->scaled) g = (T)tm->alpha * g;                                                      \
+            acc = m == 0 ? g : acc + g;                                                                \
+        }                                                                                              \
+        T out = acc;                                                                                   \
+        store_raw(dst->data, dst->dtype, doff, &out);                                                  \
+    } while (0)
+
+int orc_map_terms(const stc_term* terms, int nterms, const stc_grid* dst, int dst_padded, int nthreads) {
+    if (!terms || !dst || nterms < 1 || nterms > STC_MAX_TERMS) return STC_ERR_INVALID;
+    const int dt = dst->dtype;
+    if (dt != STC_F64 && dt != STC_F32) return STC_ERR_UNSUPPORTED;
+    view_t vw[STC_MAX_TERMS];
+    gather_t gt[STC_MAX_TERMS];
+    int maxL = 1;
+    for (int m = 0; m < nterms; ++m) {
+        const stc_term* tm = &terms[m];
+        if (!tm->grid || tm->grid->dtype != dt || tm->grid->ndims != dst->ndims) return STC_ERR_INVALID;
+        if (tm->kind == STC_TERM_VALUE) {
+            int rc = make_view(tm->grid, 0, STC_CONDITIONAL, &vw[m]);
+            if (rc) return rc;
+        } else {
+            const stc_stencil* st = tm->stencil;
+            const stc_bc* bc = tm->bc;
+            if (!st || !bc) return STC_ERR_INVALID;
+            if (bc->boundary == STC_USE && bc->padding == STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
+            if (tm->kind == STC_TERM_KDOT && !st->weights) return STC_ERR_KERNEL_LENGTH;
+            int rc = orc_update_boundary(tm->grid, st->radius, bc);
+            if (rc) return rc;
+            rc = make_view(tm->grid, st->radius, bc->padding, &gt[m].src);
+            if (rc) return rc;
+            vw[m] = gt[m].src;
+            gt[m].st = st;
+            gt[m].bc = bc;
+            gt[m].fkind = 1;
+            gt[m].padf = dt == STC_F32 ? (double)(float)bc->padval : bc->padval;
+            gt[m].padi = 0;
+            if (st->len > maxL) maxL = st->len;
+        }
+        for (int d = 0; d < 3; ++d)
+            if (vw[m].n[d] != vw[0].n[d]) return STC_ERR_SIZE_MISMATCH;
+    }
+    const int R0 = (terms[0].kind != STC_TERM_VALUE && terms[0].bc->padding != STC_CONDITIONAL)
+                       ? terms[0].stencil->radius : 0;
+    int64_t dorg = 0;
+    for (int d = 0; d < dst->ndims; ++d) {
+        if (dst->size[d] != vw[0].n[d] + (dst_padded ? 2 * R0 : 0)) return STC_ERR_SIZE_MISMATCH;
+        if (dst_padded) dorg += (int64_t)R0 * dst->stride[d];
+    }
+    const int64_t n0 = vw[0].n[0], n1 = vw[0].n[1], n2 = vw[0].n[2];
+    const int64_t total = n0 * n1 * n2;
+    int64_t dst_st[3] = {dst->stride[0], dst->ndims > 1 ? dst->stride[1] : 0, dst->ndims > 2 ? dst->stride[2] : 0};
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel num_threads(nthreads)
+    {
+        val_t* vals = (val_t*)malloc(sizeof(val_t) * (size_t)maxL);
+#pragma omp for schedule(static)
+        for (int64_t lin = 0; lin < total; ++lin) {
+            int64_t I[3] = {lin % n0, (lin / n0) % n1, lin / (n0 * n1)};
+            int64_t doff = dorg + I[0] * dst_st[0] + I[1] * dst_st[1] + I[2] * dst_st[2];
+            if (dt == STC_F64) ORC_TERM_BODY(double);
+            else ORC_TERM_BODY(float);
+        }
+        free(vals);
+    }
+    return STC_OK;
+}
+
+/* ---------------------------------------------------------------- scatterstencil! */
+/* scatterstencil!(f, op, dest, source) (src/scatterstencil.jl:36-74) run on one thread: passes over the
+ * columns j = p, p + stride, ... (stride = 2R + 1), rows in order, offsets in order; targets mapped by
+ * _scatter_to! (src/scatterstencil.jl:76-112): Remove/Use skip, Wrap mod1, Reflect 2 - i / 2n - i. */
+static int scatter_target(int boundary, int64_t t, int64_t n, int64_t* out) {
+    if (t >= 0 && t < n) { *out = t; return 1; }
+    if (boundary == STC_WRAP) { int64_t m = t % n; *out = m < 0 ? m + n : m; return 1; }
+    if (boundary == STC_REFLECT) { *out = t < 0 ? -t : 2 * n - 2 - t; return 1; }
+    return 0;
+}
+
+#define ORC_SCATTER_BODY(T, ADDF, MAXF, MINF)                                                          \
+    do {                                                                                               \
+        T* d = (T*)dst->data;                                                                          \
+        for (int64_t p = 0; p < stride; ++p)                                                           \
+            for (int64_t j = p; j < nx; j += stride)                                                   \
+                for (int64_t i = 0; i < ny; ++i) {                                                     \
+                    const int64_t I[3] = {i, j, 0};                                                    \
+                    const T c = (T)load_f(v.data, v.dt, poff(&v, I));                                  \
+                    for (int k = 0; k < st->len; ++k) {                                                \
+                        T val;                                                                         \
+                        if (op->value == STC_SCATTER_CONST) val = (T)op->constant;                     \
+                        else if (op->value == STC_SCATTER_CENTER) val = c;                             \
+                        else { T w = (T)st->weights[k]; val = c * w; }                                 \
+                        int64_t ti, tj;                                                                \
+                        if (!scatter_target(bc->boundary, i + st->offsets[2 * k], ny, &ti)) continue;  \
+                        if (!scatter_target(bc->boundary, j + st->offsets[2 * k + 1], nx, &tj)) continue; \
+                        T* q = d + ti * dst->stride[0] + tj * dst->stride[1];                          \
+                        if (op->combine == STC_COMBINE_ADD) *q = ADDF(*q, val);                        \
+                        else if (op->combine == STC_COMBINE_MAX) *q = MAXF(*q, val);                   \
+                        else *q = MINF(*q, val);                                                       \
+                    }                                                                                  \
+                }                                                                                      \
+    } while (0)
+
+static double add_d(double a, double b) { return a + b; }
+static float add_f(float a, float b) { return a + b; }
+
+int orc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* st, const stc_scatter_op* op,
+                const stc_bc* bc) {
+    if (!src || !dst || !st || !op || !bc || src->ndims != 2 || dst->ndims != 2 || st->ndims != 2)
+        return STC_ERR_UNSUPPORTED;
+    if (src->dtype != dst->dtype || (src->dtype != STC_F64 && src->dtype != STC_F32)) return STC_ERR_UNSUPPORTED;
+    if (op->value == STC_SCATTER_WEIGHTED && !st->weights) return STC_ERR_KERNEL_LENGTH;
+    if (bc->boundary == STC_USE && bc->padding == STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
+    int rc = orc_update_boundary(src, st->radius, bc);
+    if (rc) return rc;
+    view_t v;
+    rc = make_view(src, st->radius, bc->padding, &v);
+    if (rc) return rc;
+    const int64_t ny = v.n[0], nx = v.n[1];
+    if (dst->size[0] != ny || dst->size[1] != nx) return STC_ERR_SIZE_MISMATCH;
+    const int64_t stride = 2 * (int64_t)st->radius + 1;
+    if (src->dtype == STC_F64) ORC_SCATTER_BODY(double, add_d, jl_max, jl_min);
+    else ORC_SCATTER_BODY(float, add_f, jl_maxf, jl_minf);
+    return STC_OK;
+}

@@ -12,8 +12,9 @@ from ._abi import ArgumentError
 from .batch import Batch
 from .boundary import Conditional, Halo, Reflect, Remove, Use, Wrap
 from .gather import gatherstencil, gatherstencil_, mapstencil, mapstencil_, mass, update_boundary_
-from .ops import Diffusion, LifeRule, kernelproduct, life, maximum, mean, minimum
+from .ops import Diffusion, LifeRule, Scaled, Terms, center, kernelproduct, life, maximum, mean, minimum, scaled, value
 from .ops import sum  # noqa: A004
+from .scatter import ScatterConst, scatter_center, scatter_weighted, scatterstencil_
 from .serve import Server
 from .stencil import (AngledCross, Annulus, BackSlash, Cardinal, Circle, Cross, Diamond, ForwardSlash, Horizontal,
                       Kernel, Moore, NamedStencil, Ordinal, Positional, Rectangle, Stencil, Vertical, VonNeumann,
@@ -24,7 +25,9 @@ __all__ = [
     "AbstractStencilArray", "StencilArray", "SwitchingStencilArray", "switch", "colmajor_empty", "colmajor_like",
     "colmajor_zeros", "to_device", "to_host", "ArgumentError", "Conditional", "Halo", "Reflect", "Remove", "Use",
     "Wrap", "gatherstencil", "gatherstencil_", "mapstencil", "mapstencil_", "mass", "update_boundary_",
-    "Diffusion", "LifeRule", "kernelproduct", "life", "maximum", "mean", "minimum", "sum", "AngledCross",
+    "Diffusion", "LifeRule", "kernelproduct", "life", "maximum", "mean", "minimum", "sum", "Terms", "Scaled",
+    "scaled", "center", "value", "scatterstencil_", "ScatterConst", "scatter_center", "scatter_weighted",
+    "AngledCross",
     "Annulus", "BackSlash", "Cardinal", "Circle", "Cross", "Diamond", "ForwardSlash", "Horizontal", "Kernel",
     "Moore", "NamedStencil", "Ordinal", "Positional", "Rectangle", "Stencil", "Vertical", "VonNeumann", "Window",
 ]

@@ -81,6 +81,16 @@ class BcDesc(C.Structure):
                 ("padval_int", C.c_int64)]
 
 
+# stc_term_kind
+TERM_CENTER, TERM_SUM, TERM_MEAN, TERM_KDOT, TERM_VALUE = range(5)
+MAX_TERMS = 4
+
+
+class TermDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("scaled", C.c_int32), ("alpha", C.c_double),
+                ("grid", C.POINTER(Grid)), ("stencil", C.POINTER(StencilDesc)), ("bc", C.POINTER(BcDesc))]
+
+
 class JobDesc(C.Structure):
     _fields_ = [("grid", Grid), ("stencil", StencilDesc), ("op", OpDesc), ("bc", BcDesc),
                 ("nsteps", C.c_int64)]

@@ -15,7 +15,7 @@ from . import _lib
 from .array import (AbstractStencilArray, StencilArray, SwitchingStencilArray, _is_torch, colmajor_empty,
                     to_device)
 from .boundary import Conditional, Halo
-from .ops import as_reduction
+from .ops import Terms, as_reduction
 from .stencil import Stencil
 
 
@@ -86,13 +86,52 @@ def _new_dest(like, shape, code):
     return np.empty(shape, dtype=A.NP_DTYPE[code], order="F")
 
 
+def _term_item(a):
+    """A multi-array argument as the oracle-style item: (parent, stencil, boundary, padding) for a
+    StencilArray (a SwitchingStencilArray contributes its current source), else the plain array."""
+    if isinstance(a, SwitchingStencilArray):
+        return (a.source, a.stencil, a.boundary, a.padding)
+    if isinstance(a, AbstractStencilArray):
+        return (a.parent, a.stencil, a.boundary, a.padding)
+    return a
+
+
+def _run_terms(f: Terms, dest, args, dst_padded: bool):
+    """dest[I] = f(args at I) through stc_map_terms (src/gatherstencil.jl:89-113)."""
+    lib = _lib.load()
+    items = [_term_item(a) for a in args]
+    arrays = [it[0] if isinstance(it, tuple) else it for it in items]
+    halo_idx = [i for i, it in enumerate(items) if isinstance(it, tuple) and isinstance(it[3], Halo)]
+    stage = _Staged(*arrays, dest, writeback=tuple(halo_idx) + (len(arrays),))
+    dev = stage.dev
+    for d in dev:
+        _require_device(d)
+    ditems = [(dv,) + it[1:] if isinstance(it, tuple) else dv for it, dv in zip(items, dev[:-1])]
+    code = _code_of(dev[0])
+    descs, keep = f.lower(ditems, code, _grid)
+    gd = _grid(dev[-1])
+    arr = (A.TermDesc * len(descs))(*descs)
+    _lib.check(lib.stc_map_terms(arr, len(descs), C.byref(gd), int(dst_padded), _lib.current_stream_handle(), 0),
+               "mapstencil")
+    del keep
+    stage.done()
+    return dest
+
+
 def mapstencil(f, *args, boundary=None, padding=None):
-    """mapstencil(f, A::StencilArray) or mapstencil(f, stencil, A; boundary, padding).
+    """mapstencil(f, A::StencilArray, args...) or mapstencil(f, stencil, A; boundary, padding).
 
     Returns a new array of size(A) holding f applied to the stencil around every cell
-    (src/gatherstencil.jl:14-39).  Extra array arguments (the reference's multi-array form) are not
-    registered reductions and raise NotImplementedError.
+    (src/gatherstencil.jl:14-39).  With extra array arguments (the reference's multi-array form) f
+    must be a registered `Terms` sum, one term per argument.
     """
+    if isinstance(f, Terms):
+        sa = args[0]
+        if not isinstance(sa, AbstractStencilArray):
+            raise TypeError("mapstencil needs a StencilArray first argument")
+        dest = _new_dest(sa.parent if not isinstance(sa, SwitchingStencilArray) else sa.source, sa.shape,
+                         _code_of(sa.parent if not isinstance(sa, SwitchingStencilArray) else sa.source))
+        return _run_terms(f, dest, args, dst_padded=False)
     red = as_reduction(f)
     if args and isinstance(args[0], Stencil):
         hood, arr = args[0], args[1]
@@ -111,13 +150,29 @@ def mapstencil(f, *args, boundary=None, padding=None):
     return _run_map(red, dest, sa, dst_padded=False)
 
 
-def mapstencil_(f, dest, source=None, *, steps: int = 1):
+def mapstencil_(f, dest, source=None, *more, steps: int = 1):
     """mapstencil!(f, dest, source) or mapstencil!(f, A::SwitchingStencilArray).
 
     For a SwitchingStencilArray, runs `steps` maps (default 1) and returns the switched array, as
     `A = mapstencil!(f, A)` repeated `steps` times would (src/gatherstencil.jl:77-83).
     """
+    if isinstance(f, Terms):
+        if isinstance(dest, SwitchingStencilArray):
+            # gatherstencil!(f, A::SwitchingStencilArray, B, args...): A's source is the first argument,
+            # its dest parent receives the result, then switch(A) (src/gatherstencil.jl:84-88)
+            args = (dest,) + ((source,) if source is not None else ()) + tuple(more)
+            _run_terms(f, dest.dest, args, dst_padded=isinstance(dest.padding, Halo))
+            return dest.switch()
+        sa = source
+        if not isinstance(sa, AbstractStencilArray):
+            raise TypeError("mapstencil_(f, dest, source, args...) needs a StencilArray source")
+        padded = tuple(dest.shape) != tuple(sa.shape)
+        if padded and not (isinstance(sa.padding, Halo) and tuple(dest.shape) == tuple(sa.parent.shape)):
+            raise A.ArgumentError(f"Source array sizes must match. Found: {tuple(sa.shape)} and {tuple(dest.shape)}")
+        return _run_terms(f, dest, (sa,) + tuple(more), dst_padded=padded)
     red = as_reduction(f)
+    if more:
+        raise NotImplementedError("extra array arguments need a registered Terms f")
     if isinstance(dest, SwitchingStencilArray):
         return _run_steps(red, dest, int(steps))
     if not isinstance(source, AbstractStencilArray):
