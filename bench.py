@@ -330,7 +330,7 @@ def run_gpu(args):
     return 0
 
 
-# ------------------------------------------------------------------ other BASELINE configurations
+# ------------------------------------------------------------------ the other benchmark workloads
 def _timed_steps(fn, steps, warmup, flush):
     """Device time of `steps` calls of fn(), L2 flushed (outside the timing) before each."""
     import torch
@@ -366,7 +366,7 @@ def _peaks():
 
 
 def run_mean_blur(args):
-    """Config 1: mapstencil(mean, StencilArray(rand(1000,1000), Window(1))), Float64, Remove(0.0),
+    """Mean blur: mapstencil(mean, StencilArray(rand(1000,1000), Window(1))), Float64, Remove(0.0),
     Conditional, one map per step; device time per map with L2 flushed before each."""
     import torch
     entry.build()
@@ -408,7 +408,7 @@ def _gauss_weights(st):
 
 
 def run_gauss(args):
-    """Config 3a: Kernel(Window(3)) normalised Gaussian (sigma 1.5) on 8192^2 Float32 U[0,1), Remove(0);
+    """7x7 Gaussian filter: Kernel(Window(3)) normalised Gaussian (sigma 1.5) on 8192^2 Float32 U[0,1), Remove(0);
     FP32 and BF16 storage; max relative error against the FP64 oracle (over the whole grid)."""
     import torch
     entry.build()
@@ -447,7 +447,7 @@ def run_gauss(args):
 
 
 def run_diffusion(args):
-    """Config 3b: VonNeumann(1,3) explicit diffusion c + 0.1 (sum - 6c) on 512^3 U[0,1), Wrap, 200 steps,
+    """3D diffusion: VonNeumann(1,3) explicit diffusion c + 0.1 (sum - 6c) on 512^3 U[0,1), Wrap, 200 steps,
     FP32 and BF16 storage; FP64 total-mass drift on the GPU (K4); max relative error vs the FP64
     oracle measured on a 96^3 grid run the same 200 steps."""
     import torch
@@ -514,7 +514,7 @@ def _batched_jobs(st, rng, n=256):
 
 
 def run_batched(args):
-    """Config 4: 256 Float32 grids, side log-uniform [64, 2048], stencil from {Window(1) mean, Circle(3) mean,
+    """Batched uneven grids: 256 Float32 grids, side log-uniform [64, 2048], stencil from {Window(1) mean, Circle(3) mean,
     Cross(2) sum, 5x5 N(0,1) kernel}, 1-50 steps, Remove or Wrap: one graph-captured persistent launch
     (autotuned) against 256 plain synchronising mapstencil! loops."""
     import torch
@@ -542,7 +542,7 @@ def run_batched(args):
     seq.plan(autotune=False)
     ts = _timed_steps(seq.run_sequential, max(2, args.steps // 3), 1, flush)
     tb_s, ts_s = tb / args.steps, ts / max(2, args.steps // 3)
-    line = {"workload": "256 uneven Float32 grids, config-4 mix", "metric": METRIC, "unit": UNIT,
+    line = {"workload": "256 uneven Float32 grids (Window(1) mean, Circle(3) mean, Cross(2) sum, 5x5 kernel mix)", "metric": METRIC, "unit": UNIT,
             "value": cells / tb_s / 1e9, "ms_per_batch": 1e3 * tb_s, "plain_ms": 1e3 * ts_s,
             "plain_gcell_s": cells / ts_s / 1e9, "speedup_vs_plain": ts_s / tb_s, "cell_steps": cells,
             "plan_and_autotune_s": plan_s}
@@ -550,8 +550,8 @@ def run_batched(args):
 
 
 def run_serving(args):
-    """Config 5: Poisson arrivals at several rates; jobs {side log-uniform [128, 4096], Float32 / BF16 /
-    UInt8, config-4 stencils or Moore(1) Life, steps U{1..200}}; continuous batching against the same
+    """Serving stream: Poisson arrivals at several rates; jobs {side log-uniform [128, 4096], Float32 / BF16 /
+    UInt8, the batched-workload stencils or Moore(1) Life, steps U{1..200}}; continuous batching against the same
     arrivals served one at a time by plain calls (host->device, mapstencil! loop, device->host)."""
     import math
     import torch
@@ -629,7 +629,7 @@ def run_serving(args):
                                  "p99_ms": 1e3 * float(np.percentile(plat, 99)), "makespan_s": fin},
             "jobs": njobs, "cell_steps": cells}
     best = max(out.values(), key=lambda v: v["served"]["gcell_s"])
-    line = {"workload": "serving stream, Poisson arrivals, config-5 job mix", "metric": METRIC, "unit": UNIT,
+    line = {"workload": "serving stream, Poisson arrivals, mixed jobs (sides 128-4096, f32/bf16/u8, 1-200 steps)", "metric": METRIC, "unit": UNIT,
             "value": best["served"]["gcell_s"], "rates": out, "steps_per_tick": args.serve_tick}
     print(json.dumps(line), flush=True)
 
@@ -647,7 +647,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="life", choices=["life"] + sorted(WORKLOADS),
-                    help="life (the headline line) or one of the other BASELINE configurations")
+                    help="life (the headline line) or one of the other benchmark workloads")
     ap.add_argument("--side", type=int, default=0, help="diffusion: grid side (default 512)")
     ap.add_argument("--serve-jobs", type=int, default=120)
     ap.add_argument("--serve-rates", default="100,300,1000,3000,5000")

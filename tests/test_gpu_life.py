@@ -46,7 +46,7 @@ def _logical(t, pad, st):
 
 
 def test_life_4096_every_100_steps(cuda, st, orc, abi):
-    """Config 2: 4096x4096 UInt8, density 0.3 from seed 2, Wrap, Halo padding, 1000 generations,
+    """The Life benchmark grid: 4096x4096 UInt8, density 0.3 from seed 2, Wrap, Halo padding, 1000 generations,
     compared with the oracle after every 100."""
     rng = np.random.Generator(np.random.PCG64(2))
     a = np.asfortranarray((rng.random((4096, 4096)) < 0.3).astype(np.uint8))

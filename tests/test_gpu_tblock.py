@@ -75,7 +75,7 @@ def test_other_blocked_shapes_and_halo(cuda, st, orc, abi, monkeypatch, shape_na
 
 
 def test_diffusion_512_cubed_mass_conserved(cuda, st):
-    """Config 3b size: 512^3 Float32, Wrap, 200 steps through the default multi-step path; the FP64
+    """The diffusion benchmark size: 512^3 Float32, Wrap, 200 steps through the default multi-step path; the FP64
     total of the grid (a conserved quantity for this scheme) drifts only by rounding."""
     import torch
     rng = np.random.Generator(np.random.PCG64(4))
