@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "dispatch.h"
@@ -46,6 +47,7 @@ struct TBParams {
     int32_t ntx, nty, nzc;
     uint32_t plane_bytes;            // PX*PY*sizeof(T) rounded to 128
     int32_t fixup;                   // edge tiles need patching after TMA
+    int32_t aligned;                 // dst rows allow 4-element vector stores (vector variant)
     int32_t* status;
     // op parameters (the fields the op structs read)
     int32_t L;
@@ -108,7 +110,76 @@ __device__ __forceinline__ T tb_fold(const T* lo, const T* mid, const T* hi, int
     return Op::finish(acc, mid[0], p);
 }
 
+// ---- vector columns: one work item = 4 adjacent cells of a plane row ----
+// Which rows of the three planes the generated table reads, and whether it reads their x - 1 / x + 1,
+// as compile-time bit masks over the 3 x 3 (z, y) rows (scalars, so device code never reads the table
+// object itself at run time).
+template <class Sh> struct TbUse {
+    static constexpr unsigned mask(int dx, bool any_x) {
+        unsigned m = 0;
+        for (int k = 0; k < Sh::L; ++k)
+            if (any_x || Sh::table.o[k].x == dx) m |= 1u << ((Sh::table.o[k].z + 1) * 3 + (Sh::table.o[k].y + 1));
+        return m;
+    }
+    static constexpr unsigned kRows = mask(0, true), kXm = mask(-1, false), kXp = mask(1, false);
+};
+
+template <class V, class T> __device__ __forceinline__ V tb_widen(T v) {
+    if constexpr (std::is_same_v<V, T>) return v;
+    else return __bfloat162float(v);
+}
+
+// The four cells at shared-memory offset `off` (a multiple of 4) of level t from the level t-1 planes
+// (lo, mid, hi): each row the table reads is one aligned 4-wide load, plus its left / right neighbour
+// when the table reads x - 1 / x + 1; every cell then folds its neighbours in table order (the same
+// op structs, widened as in the single-map vector kernel), so results equal the one-cell fold.
 template <class T, class Op, class Sh>
+__device__ __forceinline__ void tb_cells4(const T* lo, const T* mid, const T* hi, int off, int PX, const TBParams& p,
+                                          T* res) {
+    using OpV = typename Widen<Op>::type;
+    using V = std::conditional_t<Widen<Op>::kWide, float, T>;
+    using U = TbUse<Sh>;
+    constexpr auto Tb = Sh::table;
+    V w[3][3][6];
+#pragma unroll
+    for (int zz = 0; zz < 3; ++zz)
+#pragma unroll
+        for (int yy = 0; yy < 3; ++yy) {
+            const unsigned bit = 1u << (zz * 3 + yy);
+            if (!(U::kRows & bit)) continue;
+            const T* pl = (zz == 0 ? lo : (zz == 1 ? mid : hi)) + off + (yy - 1) * PX;
+            ld_row_vec<T, V, 4>(pl, &w[zz][yy][1]);
+            if (U::kXm & bit) w[zz][yy][0] = tb_widen<V>(pl[-1]);
+            if (U::kXp & bit) w[zz][yy][5] = tb_widen<V>(pl[4]);
+        }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        typename OpV::A acc;
+        if constexpr (OpV::kZeroInit) acc = OpV::first(V(0), 0);
+#pragma unroll
+        for (int k = 0; k < Sh::L; ++k) {
+            const V v = w[Tb.o[k].z + 1][Tb.o[k].y + 1][c + Tb.o[k].x + 1];
+            if (!OpV::kZeroInit && k == 0) acc = OpV::first(v, 0);
+            else acc = OpV::step(acc, v, k, p);
+        }
+        if (!(U::kRows & (1u << 4))) w[1][1][c + 1] = tb_widen<V>(mid[off + c]);   // the centre, if the table skipped it
+        res[c] = OpV::finish(acc, w[1][1][c + 1], p);
+    }
+}
+
+template <class T> __device__ __forceinline__ void sts4(T* d, const T* v) {
+    if constexpr (sizeof(T) == 4) {
+        uint4 u;
+        memcpy(&u, v, 16);
+        *(uint4*)d = u;
+    } else {
+        uint2 u;
+        memcpy(&u, v, 8);
+        *(uint2*)d = u;
+    }
+}
+
+template <class T, class Op, class Sh, bool VEC>
 __global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant__ TBParams p) {
     extern __shared__ __align__(128) unsigned char tsm[];
     const int k = p.k, PX = p.PX, PY = p.PY;
@@ -217,6 +288,48 @@ __global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant_
             const int64_t z = plane_z(j);
             const int xa = p.padl - k + t, xb = p.padl + p.TX + k - t;
             const int ya = t, yb = p.TY + 2 * k - t;
+            if constexpr (VEC) {
+                // work items: 4-cell groups from the multiple of 4 at or below xa (the extra cells left
+                // of the valid region are computed and never read); padl and PX leave a spare column
+                // group on each side, so the x - 1 / x + 1 reads stay inside the plane.
+                const bool last = t == k;
+                const int gx0 = last ? p.padl : (xa & ~3);
+                const int ngx = last ? (p.TX >> 2) : ((xb - gx0 + 3) >> 2);
+                const int row0 = last ? k : ya, nrows = last ? p.TY : yb - ya;
+                const int nit = ngx * nrows;
+                const float inv = 1.0f / (float)ngx;
+                const bool zout = z < 0 || z >= p.n[2];
+                T* out = last ? nullptr : planeL(t, j);
+                T* dst = (T*)p.dst;
+                const int nvx = (int)min((int64_t)p.TX, p.n[0] - x0), nvy = (int)min((int64_t)p.TY, p.n[1] - y0);
+                for (int it = threadIdx.x; it < nit; it += blockDim.x) {
+                    const int r = __float2int_rz(((float)it + 0.5f) * inv);   // it / ngx, exact (ngx <= 64)
+                    const int g = it - r * ngx;
+                    const int by = row0 + r, bx = gx0 + 4 * g;
+                    const int off = by * PX + bx;
+                    T res[4];
+                    tb_cells4<T, Op, Sh>(lo, mid, hi, off, PX, p, res);
+                    if (!last) {
+                        if (!wrapb) {
+                            // Remove: cells outside the grid hold padval at every level
+                            const int64_t gy = y0 - k + by, gxa = x0 - p.padl + bx;
+                            const bool row_out = zout || gy < 0 || gy >= p.n[1];
+                            if (row_out || gxa < 0 || gxa + 3 >= p.n[0]) {
+#pragma unroll
+                                for (int c = 0; c < 4; ++c)
+                                    if (row_out || gxa + c < 0 || gxa + c >= p.n[0]) res[c] = pv;
+                            }
+                        }
+                        sts4<T>(out + off, res);
+                    } else {
+                        const int ly = r, lx = 4 * g;
+                        if (ly < nvy && lx < nvx)
+                            st_row_vec<T, 4>(dst + p.dst_org + z * p.dstr[2] + (y0 + ly) * p.dstr[1] + x0 + lx, res,
+                                             p.aligned != 0, nvx - lx);
+                    }
+                }
+                continue;
+            }
             if (t < k) {
                 T* out = planeL(t, j);
                 const bool zout = z < 0 || z >= p.n[2];
@@ -270,16 +383,23 @@ static TbEncodeFn tb_encoder() {
 
 using TbLaunch = cudaError_t (*)(const TBParams&, int grid, size_t smem, cudaStream_t);
 
-template <class T, class Op, class Sh>
-static cudaError_t tb_launch(const TBParams& p, int grid, size_t smem, cudaStream_t s) {
+template <class T, class Op, class Sh, bool VEC>
+static cudaError_t tb_launch_v(const TBParams& p, int grid, size_t smem, cudaStream_t s) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [&] {
-        attr = cudaFuncSetAttribute(tb3d_kernel<T, Op, Sh>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr = cudaFuncSetAttribute(tb3d_kernel<T, Op, Sh, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     });
     if (attr != cudaSuccess) return attr;
-    tb3d_kernel<T, Op, Sh><<<grid, kTbThreads, smem, s>>>(p);
+    tb3d_kernel<T, Op, Sh, VEC><<<grid, kTbThreads, smem, s>>>(p);
     return cudaGetLastError();
+}
+
+// the vector variant for Conditional grids (tile columns on 16-byte boundaries), else one cell per lane
+template <class T, class Op, class Sh>
+static cudaError_t tb_launch(const TBParams& p, int grid, size_t smem, cudaStream_t s) {
+    return (p.hx[0] % 4 == 0 && p.padl % 4 == 0) ? tb_launch_v<T, Op, Sh, true>(p, grid, smem, s)
+                                                  : tb_launch_v<T, Op, Sh, false>(p, grid, smem, s);
 }
 
 struct TbEntry { int dt, opv, shape; TbLaunch fn; };
@@ -353,11 +473,17 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     // launches: the first nsteps-1 steps, split so that state nsteps-1 ends in the parent the reference
     // leaves it in (a after an odd number of steps... i.e. m launches with m = nsteps-1 (mod 2))
     // deepest k <= 4 whose rings keep two CTAs per SM (<= 110 KB of shared memory)
+    // Box geometry: the vector variant (Conditional grids, hx = 0) keeps the tile's first column at a
+    // multiple of 4 and 16 bytes (padl = 8 >= k + 4) with room for its aligned 4-cell groups and their
+    // x +- 1 reads on both sides; the one-cell variant needs only k columns of halo.
+    const bool vec = p.hx[0] % 4 == 0;
+    auto padl_for = [&](int kk) { return vec ? 8 : kk + (((p.hx[0] - kk) % V) + V) % V; };
+    auto px_for = [&](int kk, int padl) { return (padl + p.TX + kk + (vec ? 7 : 0) + V - 1) / V * V; };
     int kmax = 4;
     {
         while (kmax > 1) {
-            const int padl = kmax + (((p.hx[0] - kmax) % V) + V) % V;
-            const int PX = (padl + p.TX + kmax + V - 1) / V * V;
+            const int padl = padl_for(kmax);
+            const int PX = px_for(kmax, padl);
             const size_t pbytes = ((size_t)PX * (p.TY + 2 * kmax) * es + 127) / 128 * 128;
             if ((size_t)(kTbRing0 + kTbRingL * (kmax - 1)) * pbytes <= 110 * 1024) break;
             --kmax;
@@ -375,8 +501,8 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         const stc_grid* sg = par[cur];
         const stc_grid* dg = par[1 - cur];
         p.k = kk;
-        p.padl = kk + (int)(((p.hx[0] - kk) % V + V) % V);
-        p.PX = (p.padl + p.TX + kk + V - 1) / V * V;
+        p.padl = padl_for(kk);
+        p.PX = px_for(kk, p.padl);
         p.PY = p.TY + 2 * kk;
         p.plane_bytes = (uint32_t)(((size_t)p.PX * p.PY * es + 127) / 128 * 128);
         const size_t smem = (size_t)(kTbRing0 + kTbRingL * (kk - 1)) * p.plane_bytes + 8 * kTbRing0;
@@ -385,6 +511,11 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         p.dst = dg->data;
         p.src_org = halo ? 1 + sg->stride[1] + sg->stride[2] : 0;
         p.dst_org = halo ? 1 + dg->stride[1] + dg->stride[2] : 0;
+        {
+            const int VA = std::min(16, 4 * es);
+            p.aligned = ((uintptr_t)dg->data + (uintptr_t)p.dst_org * es) % VA == 0 && (dg->stride[1] * es) % VA == 0 &&
+                        (dg->stride[2] * es) % VA == 0;
+        }
         for (int d = 0; d < 3; ++d) { p.sst[d] = sg->stride[d]; p.dstr[d] = dg->stride[d]; }
         cuuint64_t gdim[3] = {(cuuint64_t)sg->size[0], (cuuint64_t)sg->size[1], (cuuint64_t)sg->size[2]};
         cuuint64_t gstr[2] = {(cuuint64_t)(sg->stride[1] * es), (cuuint64_t)(sg->stride[2] * es)};
