@@ -60,7 +60,12 @@ class _Staged:
                 h[...] = d.cpu().numpy()
 
 
-def _run_map(red, dest, src: AbstractStencilArray, dst_padded: bool):
+def _flags(sync: bool, staged) -> int:
+    """STC_ASYNC only when nothing has to be copied back to host memory afterwards."""
+    return 0 if (sync or any(h is not None and not _is_torch(h) for h in staged.host)) else 1
+
+
+def _run_map(red, dest, src: AbstractStencilArray, dst_padded: bool, sync: bool = True):
     lib = _lib.load()
     st = A.LoweredStencil(src.stencil)
     op = A.lower_op(red)
@@ -73,7 +78,7 @@ def _run_map(red, dest, src: AbstractStencilArray, dst_padded: bool):
     gs, gd = _grid(sp), _grid(dp)
     stream = _lib.current_stream_handle()
     _lib.check(lib.stc_map(C.byref(gs), C.byref(gd), int(dst_padded), C.byref(st.desc), C.byref(op), C.byref(bc),
-                           stream, 0), "mapstencil")
+                           stream, _flags(sync, stage)), "mapstencil")
     stage.done()
     return dest
 
@@ -150,11 +155,14 @@ def mapstencil(f, *args, boundary=None, padding=None):
     return _run_map(red, dest, sa, dst_padded=False)
 
 
-def mapstencil_(f, dest, source=None, *more, steps: int = 1):
+def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
     """mapstencil!(f, dest, source) or mapstencil!(f, A::SwitchingStencilArray).
 
     For a SwitchingStencilArray, runs `steps` maps (default 1) and returns the switched array, as
-    `A = mapstencil!(f, A)` repeated `steps` times would (src/gatherstencil.jl:77-83).
+    `A = mapstencil!(f, A)` repeated `steps` times would (src/gatherstencil.jl:77-83).  Like the
+    reference (KernelAbstractions.synchronize, src/gatherstencil.jl:100) the call waits for the GPU;
+    `sync=False` returns once the work is queued on the current CUDA stream (errors a kernel reports
+    then surface at the next synchronising call), so consecutive calls keep the GPU busy.
     """
     if isinstance(f, Terms):
         if isinstance(dest, SwitchingStencilArray):
@@ -174,7 +182,7 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1):
     if more:
         raise NotImplementedError("extra array arguments need a registered Terms f")
     if isinstance(dest, SwitchingStencilArray):
-        return _run_steps(red, dest, int(steps))
+        return _run_steps(red, dest, int(steps), sync)
     if not isinstance(source, AbstractStencilArray):
         raise TypeError("mapstencil_(f, dest, source) needs a StencilArray source")
     if tuple(dest.shape) != tuple(source.shape):
@@ -182,11 +190,11 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1):
         if not padded:
             raise A.ArgumentError(f"Source array sizes must match. Found: {tuple(source.shape)} and "
                                   f"{tuple(dest.shape)}")
-        return _run_map(red, dest, source, dst_padded=True)
-    return _run_map(red, dest, source, dst_padded=False)
+        return _run_map(red, dest, source, dst_padded=True, sync=sync)
+    return _run_map(red, dest, source, dst_padded=False, sync=sync)
 
 
-def _run_steps(red, S: SwitchingStencilArray, steps: int) -> SwitchingStencilArray:
+def _run_steps(red, S: SwitchingStencilArray, steps: int, sync: bool = True) -> SwitchingStencilArray:
     if steps < 0:
         raise ValueError("steps must be >= 0")
     lib = _lib.load()
@@ -201,7 +209,7 @@ def _run_steps(red, S: SwitchingStencilArray, steps: int) -> SwitchingStencilArr
     out = C.c_int32(0)
     stream = _lib.current_stream_handle()
     _lib.check(lib.stc_map_steps(C.byref(ga), C.byref(gb), C.byref(st.desc), C.byref(op), C.byref(bc), steps,
-                                 C.byref(out), stream, 0), "mapstencil!")
+                                 C.byref(out), stream, _flags(sync, stage)), "mapstencil!")
     stage.done()
     if out.value:
         return S.switch()

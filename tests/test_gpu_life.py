@@ -133,3 +133,20 @@ def test_life_persistent_depths(cuda, st, orc, abi, monkeypatch, depth, bname):
         assert np.array_equal(_logical(S2.source, st.Conditional(), st), res), (depth, steps)
         if steps > 1:
             assert np.array_equal(_logical(S2.dest, st.Conditional(), st), prev), (depth, steps)
+
+
+def test_queued_calls_equal_waiting_calls(cuda, st):
+    """mapstencil_(..., sync=False) only skips the wait: three queued 100-generation calls give the state
+    one waiting 300-generation call gives."""
+    import torch
+    rng = np.random.default_rng(12)
+    g = np.asfortranarray((rng.random((256, 192)) < 0.3).astype(np.uint8))
+    S1 = st.SwitchingStencilArray(st.to_device(g), st.Moore(1), st.Wrap(), st.Halo("out"))
+    for _ in range(3):
+        S1 = st.mapstencil_(st.life, S1, steps=100, sync=False)
+    torch.cuda.synchronize()
+    S2 = st.SwitchingStencilArray(st.to_device(g), st.Moore(1), st.Wrap(), st.Halo("out"))
+    S2 = st.mapstencil_(st.life, S2, steps=300)
+    a = st.to_host(S1.source)[1:-1, 1:-1]
+    b = st.to_host(S2.source)[1:-1, 1:-1]
+    assert np.array_equal(a, b)
