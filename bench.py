@@ -656,7 +656,7 @@ def main():
     ap.add_argument("--side", type=int, default=0, help="diffusion: grid side (default 512)")
     ap.add_argument("--serve-jobs", type=int, default=120)
     ap.add_argument("--serve-rates", default="100,300,1000,3000,5000")
-    ap.add_argument("--serve-tick", type=int, default=16)
+    ap.add_argument("--serve-tick", type=int, default=32)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

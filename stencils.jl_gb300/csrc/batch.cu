@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -403,7 +404,16 @@ bool batch_supported(int dtype, int opv) {
 namespace stc {
 
 
-constexpr size_t kResidentSmem = 96 * 1024;   // a grid held twice below this runs resident
+// a grid held twice below this runs resident (STC_BATCH_RESIDENT_KB overrides, a tuning knob); the
+// launch's shared memory per CTA is the largest any job needs, so this also sets CTAs per SM
+static size_t resident_smem_cap() {
+    static const size_t cap = [] {
+        const char* e = getenv("STC_BATCH_RESIDENT_KB");
+        const long v = e ? atol(e) : 0;
+        return (size_t)((v >= 8 && v <= 200) ? v : 96) * 1024;
+    }();
+    return cap;
+}
 constexpr size_t kTiledSmemCap = 200 * 1024;
 
 static size_t tiled_smem(const BatchSpec& s, const Geometry& g) {
@@ -601,7 +611,7 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
         b->planned_cell_steps += (double)j.n0 * j.n1 * s.nsteps;
         if (s.nsteps == 0) { j.rounds = 0; continue; }
         const bool forced = s.force_tw > 0;
-        if (!forced && resident_smem(s) <= kResidentSmem) {
+        if (!forced && resident_smem(s) <= resident_smem_cap()) {
             j.resident = 1;
             j.tw = j.n0; j.th = j.n1; j.k = j.nsteps;
             j.ntx = j.nty = j.tiles = 1;
