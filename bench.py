@@ -639,7 +639,86 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+def run_terms(args):
+    """Maps over two arrays: mapstencil(f, A, B) with f = center(hood_A) + 0.1 * sum(neighbors(hood_B)) (the
+    reference's diffusion-with-source form), Float64 4096x4096, Moore(1), Remove(0) on both; bit-exact
+    against the oracle on the full grid; CPU baseline = the oracle on all host cores."""
+    import torch
+    entry.build()
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    from oracle import oracle as orc
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    rng = np.random.Generator(np.random.PCG64(7))
+    n = 4096
+    a = np.asfortranarray(rng.random((n, n)))
+    b = np.asfortranarray(rng.random((n, n)))
+    f = st.Terms(st.center, st.scaled(0.1, st.sum))
+    sa = st.StencilArray(st.to_device(a), st.Moore(1), st.Remove(0.0))
+    sb = st.StencilArray(st.to_device(b), st.Moore(1), st.Remove(0.0))
+    out = st.mapstencil(f, sa, sb)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    _lib.profile_enable(True)
+    t = _timed_steps(lambda: st.mapstencil_(f, out, sa, sb, sync=False), args.steps, args.warmup, flush)
+    prof = _lib.profile_report()
+    _lib.profile_enable(False)
+    items = [(a.copy(order="F"), st.Moore(1), st.Remove(0.0), st.Conditional()),
+             (b.copy(order="F"), st.Moore(1), st.Remove(0.0), st.Conditional())]
+    thr = orc.max_threads()
+    t0 = time.perf_counter()
+    want = orc.map_terms(f, items, A.F64, nthreads=thr)
+    cpu_s = time.perf_counter() - t0
+    exact = st.to_host(out).tobytes(order="F") == want.tobytes(order="F")
+    line = {"workload": "two-array map center(A) + 0.1*sum(neighbors(B)), Float64 4096x4096, Moore(1), Remove(0)",
+            "metric": METRIC, "unit": UNIT, "value": args.steps * n * n / t / 1e9, "us_per_map": 1e6 * t / args.steps,
+            "bit_exact_vs_oracle": bool(exact), "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"]),
+            "cpu_baseline": {"value": n * n / cpu_s / 1e9, "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": "one full map"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_scatter(args):
+    """scatterstencil!(f, +, dest, source): every cell scatters 0.1 to its Moore(1) neighbours, Float64
+    4096x4096, Remove(0), dest accumulated in place; bit-exact against the oracle (the reference's pass
+    schedule on one thread), which is also the CPU baseline."""
+    import operator
+    import torch
+    entry.build()
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    from oracle import oracle as orc
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    rng = np.random.Generator(np.random.PCG64(8))
+    n = 4096
+    src = np.asfortranarray(rng.random((n, n)))
+    sa = st.StencilArray(st.to_device(src), st.Moore(1), st.Remove(0.0))
+    dest = st.to_device(np.zeros((n, n), order="F"))
+    f = st.scatter_center
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    _lib.profile_enable(True)
+    t = _timed_steps(lambda: st.scatterstencil_(f, operator.add, dest, sa), args.steps, args.warmup, flush)
+    prof = _lib.profile_report()
+    _lib.profile_enable(False)
+    calls = args.warmup + args.steps
+    d1 = st.to_device(np.zeros((n, n), order="F"))
+    st.scatterstencil_(f, operator.add, d1, sa)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    want = orc.scatter(f, operator.add, np.zeros((n, n), order="F"), src.copy(order="F"), A.F64, st.Moore(1),
+                       st.Remove(0.0), st.Conditional())
+    cpu_s = time.perf_counter() - t0
+    exact = st.to_host(d1).tobytes(order="F") == want.tobytes(order="F")
+    line = {"workload": "scatterstencil! centre value to Moore(1) neighbours with +, Float64 4096x4096, Remove(0)",
+            "metric": METRIC, "unit": UNIT, "value": args.steps * n * n / t / 1e9, "us_per_call": 1e6 * t / args.steps,
+            "bit_exact_vs_oracle_one_call": bool(exact), "calls_accumulated": calls,
+            "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"]),
+            "cpu_baseline": {"value": n * n / cpu_s / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "one full scatter (the oracle's schedule is sequential)"}}
+    print(json.dumps(line), flush=True)
+
+
 WORKLOADS = {"mean_blur": run_mean_blur, "gauss": run_gauss, "diffusion": run_diffusion, "batched": run_batched,
+             "terms": run_terms, "scatter": run_scatter,
              "serving": run_serving}
 
 

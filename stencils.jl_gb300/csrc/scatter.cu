@@ -7,6 +7,8 @@
 // column, source column, source row, offset).  No atomics, and the result is bit-exact with that order
 // for every combine op, including floating-point +.
 #include <algorithm>
+#include <tuple>
+#include <vector>
 
 #include "common.cuh"
 #include "dispatch.h"
@@ -15,6 +17,7 @@
 namespace stc {
 
 constexpr int kScatterMaxLen = 256;
+constexpr int kScatterPermMax = 2048;   // (2R + 1) * L entries of the interior orders
 
 struct ScatterParams {
     const void* src;
@@ -24,8 +27,14 @@ struct ScatterParams {
     int64_t ny, nx;            // logical size (axis 0, axis 1)
     int32_t L, R, boundary, value, combine;
     double constant;
+    int32_t perm_ok;           // interior cells use perm (else every cell runs the selection loop)
     int8_t off[kScatterMaxLen][2];
     double w[kScatterMaxLen];
+    // For a dest cell far enough from every edge (R, or R + 1 under Reflect) each offset k brings
+    // exactly one contribution, from
+    // (ti - o0, tj - o1); their order depends only on tj mod (2R + 1): perm[(tj mod (2R+1)) * L + i]
+    // is the i-th offset in (pass, source row, offset) order.
+    uint8_t perm[kScatterPermMax];
 };
 
 // Source coordinates u on one axis whose target u + o maps to t (at most 3): Remove/Use only u + o = t;
@@ -67,6 +76,28 @@ __global__ void __launch_bounds__(256) scatter_kernel(const __grid_constant__ Sc
          lin += (int64_t)gridDim.x * blockDim.x) {
         const int64_t ti = lin % p.ny, tj = lin / p.ny;
         T acc = dst[ti + tj * p.dst1];
+        auto combine = [&](T val) {
+            if (p.combine == STC_COMBINE_ADD) acc = sc_add<T>(acc, val);
+            else if (p.combine == STC_COMBINE_MAX) acc = jl_max(acc, val);
+            else acc = jl_min(acc, val);
+        };
+        auto value = [&](int k, int64_t si, int64_t sj) -> T {
+            if (p.value == STC_SCATTER_CONST) return (T)p.constant;
+            const T c = src[p.sorg + si + sj * p.sst1];
+            return p.value == STC_SCATTER_CENTER ? c : sc_mul<T>(c, (T)p.w[k]);
+        };
+        // interior: no source's target is wrapped or reflected onto this cell (Reflect maps the edge
+        // row's x - R onto x + R, so it needs one more cell of margin)
+        const int m = p.R + (p.boundary == STC_REFLECT ? 1 : 0);
+        if (p.perm_ok && ti >= m && ti < p.ny - m && tj >= m && tj < p.nx - m) {
+            const uint8_t* order = p.perm + (tj % stride) * p.L;
+            for (int i = 0; i < p.L; ++i) {
+                const int k = order[i];
+                combine(value(k, ti - p.off[k][0], tj - p.off[k][1]));
+            }
+            dst[ti + tj * p.dst1] = acc;
+            continue;
+        }
         // Visit contributions in increasing (pass, column, row, offset): each round picks the smallest
         // key above the previous one among all candidates (a handful per cell).
         int64_t pk = -1, pj = -1, pi = -1, pkk = -1;
@@ -93,16 +124,7 @@ __global__ void __launch_bounds__(256) scatter_kernel(const __grid_constant__ Sc
                     }
             }
             if (bk == INT64_MAX) break;
-            const int k = (int)bkk;
-            T val;
-            if (p.value == STC_SCATTER_CONST) val = (T)p.constant;
-            else {
-                const T c = src[p.sorg + bi + bj * p.sst1];
-                val = p.value == STC_SCATTER_CENTER ? c : sc_mul<T>(c, (T)p.w[k]);
-            }
-            if (p.combine == STC_COMBINE_ADD) acc = sc_add<T>(acc, val);
-            else if (p.combine == STC_COMBINE_MAX) acc = jl_max(acc, val);
-            else acc = jl_min(acc, val);
+            combine(value((int)bkk, bi, bj));
             pk = bk; pj = bj; pi = bi; pkk = bkk;
         }
         dst[ti + tj * p.dst1] = acc;
@@ -156,6 +178,22 @@ int stc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* st,
         p.off[k][1] = (int8_t)oy;
         if (st->weights) p.w[k] = f32 ? (double)(float)st->weights[k] : st->weights[k];
     }
+    // interior orders: sort the offsets by (pass of the source column, source row, offset) for each
+    // residue of the dest column; offsets are distinct, so the pass separates different columns
+    const int stride = 2 * R + 1;
+    p.perm_ok = stride * st->len <= kScatterPermMax && st->len <= 256;
+    if (p.perm_ok)
+        for (int r = 0; r < stride; ++r) {
+            std::vector<int> ks(st->len);
+            for (int k = 0; k < st->len; ++k) ks[k] = k;
+            auto key = [&](int k) {
+                const int o0 = st->offsets[2 * k], o1 = st->offsets[2 * k + 1];
+                const int pass = ((r - o1) % stride + stride) % stride;
+                return std::make_tuple(pass, -o0, k);   // source row ti - o0 ascending
+            };
+            std::sort(ks.begin(), ks.end(), [&](int x, int y) { return key(x) < key(y); });
+            for (int i = 0; i < st->len; ++i) p.perm[r * st->len + i] = (uint8_t)ks[i];
+        }
     DeviceCtx* ctx = nullptr;
     int rc = device_ctx(&ctx);
     if (rc) return rc;

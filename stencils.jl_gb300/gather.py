@@ -101,7 +101,7 @@ def _term_item(a):
     return a
 
 
-def _run_terms(f: Terms, dest, args, dst_padded: bool):
+def _run_terms(f: Terms, dest, args, dst_padded: bool, sync: bool = True):
     """dest[I] = f(args at I) through stc_map_terms (src/gatherstencil.jl:89-113)."""
     lib = _lib.load()
     items = [_term_item(a) for a in args]
@@ -116,8 +116,8 @@ def _run_terms(f: Terms, dest, args, dst_padded: bool):
     descs, keep = f.lower(ditems, code, _grid)
     gd = _grid(dev[-1])
     arr = (A.TermDesc * len(descs))(*descs)
-    _lib.check(lib.stc_map_terms(arr, len(descs), C.byref(gd), int(dst_padded), _lib.current_stream_handle(), 0),
-               "mapstencil")
+    _lib.check(lib.stc_map_terms(arr, len(descs), C.byref(gd), int(dst_padded), _lib.current_stream_handle(),
+                                 _flags(sync, stage)), "mapstencil")
     del keep
     stage.done()
     return dest
@@ -169,7 +169,7 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
             # gatherstencil!(f, A::SwitchingStencilArray, B, args...): A's source is the first argument,
             # its dest parent receives the result, then switch(A) (src/gatherstencil.jl:84-88)
             args = (dest,) + ((source,) if source is not None else ()) + tuple(more)
-            _run_terms(f, dest.dest, args, dst_padded=isinstance(dest.padding, Halo))
+            _run_terms(f, dest.dest, args, dst_padded=isinstance(dest.padding, Halo), sync=sync)
             return dest.switch()
         sa = source
         if not isinstance(sa, AbstractStencilArray):
@@ -177,7 +177,7 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
         padded = tuple(dest.shape) != tuple(sa.shape)
         if padded and not (isinstance(sa.padding, Halo) and tuple(dest.shape) == tuple(sa.parent.shape)):
             raise A.ArgumentError(f"Source array sizes must match. Found: {tuple(sa.shape)} and {tuple(dest.shape)}")
-        return _run_terms(f, dest, (sa,) + tuple(more), dst_padded=padded)
+        return _run_terms(f, dest, (sa,) + tuple(more), dst_padded=padded, sync=sync)
     red = as_reduction(f)
     if more:
         raise NotImplementedError("extra array arguments need a registered Terms f")
