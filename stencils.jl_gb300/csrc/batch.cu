@@ -419,6 +419,11 @@ static size_t resident_smem_cap() {
     return cap;
 }
 constexpr size_t kTiledSmemCap = 200 * 1024;
+// The launch's shared memory per CTA is the largest any job needs, so one job's geometry sets every
+// job's occupancy: autotuner candidates stay within the vector tiles' boxes (38 KB), which keeps the
+// launch at 3 CTAs per SM.  (Uncapped, the tuner picked deep k-step tiles that were fastest alone
+// and made the 256-grid batch 33.6 ms instead of 22.8.)
+constexpr size_t kTunedSmemCap = 40 * 1024;
 
 static size_t tiled_smem(const BatchSpec& s, const Geometry& g) {
     const size_t es = dtype_size(s.a.dtype);
@@ -512,10 +517,17 @@ static int autotune_spec(const BatchSpec& s, DeviceCtx* ctx, cudaStream_t stream
         for (int th : ths)
             for (int k : ks) {
                 Geometry g{tw, th, k};
-                if (k > steps || tiled_smem(s, g) > kTiledSmemCap) continue;
+                if (k > steps || tiled_smem(s, g) > kTunedSmemCap) continue;
                 if (tw * th < 1024 || tw * th > 8192) continue;
                 cands.push_back(g);
             }
+    // the one-step vector-column tiles, where the shape has them, compete with the k-step tiles
+    {
+        int vtw = 0, vth = 0;
+        size_t vsmem = 0;
+        const int shape = table_matches_shape(s.shape, s.R, 2, s.offs.data(), s.L) ? s.shape : STC_SHAPE_TABLE;
+        if (vec_geometry(s, shape, &vtw, &vth, &vsmem)) cands.push_back(Geometry{vtw, vth, 1, 1});
+    }
     if (cands.empty()) { *out = default_geometry(s); return STC_OK; }
     // enough copies of the job to fill the GPU the way a loaded batch would
     const int64_t tiles = ((n0 + 63) / 64) * ((n1 + 31) / 32);
@@ -539,9 +551,10 @@ static int autotune_spec(const BatchSpec& s, DeviceCtx* ctx, cudaStream_t stream
             t.a.data = (char*)scratch + (size_t)(2 * c) * gbytes;
             t.b.data = (char*)scratch + (size_t)(2 * c + 1) * gbytes;
             t.a.stride[1] = t.b.stride[1] = n0;
-            t.force_tw = g.tw;
-            t.force_th = g.th;
-            t.force_k = g.k;
+            t.force_tw = g.vec ? 0 : g.tw;
+            t.force_th = g.vec ? 0 : g.th;
+            t.force_k = g.vec ? 0 : g.k;
+            t.force_vec = g.vec;
             trial.specs.push_back(t);
         }
         if ((rc = batch_build(&trial, false, stream, ctx))) break;
@@ -615,7 +628,7 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
         }
         b->planned_cell_steps += (double)j.n0 * j.n1 * s.nsteps;
         if (s.nsteps == 0) { j.rounds = 0; continue; }
-        const bool forced = s.force_tw > 0;
+        const bool forced = s.force_tw > 0 || s.force_vec;
         if (!forced && resident_smem(s) <= resident_smem_cap()) {
             j.resident = 1;
             j.tw = j.n0; j.th = j.n1; j.k = j.nsteps;
@@ -628,7 +641,30 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
         }
         int vtw = 0, vth = 0;
         size_t vsmem = 0;
-        if (!forced && vec_geometry(s, j.shape, &vtw, &vth, &vsmem)) {
+        const bool has_vec = vec_geometry(s, j.shape, &vtw, &vth, &vsmem);
+        // geometry: an autotuner trial's, else the autotuner's choice for the job's size class (cached
+        // per class), else the vector tiles where the shape has them, else the default k-step tiles
+        Geometry g{0, 0, 0};
+        bool use_vec = false;
+        if (s.force_vec) {
+            use_vec = has_vec;
+        } else if (forced) {
+            g = Geometry{s.force_tw, s.force_th, s.force_k};
+        } else if (autotune) {
+            int rc = autotune_spec(s, ctx, stream, &g);
+            if (rc) return rc;
+            use_vec = has_vec && g.vec;
+        } else {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(tune_key(s));
+            if (it != g_tune_cache.end() && !(b->prefer_vec && has_vec)) {
+                g = it->second;
+                use_vec = has_vec && g.vec;
+            } else {
+                use_vec = has_vec;
+            }
+        }
+        if (use_vec) {
             // one step per round on vector-column tiles
             j.resident = 0;
             j.vec = 1;
@@ -644,16 +680,7 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
             b->result_in_b[i] = j.rounds & 1;
             continue;
         }
-        Geometry g;
-        if (forced) g = Geometry{s.force_tw, s.force_th, s.force_k};
-        else if (autotune) {
-            int rc = autotune_spec(s, ctx, stream, &g);
-            if (rc) return rc;
-        } else {
-            std::lock_guard<std::mutex> lk(g_tune_mu);
-            auto it = g_tune_cache.find(tune_key(s));
-            g = it != g_tune_cache.end() ? it->second : default_geometry(s);
-        }
+        if (g.tw <= 0 || g.vec) g = default_geometry(s);
         g.k = (int)std::max<int64_t>(1, std::min<int64_t>(g.k, s.nsteps));
         j.resident = 0;
         j.tw = g.tw; j.th = g.th; j.k = g.k;
@@ -810,12 +837,74 @@ int stc_batch_add(stc_batch* b, const stc_grid* a, const stc_grid* bg, const stc
     return (int)b->specs.size() - 1;
 }
 
+namespace stc {
+// Device time of one launch of the batch's plan (prefer_vec or the tuned geometries) run on zeroed
+// scratch copies of every job's grids, so the caller's data is untouched; < 0 when it cannot be timed.
+static float batch_trial_ms(const stc_batch* b, bool prefer_vec, cudaStream_t stream, DeviceCtx* ctx) {
+    // every scratch grid starts on a 256-byte boundary (grids of different element sizes share the block)
+    auto grid_bytes = [](const BatchSpec& sp) {
+        return align_to((size_t)sp.a.size[0] * sp.a.size[1] * dtype_size(sp.a.dtype), 256);
+    };
+    size_t total = 0;
+    for (const BatchSpec& sp : b->specs) total += 2 * grid_bytes(sp);
+    void* scratch = nullptr;
+    if (total == 0 || cudaMalloc(&scratch, total) != cudaSuccess) {
+        cudaGetLastError();
+        return -1.f;
+    }
+    cudaMemsetAsync(scratch, 0, total, stream);
+    stc_batch trial;
+    trial.prefer_vec = prefer_vec;
+    size_t off = 0;
+    for (const BatchSpec& sp : b->specs) {
+        BatchSpec t = sp;
+        const size_t gb = grid_bytes(sp);
+        t.a.data = (char*)scratch + off;
+        t.b.data = (char*)scratch + off + gb;
+        t.a.stride[1] = t.b.stride[1] = sp.a.size[0];
+        off += 2 * gb;
+        trial.specs.push_back(t);
+    }
+    float best = -1.f;
+    if (batch_build(&trial, false, stream, ctx) == STC_OK) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        for (int rep = 0; rep < 3; ++rep) {
+            cudaEventRecord(e0, stream);
+            cudaGraphLaunch(trial.exec, stream);
+            cudaEventRecord(e1, stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && (best < 0.f || ms < best)) best = ms;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    batch_free(&trial);
+    cudaStreamSynchronize(stream);
+    cudaFree(scratch);
+    return best;
+}
+}  // namespace stc
+
 int stc_batch_plan(stc_batch* b, int32_t autotune, void* stream) {
     if (!b) return STC_ERR_INVALID;
     DeviceCtx* ctx = nullptr;
     int rc = device_ctx(&ctx);
     if (rc) return rc;
-    return batch_build(b, autotune != 0, (cudaStream_t)stream, ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    b->prefer_vec = false;
+    if (!autotune) return batch_build(b, false, s, ctx);
+    // 1. per size class, the fastest tile geometry (cached); 2. for the whole batch, the tuned plan
+    // against vector tiles everywhere they apply, each timed once on scratch copies (one job's
+    // geometry sets the shared memory, so the occupancy, of every job in the launch)
+    if ((rc = batch_build(b, true, s, ctx, false))) return rc;
+    const float tuned = batch_trial_ms(b, false, s, ctx);
+    const float vec = batch_trial_ms(b, true, s, ctx);
+    b->prefer_vec = vec >= 0.f && (tuned < 0.f || vec < tuned);
+    return batch_build(b, false, s, ctx);
 }
 
 int stc_batch_run(stc_batch* b, void* stream, uint32_t flags) {

@@ -72,10 +72,12 @@ struct BatchSpec {
     stc_bc bc{};
     int64_t nsteps = 0;
     int opv = 0;
-    int force_tw = 0, force_th = 0, force_k = 0;   // autotuner trials
+    int force_tw = 0, force_th = 0, force_k = 0;   // autotuner trials: k-step tiles of this geometry
+    int force_vec = 0;                              // autotuner trials: one-step vector-column tiles
 };
 
-struct Geometry { int tw, th, k; };
+// tiled-job geometry; vec = 1 selects one-step vector-column tiles (tw, th fixed by the element type)
+struct Geometry { int tw, th, k; int vec = 0; };
 
 }  // namespace stc
 
@@ -96,6 +98,7 @@ struct stc_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool planned = false;
+    bool prefer_vec = false;   // plan vector tiles wherever the shape has them, ignoring tuned geometries
     double planned_cell_steps = 0;
 };
 
