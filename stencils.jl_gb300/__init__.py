@@ -17,8 +17,8 @@ from .ops import sum  # noqa: A004
 from .scatter import ScatterConst, scatter_center, scatter_weighted, scatterstencil_
 from .serve import Server
 from .stencil import (AngledCross, Annulus, BackSlash, Cardinal, Circle, Cross, Diamond, ForwardSlash, Horizontal,
-                      Kernel, Moore, NamedStencil, Ordinal, Positional, Rectangle, Stencil, Vertical, VonNeumann,
-                      Window)
+                      Kernel, Layered, Moore, NamedStencil, Ordinal, Positional, Rectangle, Stencil, Vertical,
+                      VonNeumann, Window)
 
 __all__ = [
     "Batch", "Server",
@@ -30,4 +30,5 @@ __all__ = [
     "AngledCross",
     "Annulus", "BackSlash", "Cardinal", "Circle", "Cross", "Diamond", "ForwardSlash", "Horizontal", "Kernel",
     "Moore", "NamedStencil", "Ordinal", "Positional", "Rectangle", "Stencil", "Vertical", "VonNeumann", "Window",
+    "Layered",
 ]

@@ -158,12 +158,19 @@ class AbstractStencilArray:
         return tuple(self._bounded(J) for J in self.stencil.indices(tuple(I)))
 
     def neighbors(self, I):
-        """neighbors(A, I): neighbour values around the 1-based index I (src/array.jl:68-115)."""
+        """neighbors(A, I): neighbour values around the 1-based index I (src/array.jl:68-115); for a
+        Layered stencil, one tuple per layer (src/stencils/layered.jl:52-54)."""
+        return self._neighbors(self.stencil, I)
+
+    def _neighbors(self, stencil, I):
+        from .stencil import Layered
+        if isinstance(stencil, Layered):
+            return tuple(self._neighbors(l, I) for l in stencil.layers)
         host = to_host(self.parent)
         R = self.radius
         vals = []
         halo = isinstance(self.padding, Halo)
-        for J in self.stencil.indices(tuple(I)):
+        for J in stencil.indices(tuple(I)):
             if halo:
                 vals.append(host[tuple(j - 1 + R for j in J)])
                 continue
@@ -177,9 +184,15 @@ class AbstractStencilArray:
         return vals
 
     def center(self, I):
+        """center of the stencil at the 1-based index I; for a Layered stencil, one per layer."""
+        from .stencil import Layered
         host = to_host(self.parent)
         off = self.radius if isinstance(self.padding, Halo) else 0
-        return host[tuple(i - 1 + off for i in I)]
+        c = host[tuple(i - 1 + off for i in I)]
+
+        def per(st):
+            return tuple(per(l) for l in st.layers) if isinstance(st, Layered) else c
+        return per(self.stencil)
 
 
 class StencilArray(AbstractStencilArray):

@@ -30,8 +30,6 @@ template <> struct Elem<STC_BOOL> { using T = uint8_t;         static constexpr 
 template <> struct Elem<STC_I32>  { using T = int32_t;         static constexpr bool is_float = false; };
 template <> struct Elem<STC_I64>  { using T = int64_t;         static constexpr bool is_float = false; };
 
-// value -> accumulator
-template <class A> __device__ __forceinline__ A to_acc(double x) { return (A)x; }
 __device__ __forceinline__ double cvt_d(double x) { return x; }
 __device__ __forceinline__ double cvt_d(float x) { return (double)x; }
 __device__ __forceinline__ double cvt_d(__nv_bfloat16 x) { return (double)__bfloat162float(x); }

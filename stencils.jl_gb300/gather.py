@@ -16,7 +16,7 @@ from .array import (AbstractStencilArray, StencilArray, SwitchingStencilArray, _
                     to_device)
 from .boundary import Conditional, Halo
 from .ops import Terms, as_reduction
-from .stencil import Stencil
+from .stencil import Layered, Stencil, with_radius
 
 
 def result_dtype_code(red, src_code: int, stencil) -> int:
@@ -91,20 +91,24 @@ def _new_dest(like, shape, code):
     return np.empty(shape, dtype=A.NP_DTYPE[code], order="F")
 
 
-def _term_item(a):
-    """A multi-array argument as the oracle-style item: (parent, stencil, boundary, padding) for a
-    StencilArray (a SwitchingStencilArray contributes its current source), else the plain array."""
-    if isinstance(a, SwitchingStencilArray):
-        return (a.source, a.stencil, a.boundary, a.padding)
+def _term_items(a):
+    """A multi-array argument as oracle-style items: (parent, stencil, boundary, padding) for a
+    StencilArray (a SwitchingStencilArray contributes its current source; a Layered stencil one item
+    per leaf layer, each with the Layered radius, over the same parent), else the plain array."""
     if isinstance(a, AbstractStencilArray):
-        return (a.parent, a.stencil, a.boundary, a.padding)
-    return a
+        parent = a.source if isinstance(a, SwitchingStencilArray) else a.parent
+        if isinstance(a.stencil, Layered):
+            R = a.stencil.radius
+            return [(parent, with_radius(l, R), a.boundary, a.padding) for l in a.stencil.leaves()]
+        return [(parent, a.stencil, a.boundary, a.padding)]
+    return [a]
+
 
 
 def _run_terms(f: Terms, dest, args, dst_padded: bool, sync: bool = True):
     """dest[I] = f(args at I) through stc_map_terms (src/gatherstencil.jl:89-113)."""
     lib = _lib.load()
-    items = [_term_item(a) for a in args]
+    items = [it for a in args for it in _term_items(a)]
     arrays = [it[0] if isinstance(it, tuple) else it for it in items]
     halo_idx = [i for i, it in enumerate(items) if isinstance(it, tuple) and isinstance(it[3], Halo)]
     stage = _Staged(*arrays, dest, writeback=tuple(halo_idx) + (len(arrays),))

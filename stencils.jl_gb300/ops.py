@@ -161,16 +161,17 @@ class Terms:
     `Terms(center, scaled(0.1, sum))`."""
 
     def __init__(self, *terms):
-        if not 1 <= len(terms) <= 4:
+        used = [t for t in terms if t is not None]
+        if not 1 <= len(used) <= 4:
             raise ValueError("1 to 4 terms")
-        for t in terms:
+        for t in used:
             base = t.term if isinstance(t, Scaled) else t
             if not isinstance(base, Reduction) or base.name not in _TERM_KIND:
                 raise NotImplementedError(f"{t!r} is not a registered term")
         self.terms = terms
 
     def __repr__(self):
-        return " + ".join(map(repr, self.terms))
+        return " + ".join(repr(t) for t in self.terms if t is not None)
 
     def lower(self, items, code, grid_fn):
         """TermDesc descriptors for `items`: per argument either a (parent, stencil, boundary, padding)
@@ -180,6 +181,8 @@ class Terms:
             raise ValueError(f"{len(self.terms)} terms for {len(items)} arguments")
         descs, keep = [], []
         for t, it in zip(self.terms, items):
+            if t is None:   # an argument (or layer) the sum does not use
+                continue
             base, alpha = (t.term, t.alpha) if isinstance(t, Scaled) else (t, 0.0)
             d = A.TermDesc()
             d.kind = _TERM_KIND[base.name]

@@ -343,3 +343,81 @@ class Kernel(Stencil):
 def stencil_radius_ok(st: Stencil) -> bool:
     """True when every offset lies within the radius used for halos and bounds checks."""
     return st.max_abs_offset() <= st.radius
+
+
+class Layered:
+    """Several stencils used together over one array (src/stencils/layered.jl:13-60).
+
+    `Layered(a, b)` or `Layered(name=a, ...)`; layers may themselves be Layered.  The radius is the
+    largest layer radius (so a Halo parent is padded for every layer); `offsets`, `indices`,
+    `distances`, `len` return one entry per layer, and layers are reached by position or name.
+    Maps over a Layered stencil take a registered `Terms` sum with one term per leaf layer (in
+    order, nested layers flattened; `None` for a layer the sum does not use): each term reads the
+    same parent through its own layer.
+    """
+
+    shape_id = SHAPE_TABLE
+
+    def __init__(self, *layers, **named):
+        if layers and named:
+            raise ValueError("Layered takes positional or named layers, not both")
+        if len(layers) == 1 and isinstance(layers[0], (tuple, list)):
+            layers = tuple(layers[0])
+        self.names = tuple(named) if named else None
+        self.layers = tuple(named.values()) if named else tuple(layers)
+        if not self.layers:
+            raise ValueError("Layered needs at least one layer")
+        for l in self.layers:
+            if not isinstance(l, (Stencil, Layered)):
+                raise TypeError(f"layers must be stencils, got {type(l).__name__}")
+        self.ndims = self.layers[0].ndims
+        if any(l.ndims != self.ndims for l in self.layers):
+            raise ValueError("all layers need the same number of dimensions")
+        self.radius = max(l.radius for l in self.layers)
+
+    def __len__(self):
+        raise TypeError("length(::Layered) is a tuple: use lengths()")
+
+    def lengths(self):
+        return tuple(l.lengths() if isinstance(l, Layered) else len(l) for l in self.layers)
+
+    def __getitem__(self, key):
+        if isinstance(key, str):
+            return self.layers[self.names.index(key)]
+        return self.layers[key]
+
+    def __getattr__(self, name):
+        names = self.__dict__.get("names")
+        if names and name in names:
+            return self.__dict__["layers"][names.index(name)]
+        raise AttributeError(name)
+
+    def offsets(self):
+        return tuple(l.offsets() for l in self.layers)
+
+    def indices(self, I):
+        return tuple(l.indices(I) for l in self.layers)
+
+    def distances(self):
+        return tuple(l.distances() for l in self.layers)
+
+    def leaves(self):
+        """The leaf stencils in order, nested Layered flattened."""
+        out = []
+        for l in self.layers:
+            out.extend(l.leaves() if isinstance(l, Layered) else [l])
+        return out
+
+    def __repr__(self):
+        body = ", ".join(f"{n}={l!r}" for n, l in zip(self.names, self.layers)) if self.names else \
+            ", ".join(map(repr, self.layers))
+        return f"Layered({body})"
+
+
+def with_radius(stencil: Stencil, R: int) -> Stencil:
+    """The same offsets (and weights) with the halo radius R of an enclosing Layered stencil."""
+    import copy
+    s = copy.copy(stencil)
+    s.radius = int(R)
+    s.shape_id = SHAPE_TABLE
+    return s
