@@ -52,7 +52,8 @@ typedef enum {
     STC_ERR_KERNEL_LENGTH = -3,   /* "Stencil length .. does not match kernel length"  src/stencils/kernel.jl:342 */
     STC_ERR_UNSUPPORTED = -4,     /* shape / op / dtype / boundary combination not registered (a MethodError
                                      in the reference, e.g. Use with Conditional padding has no getneighbor) */
-    STC_ERR_INVALID = -5,         /* malformed descriptor (null pointer, bad ndims, stride[0] != 1, ...) */
+    STC_ERR_INVALID = -5,         /* malformed descriptor (null pointer, bad ndims, stride[0] != 1, ...), or a
+                                     dest whose element bytes overlap a source's (no defined result) */
     STC_ERR_CUDA = -6,            /* a CUDA runtime call failed */
     STC_ERR_TIMEOUT = -7,         /* a bounded device-side wait ran out; the kernel returned early */
     STC_ERR_NO_DEVICE = -8,       /* no usable sm_100-family GPU */

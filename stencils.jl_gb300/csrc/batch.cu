@@ -803,6 +803,7 @@ int stc_batch_add(stc_batch* b, const stc_grid* a, const stc_grid* bg, const stc
     if (!b || nsteps < 0) return STC_ERR_INVALID;
     int rc = validate_map(a, bg, 1, st, op, bc);
     if (rc) return rc;
+    if (nsteps > 0 && grids_overlap(a, bg)) return STC_ERR_INVALID;
     if (a->ndims != 2 || st->ndims != 2 || bc->padding != STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
     if (!(bc->boundary == STC_REMOVE || bc->boundary == STC_WRAP)) return STC_ERR_UNSUPPORTED;
     if (st->len > kBatchMaxL || st->radius > kBatchMaxR) return STC_ERR_UNSUPPORTED;

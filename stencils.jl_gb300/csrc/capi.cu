@@ -187,6 +187,25 @@ static int check_grid(const stc_grid* g) {
     return STC_OK;
 }
 
+// True if the byte ranges spanned by a's and b's elements intersect (conservative for interleaved
+// views of one buffer).  A dest that shares memory with its source has no defined result: the tiled
+// kernels read boxes other CTAs are writing, and the reference's threads race the same way.
+bool grids_overlap(const stc_grid* a, const stc_grid* b) {
+    auto span = [](const stc_grid* g, uintptr_t& lo, uintptr_t& hi) {
+        int64_t last = 0;
+        for (int d = 0; d < g->ndims; ++d) {
+            if (g->size[d] == 0) return false;
+            last += (g->size[d] - 1) * g->stride[d];
+        }
+        lo = (uintptr_t)g->data;
+        hi = lo + (uintptr_t)((last + 1) * (int64_t)dtype_size(g->dtype));
+        return true;
+    };
+    uintptr_t al, ah, bl, bh;
+    if (!span(a, al, ah) || !span(b, bl, bh)) return false;
+    return al < bh && bl < ah;
+}
+
 int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
                  const stc_op* op, const stc_bc* bc) {
     int rc;
@@ -476,6 +495,7 @@ int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded, const 
             const stc_bc* bc, void* stream, uint32_t flags) {
     int rc = validate_map(src, dst, dst_padded, st, op, bc);
     if (rc) return rc;
+    if (grids_overlap(src, dst)) return STC_ERR_INVALID;
     DeviceCtx* ctx = nullptr;
     if ((rc = device_ctx(&ctx))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
@@ -568,7 +588,7 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
     if (rc) return rc;
     for (int d = 0; d < a->ndims; ++d)
         if (a->size[d] != b->size[d] || a->dtype != b->dtype) return STC_ERR_SIZE_MISMATCH;
-    if (a->data == b->data && nsteps > 0) return STC_ERR_INVALID;
+    if (nsteps > 0 && grids_overlap(a, b)) return STC_ERR_INVALID;
     DeviceCtx* ctx = nullptr;
     if ((rc = device_ctx(&ctx))) return rc;
     cudaStream_t s = (cudaStream_t)stream;

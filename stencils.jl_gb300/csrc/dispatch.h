@@ -51,6 +51,8 @@ int cuda_fail(cudaError_t e);
 
 int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
                  const stc_op* op, const stc_bc* bc);
+// true if the two grids' element byte ranges intersect
+bool grids_overlap(const stc_grid* a, const stc_grid* b);
 int result_dtype(int op, int sdt, int wdt);
 // true if the FMA-corrected Float32 quotient by L is exact for every input (checked once per L)
 bool fastdiv_f_exact(int L);

@@ -801,6 +801,7 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     if (rc) return rc;
     for (int d = 0; d < a->ndims; ++d)
         if (a->size[d] != b->size[d] || a->dtype != b->dtype) return STC_ERR_SIZE_MISMATCH;
+    if (nsteps > 0 && grids_overlap(a, b)) return STC_ERR_INVALID;
     if (op->code != STC_OP_LIFE || a->ndims != 2 || !is_moore1_2d(st)) return STC_ERR_UNSUPPORTED;
     if (!(a->dtype == STC_U8 || a->dtype == STC_BOOL || a->dtype == STC_I32 || a->dtype == STC_I64))
         return STC_ERR_UNSUPPORTED;

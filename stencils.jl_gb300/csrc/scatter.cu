@@ -159,6 +159,9 @@ int stc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* st,
     p.nx = src->size[1] - (halo ? 2 * R : 0);
     if (p.ny < 0 || p.nx < 0) return STC_ERR_RADIUS;
     if (dst->size[0] != p.ny || dst->size[1] != p.nx) return STC_ERR_SIZE_MISMATCH;
+    for (int d = 0; d < 2; ++d)
+        if (src->stride[d] < 0 || dst->stride[d] < 0) return STC_ERR_INVALID;
+    if (grids_overlap(src, dst)) return STC_ERR_INVALID;   // a dest cell's pull would read cells being written
     p.src = src->data;
     p.dst = dst->data;
     p.sst1 = src->stride[1];

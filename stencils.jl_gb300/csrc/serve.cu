@@ -271,8 +271,10 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
     // validate with the batch rules on placeholder device pointers
     stc_batch probe;
     stc_grid a = g, b = g;
-    a.data = (void*)0x100;
-    b.data = (void*)0x200;
+    // (disjoint placeholders: the batch rules reject a dest that shares memory with its source)
+    const uintptr_t span = (uintptr_t)(g.size[0] * g.size[1]) * (uintptr_t)dtype_size(g.dtype);
+    a.data = (void*)(uintptr_t)0x100;
+    b.data = (void*)((uintptr_t)0x200 + span);
     int rc = stc_batch_add(&probe, &a, &b, &job->stencil, &job->op, &job->bc, job->nsteps);
     if (rc < 0) return rc;
     ServeJob* j = new ServeJob();

@@ -122,11 +122,16 @@ int stc_map_terms(const stc_term* terms, int32_t nterms, const stc_grid* dst, in
     int64_t n[3] = {1, 1, 1};
     const int nd = dst->ndims;
     if (nd < 1 || nd > 3 || (dst->size[0] > 1 && dst->stride[0] != 1)) return STC_ERR_INVALID;
+    for (int d = 0; d < nd; ++d)
+        if (dst->size[d] < 0 || dst->stride[d] < 0) return STC_ERR_INVALID;
     for (int m = 0; m < nterms; ++m) {
         const stc_term& tm = terms[m];
         const stc_grid* g = tm.grid;
         if (!g || !g->data || g->ndims != nd || (g->size[0] > 1 && g->stride[0] != 1)) return STC_ERR_INVALID;
+        for (int d = 0; d < nd; ++d)
+            if (g->size[d] < 0 || g->stride[d] < 0) return STC_ERR_INVALID;
         if (g->dtype != dt) return STC_ERR_UNSUPPORTED;
+        if (grids_overlap(g, dst)) return STC_ERR_INVALID;   // dest may not share memory with an argument
         if (tm.kind < STC_TERM_CENTER || tm.kind > STC_TERM_VALUE) return STC_ERR_UNSUPPORTED;
         TermDev& t = p.t[m];
         t.src = g->data;

@@ -274,3 +274,21 @@ def test_argument_errors_on_gpu(cuda, st):
     bad = st.colmajor_empty((8, 7), torch.float64)
     with pytest.raises(st.ArgumentError):
         st.mapstencil_(st.mean, bad, A)
+
+
+def test_dest_sharing_the_source_memory_is_rejected(cuda, st):
+    """mapstencil!(f, dest, A) with dest = A's own parent (or a view into it) has no defined result:
+    the library refuses it with STC_ERR_INVALID instead of racing."""
+    import torch
+    from stencils_gb300._lib import StencilError
+    parent = st.to_device(np.asfortranarray(np.random.default_rng(5).random((16, 12))))
+    A = st.StencilArray(parent, st.Window(1))
+    with pytest.raises(StencilError):
+        st.mapstencil_(st.mean, parent, A)
+    S = st.SwitchingStencilArray(parent, st.Window(1), st.Wrap(), _dest=parent)
+    with pytest.raises(StencilError):
+        st.mapstencil_(st.mean, S, steps=2)
+    # a separate dest still maps
+    out = st.colmajor_empty((16, 12), torch.float64)
+    st.mapstencil_(st.mean, out, A)
+    torch.cuda.synchronize()
