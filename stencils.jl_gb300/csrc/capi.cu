@@ -422,6 +422,9 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
                p.bh <= 256 && p.bd <= 256 && 2 * (int64_t)p.stage_bytes <= smem_cap;
     for (int d = 1; d < nd; ++d)
         if ((src->stride[d] * es) % 16 != 0) tma = false;
+    // TMA box coordinates are signed 32-bit: axes this long take the cooperative (64-bit) loader
+    for (int d = 0; d < nd; ++d)
+        if (src->size[d] + tma_shift + 512 >= (1ll << 31)) tma = false;
     if (tma) {
         p.stages = (int)std::min<int64_t>(kMaxStages, std::max<int64_t>(2, (64 * 1024) / p.stage_bytes));
         while ((int64_t)p.stages * p.stage_bytes > smem_cap) --p.stages;

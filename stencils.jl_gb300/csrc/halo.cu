@@ -63,21 +63,21 @@ __global__ void halo_fill_kernel(const HaloParams p) {
     const int e0 = p.R, e1 = p.ndims > 1 ? p.R : 0, e2 = p.ndims > 2 ? p.R : 0;
     const int n0 = (int)p.n[0], n1 = (int)p.n[1], n2 = (int)p.n[2];
     const int wx = n0 + 2 * e0, wy = n1 + 2 * e1;
-    const int rowsA = 2 * e2 * wy, rowsB = n2 * 2 * e1;
+    const int64_t rowsA = (int64_t)2 * e2 * wy, rowsB = (int64_t)n2 * 2 * e1;
     const int64_t cellsC = (int64_t)n1 * n2 * 2 * e0;
     auto put = [&](int64_t x, int64_t y, int64_t z) {
         base[(x + p.R) + (y + e1) * p.st[1] + (z + e2) * p.st[2]] = halo_value<T>(p, base, x, y, z);
     };
     // parts A and B: a block per row, threads along x
-    for (int r = blockIdx.x; r < rowsA + rowsB; r += gridDim.x) {
+    for (int64_t r = blockIdx.x; r < rowsA + rowsB; r += gridDim.x) {
         int64_t y, z;
         if (r < rowsA) {
-            const int zi = r / wy;
-            y = r - zi * wy - e1;
+            const int zi = (int)(r / wy);   // < 2 e2
+            y = r - (int64_t)zi * wy - e1;
             z = zi < e2 ? zi - e2 : n2 + (zi - e2);
         } else {
-            const int q = r - rowsA;
-            const int zi = q / (2 * e1), yi = q - zi * 2 * e1;
+            const int64_t q = r - rowsA;
+            const int64_t zi = q / (2 * e1), yi = q - zi * 2 * e1;
             z = zi;
             y = yi < e1 ? yi - e1 : n1 + (yi - e1);
         }
