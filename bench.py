@@ -717,8 +717,60 @@ def run_scatter(args):
     print(json.dumps(line), flush=True)
 
 
+def run_shapes(args):
+    """The remaining shapes (offset-table kernel) and boundaries: one map per step on 8192^2 Float32
+    U[0,1) for each (stencil, reduction, boundary, padding) below, through mapstencil_; Halo paddings
+    include the ring refresh each map (update_boundary!, as the reference's gatherstencil! does).  Each
+    result is compared bit for bit with the oracle on the full grid; the oracle on all host cores is the
+    CPU baseline."""
+    import statistics
+    import torch
+    entry.build()
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    from oracle import oracle as orc
+    A = __import__("stencils_gb300._abi", fromlist=["x"])
+    n = 8192
+    rng = np.random.Generator(np.random.PCG64(11))
+    a = np.asfortranarray(rng.random((n, n), dtype=np.float32))
+    combos = [
+        ("Annulus(3) mean, Remove(0), Conditional", st.Annulus(3), st.mean, st.Remove(0.0), st.Conditional()),
+        ("Diamond(2) sum, Reflect, Conditional", st.Diamond(2), st.sum, st.Reflect(), st.Conditional()),
+        ("Rectangle((-2,1),(-1,3)) mean, Wrap, Conditional", st.Rectangle((-2, 1), (-1, 3)), st.mean, st.Wrap(),
+         st.Conditional()),
+        ("Window(1) mean, Use, Halo{:in} (output 8190^2)", st.Window(1), st.mean, st.Use(), st.Halo("in")),
+        ("Circle(3) mean, Reflect, Halo{:out}", st.Circle(3), st.mean, st.Reflect(), st.Halo("out")),
+    ]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    thr = orc.max_threads()
+    res = []
+    for name, hood, red, bnd, pad in combos:
+        sa = st.StencilArray(st.to_device(a), hood, bnd, pad)
+        out = st.mapstencil(red, sa)
+        cells = int(np.prod(out.shape))
+        _lib.profile_enable(True)
+        t = _timed_steps(lambda: st.mapstencil_(red, out, sa, sync=False), args.steps, args.warmup, flush)
+        prof = _lib.profile_report()
+        _lib.profile_enable(False)
+        got = st.to_host(out)
+        parent = st.to_host(sa.parent)
+        t0 = time.perf_counter()
+        want = orc.map(parent, A.F32, hood, red, bnd, pad, nthreads=thr)
+        cpu_s = time.perf_counter() - t0
+        res.append({"case": name, "taps": len(hood), "gcell_s": args.steps * cells / t / 1e9,
+                    "us_per_map": 1e6 * t / args.steps, "bit_exact_vs_oracle": got.tobytes(order="F") ==
+                    want.tobytes(order="F"), "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"]),
+                    "cpu_gcell_s": cells / cpu_s / 1e9})
+        del sa, out
+    line = {"workload": "remaining shapes and boundaries, Float32 8192x8192, one map per step", "metric": METRIC,
+            "unit": UNIT, "value": statistics.median(r["gcell_s"] for r in res), "value_is": "median over cases",
+            "results": res, "cpu_baseline": {"unit": UNIT, "cores": thr, "kind": "port",
+                                             "sample": "one full map per case (cpu_gcell_s per case)"}}
+    print(json.dumps(line), flush=True)
+
+
 WORKLOADS = {"mean_blur": run_mean_blur, "gauss": run_gauss, "diffusion": run_diffusion, "batched": run_batched,
-             "terms": run_terms, "scatter": run_scatter,
+             "terms": run_terms, "scatter": run_scatter, "shapes": run_shapes,
              "serving": run_serving}
 
 
