@@ -434,11 +434,44 @@ __device__ __forceinline__ void report(const MapParams& p, int code) {
 
 // ---------------------------------------------------------------------------- compute: generic
 // Thread owns XT columns (lane + 32 i) and VS slots; slot s is row warp*VS + s (2D tiles) or
-// (row warp, plane s) (3D tiles).  Each output folds over the run-time offset table.
+// (row warp, plane s) (3D tiles).  Each output folds over the run-time offset table in table order.
+// The table loop is outermost: the XT x VS folds advance together as independent chains, and each
+// offset's box displacement is formed once per thread.  Outputs past the grid's edge are folded too
+// (every slot and column of the tile lies inside the box, whatever the grid's extent) and not stored.
 template <class Tin, class Tout, class Op, int XT, int VS>
 __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOrigin& o, const Tin* box) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     Tout* dst = (Tout*)p.dst;
+    const Tin* c[VS];
+#pragma unroll
+    for (int s = 0; s < VS; ++s) {
+        const int ly = p.tiles3d ? warp : warp * VS + s;
+        const int lz = p.tiles3d ? s : 0;
+        c[s] = box + ((lz + p.rz) * p.bh + (ly + p.ry)) * p.bw + (lane + p.padl);
+    }
+    typename Op::A a[VS][XT];
+    int k0 = 0;
+    if constexpr (Op::kZeroInit) {
+#pragma unroll
+        for (int s = 0; s < VS; ++s)
+#pragma unroll
+            for (int i = 0; i < XT; ++i) a[s][i] = Op::first(c[s][32 * i], 0);
+    } else {
+        const int d = (p.off[0][2] * p.bh + p.off[0][1]) * p.bw + p.off[0][0];
+#pragma unroll
+        for (int s = 0; s < VS; ++s)
+#pragma unroll
+            for (int i = 0; i < XT; ++i) a[s][i] = Op::first(c[s][32 * i + d], 0);
+        k0 = 1;
+    }
+    for (int k = k0; k < p.L; ++k) {
+        const int d = (p.off[k][2] * p.bh + p.off[k][1]) * p.bw + p.off[k][0];
+#pragma unroll
+        for (int s = 0; s < VS; ++s)
+#pragma unroll
+            for (int i = 0; i < XT; ++i) a[s][i] = Op::step(a[s][i], c[s][32 * i + d], k, p);
+    }
+    const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0);
 #pragma unroll
     for (int s = 0; s < VS; ++s) {
         const int ly = p.tiles3d ? warp : warp * VS + s;
@@ -446,23 +479,10 @@ __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOr
         const int64_t y = o.y0 + ly, z = o.z0 + lz;
         if (y >= p.n[1] || z >= p.n[2]) continue;
         Tout* drow = dst + p.dst_org + y * p.dstr[1] + z * p.dstr[2] + o.x0;
-        const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0);
 #pragma unroll
         for (int i = 0; i < XT; ++i) {
             const int lx = lane + 32 * i;
-            if (lx >= nvx) continue;
-            const Tin* c = box + ((lz + p.rz) * p.bh + (ly + p.ry)) * p.bw + (lx + p.padl);
-            typename Op::A a;
-            int k0 = 0;
-            if constexpr (Op::kZeroInit) {
-                a = Op::first(c[0], 0);
-            } else {
-                a = Op::first(c[(p.off[0][2] * p.bh + p.off[0][1]) * p.bw + p.off[0][0]], 0);
-                k0 = 1;
-            }
-            for (int k = k0; k < p.L; ++k)
-                a = Op::step(a, c[(p.off[k][2] * p.bh + p.off[k][1]) * p.bw + p.off[k][0]], k, p);
-            drow[lx] = Op::finish(a, c[0], p);
+            if (lx < nvx) drow[lx] = Op::finish(a[s][i], c[s][32 * i], p);
         }
     }
 }
