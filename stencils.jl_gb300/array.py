@@ -90,6 +90,22 @@ def _check_radius(parent, stencil: Stencil):
             raise ArgumentError(f"stencil radius is larger than array axis {s}")
 
 
+def halo_parent_zeros(shape: Sequence[int], R: int, dtype, device="cuda"):
+    """A zeroed column-major tensor of `shape` whose interior rows (axis-0 index R onward) start on
+    128-byte lines: a view into a larger buffer, with a few leading elements before index 0 and the
+    axis-1 stride rounded up to 128 bytes.  The tiled kernels then stage boxes of it by TMA (which needs
+    16-byte row strides) and take the vector-column path (which needs the interior's first column on
+    an aligned shared-memory index).  Shape, indexing and contents are those of a plain array."""
+    import torch
+    shape = tuple(int(s) for s in shape)
+    es = torch.empty((), dtype=dtype).element_size()
+    line = max(1, 128 // es)
+    lead = (-R) % line
+    pitch = -(-(lead + shape[0]) // line) * line
+    buf = colmajor_zeros((pitch,) + shape[1:], dtype, device)
+    return buf[lead:lead + shape[0]]
+
+
 def pad_array(padding: Padding, stencil: Stencil, parent):
     """Halo(:out) allocates a parent larger by R per side with the array in its interior
     (src/padding.jl:104-110); Conditional and Halo(:in) use the array as is."""
@@ -97,7 +113,7 @@ def pad_array(padding: Padding, stencil: Stencil, parent):
         R = stencil.radius
         shape = tuple(s + 2 * R for s in parent.shape)
         if _is_torch(parent):
-            padded = colmajor_zeros(shape, parent.dtype, parent.device)
+            padded = halo_parent_zeros(shape, R, parent.dtype, parent.device)
         else:
             padded = np.zeros(shape, dtype=parent.dtype, order="F")
         inner = tuple(slice(R, R + s) for s in parent.shape)
