@@ -91,3 +91,24 @@ def test_result_dtypes(st, orc, abi):
     assert orc.result_dtype(st.life, abi.U8) == abi.U8
     with pytest.raises(NotImplementedError):
         orc.result_dtype(st.life, abi.F32)
+
+
+def test_halo_out_parents_align_interior_rows(st):
+    """pad_array for Halo{:out} on a torch parent: the reference's shape and contents, with the interior's
+    rows starting on 128-byte lines (axis-1 stride a multiple of 128 bytes)."""
+    import torch
+    from stencils_gb300.array import halo_parent_zeros, pad_array
+    for dt in (torch.float32, torch.float64, torch.bfloat16, torch.uint8, torch.int64):
+        for R in (1, 2, 3):
+            for shape in ((9,), (7, 5), (13, 6, 4)):
+                t = halo_parent_zeros(shape, R, dt, "cpu")
+                es = t.element_size()
+                assert tuple(t.shape) == shape and t.stride(0) == 1
+                if len(shape) > 1:
+                    assert (t.stride(1) * es) % 128 == 0
+                assert ((t.storage_offset() + R) * es) % 128 == 0
+                assert not t.any()
+    a = torch.from_numpy(np.asfortranarray(np.arange(35, dtype=np.float32).reshape(7, 5)))
+    p = pad_array(st.Halo("out"), st.Moore(2), a)
+    assert tuple(p.shape) == (11, 9)
+    assert np.array_equal(p[2:-2, 2:-2].numpy(), a.numpy()) and float(p.sum()) == float(a.sum())
