@@ -66,7 +66,10 @@ static cudaError_t prepare_launch(K kern, LaunchCache& c, size_t smem, int* per_
 template <class Tin, class Tout, class Op, class Sh, int XT, int VS, bool VEC = false, int MINB = 2>
 cudaError_t launch_tiled(MapParams& p, cudaStream_t stream, int num_sms) {
     static LaunchCache cache;
-    auto kern = VEC ? map_vec_kernel<Tin, Tout, Op, Sh, XT, VS, MINB> : map_kernel<Tin, Tout, Op, Sh, XT, VS>;
+    // only the variant this launcher runs is instantiated
+    void (*kern)(const MapParams);
+    if constexpr (VEC) kern = map_vec_kernel<Tin, Tout, Op, Sh, XT, VS, MINB>;
+    else kern = map_kernel<Tin, Tout, Op, Sh, XT, VS>;
     const size_t smem = (size_t)(p.use_tma ? p.stages : 1) * p.stage_bytes + (size_t)kMaxStages * 8;
     int per_sm = 0;
     cudaError_t e = prepare_launch(kern, cache, smem, &per_sm);
