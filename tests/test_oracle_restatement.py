@@ -1,0 +1,213 @@
+"""A second, independent restatement of the reference's gather in pure-Python loops, checked bit for bit
+against the C oracle on small seeded grids: 1D/2D/3D stencils (named shapes, Annulus, Rectangle,
+Positional) x boundaries (Remove, Wrap, Reflect, Use) x paddings (Conditional, Halo{:out}, Halo{:in}) x
+reductions (mean, sum, minimum, maximum, kernelproduct, Life, diffusion) in Float64, Float32, UInt8 and
+Int64, single maps and SwitchingStencilArray runs.  The reference's own goldens use integer-valued
+data; this pins the oracle's boundary handling and left-fold order on random floats as well.
+
+Semantics restated here (reference file:line):
+* neighbour J = I + o: Conditional Remove reads padval outside the array (src/array.jl:133-135);
+  Conditional Wrap / Reflect read the per-axis bounded index (src/array.jl:150-175: Wrap i +- s,
+  Reflect 2 - i and 2s - i in 1-based indices); Halo reads parent[J + R] (src/array.jl:186-188).
+* update_boundary! before each map (src/array.jl:195-239): a ring cell of logical index J gets padval
+  (Remove) or the interior value at the per-axis bounded index of J (Wrap / Reflect, `halo_val`);
+  Use and Conditional leave the parent alone.
+* sum / mean / minimum / maximum fold left in offset order from the first value; mean divides by L;
+  kernelproduct starts from zero and adds v * w per offset (src/stencils/kernel.jl:37-43); Life counts
+  nonzero neighbours against the birth / survive sets; diffusion is c + alpha (s - L c), each operation
+  rounded.
+"""
+import zlib
+
+import numpy as np
+import pytest
+
+from _backends import OracleBackend
+
+
+# ------------------------------------------------------------------ the restatement
+def _bound(kind, i, n):
+    if kind == "wrap":
+        return i + n if i < 0 else (i - n if i >= n else i)
+    return -i if i < 0 else (2 * n - 2 - i if i >= n else i)   # reflect, 0-based
+
+
+def _update_ring(parent, shape, R, kind, padval):
+    interior = parent[tuple(slice(R, R + n) for n in shape)].copy()
+    for P in np.ndindex(*parent.shape):
+        J = tuple(p - R for p in P)
+        if all(0 <= j < n for j, n in zip(J, shape)):
+            continue
+        parent[P] = padval if kind == "remove" else interior[tuple(_bound(kind, j, n) for j, n in zip(J, shape))]
+
+
+def _fold(red, vals, centre, T, L, weights, rule, alpha):
+    if red in ("mean", "sum", "diffusion"):
+        acc = T(vals[0])
+        for v in vals[1:]:
+            acc = T(acc + T(v))
+        if red == "mean":
+            return T(acc / T(L))
+        if red == "sum":
+            return acc
+        c = T(centre)
+        t = T(T(L) * c)
+        t = T(acc - t)
+        t = T(T(alpha) * t)
+        return T(c + t)
+    if red in ("minimum", "maximum"):
+        acc = T(vals[0])
+        for v in vals[1:]:
+            v = T(v)
+            if (v < acc) if red == "minimum" else (v > acc):
+                acc = v
+        return acc
+    if red == "kernelproduct":
+        acc = 0.0
+        for v, w in zip(vals, weights):
+            acc = acc + float(v) * w
+        return acc
+    if red == "life":
+        cnt = sum(1 for v in vals if v != 0)
+        birth, survive = rule
+        return int(cnt in (survive if centre != 0 else birth))
+    raise ValueError(red)
+
+
+def restated_map(parent, shape, R, offsets, bname, padval, halo, red, T, weights=None, rule=None, alpha=None,
+                 out_dtype=None):
+    """One map of the logical array held by `parent` (ring of width R when halo); updates the ring first
+    like the reference's gatherstencil! (update_boundary!) and returns the logical result."""
+    nd = parent.ndim
+    if halo and bname != "use":
+        _update_ring(parent, shape, R, bname, padval)
+    out = np.empty(shape, dtype=out_dtype or parent.dtype, order="F")
+    L = len(offsets)
+    for I in np.ndindex(*shape):
+        vals = []
+        for o in offsets:
+            J = tuple(I[d] + (o[d] if d < len(o) else 0) for d in range(nd))
+            if halo:
+                vals.append(parent[tuple(j + R for j in J)])
+            elif all(0 <= j < n for j, n in zip(J, shape)):
+                vals.append(parent[J])
+            elif bname == "remove":
+                vals.append(padval)
+            else:
+                vals.append(parent[tuple(_bound(bname, j, n) for j, n in zip(J, shape))])
+        centre = parent[tuple(i + R for i in I)] if halo else parent[I]
+        out[I] = _fold(red, vals, centre, T, L, weights, rule, alpha)
+    return out
+
+
+# ------------------------------------------------------------------ the matrix
+def _stencils(st):
+    return {
+        "Window1": (st.Window(1), 2), "Window2": (st.Window(2), 2), "Moore1": (st.Moore(1), 2),
+        "VonNeumann2": (st.VonNeumann(2), 2), "Circle2": (st.Circle(2), 2), "Cross1": (st.Cross(1), 2),
+        "Annulus2": (st.Annulus(2), 2), "Diamond1": (st.Diamond(1), 2), "Cardinal1": (st.Cardinal(1), 2),
+        "Ordinal1": (st.Ordinal(1), 2), "Rectangle": (st.Rectangle((-1, 2), (0, 1)), 2),
+        "Positional": (st.Positional((-1, 0), (1, 1), (0, -1)), 2),
+        "Moore1_3d": (st.Moore(1, 3), 3), "VonNeumann1_3d": (st.VonNeumann(1, 3), 3), "Cross1_3d": (st.Cross(1, 3), 3),
+        "Window2_1d": (st.Window(2, 1), 1),
+    }
+
+
+STENCILS = ["Window1", "Window2", "Moore1", "VonNeumann2", "Circle2", "Cross1", "Annulus2", "Diamond1", "Cardinal1",
+            "Ordinal1", "Rectangle", "Positional", "Moore1_3d", "VonNeumann1_3d", "Cross1_3d", "Window2_1d"]
+OPS = [("mean", "F64"), ("sum", "F32"), ("minimum", "F64"), ("maximum", "F32"), ("kernelproduct", "F64"),
+       ("diffusion", "F32"), ("life", "U8"), ("sum", "I64"), ("mean", "I64")]
+BCPADS = [(b, p) for p in ("cond", "halo_out", "halo_in") for b in ("remove", "wrap", "reflect", "use")
+          if not (b == "use" and p == "cond")]
+SIZES = {1: (11,), 2: (9, 8), 3: (6, 5, 5)}
+
+
+def _case_setup(st, abi, name, op, dt, rng):
+    stencil, nd = _stencils(st)[name]
+    npdt = {"F64": np.float64, "F32": np.float32, "U8": np.uint8, "I64": np.int64}[dt]
+    shape = SIZES[nd]
+    if dt in ("F64", "F32"):
+        a = (rng.random(shape) * 2 - 1).astype(npdt)
+    elif op == "life":
+        a = (rng.random(shape) < 0.4).astype(npdt)
+    else:
+        a = rng.integers(-5, 9, size=shape).astype(npdt)
+    T = {"F64": float, "F32": np.float32, "U8": int, "I64": int}[dt]
+    if op == "mean" and dt == "I64":
+        T = float
+    red = {"mean": st.mean, "sum": st.sum, "minimum": st.minimum, "maximum": st.maximum,
+           "kernelproduct": st.kernelproduct, "diffusion": st.Diffusion(0.1), "life": st.life}[op]
+    weights = None
+    if op == "kernelproduct":
+        weights = [float(x) for x in rng.standard_normal(len(stencil))]
+        stencil = st.Kernel(stencil, np.array(weights))
+    return np.asfortranarray(a), stencil, red, T, weights, getattr(abi, dt)
+
+
+def _padval(dt):
+    return 0.5 if dt in ("F64", "F32") else 3
+
+
+def _boundary(st, bname, dt):
+    return {"remove": st.Remove(_padval(dt)), "wrap": st.Wrap(), "reflect": st.Reflect(), "use": st.Use()}[bname]
+
+
+def _padding(st, pname):
+    return {"cond": st.Conditional(), "halo_out": st.Halo("out"), "halo_in": st.Halo("in")}[pname]
+
+
+def _restated(a, stencil, op, dt, bname, pname, T, weights, steps, out_dtype):
+    R = stencil.radius
+    offsets = (stencil.stencil if hasattr(stencil, "stencil") else stencil).offsets()
+    padval = T(_padval(dt)) if dt in ("F64", "F32") else _padval(dt)
+    halo = pname != "cond"
+    if pname == "halo_out":
+        parent = np.zeros(tuple(s + 2 * R for s in a.shape), dtype=a.dtype, order="F")
+        parent[tuple(slice(R, R + s) for s in a.shape)] = a
+    else:
+        parent = a.copy(order="F")
+    shape = tuple(s - 2 * R for s in parent.shape) if halo else parent.shape
+    kw = dict(weights=weights, rule=((3,), (2, 3)), alpha=0.1, out_dtype=out_dtype)
+    if steps == 0:
+        return restated_map(parent, shape, R, offsets, bname, padval, halo, op, T, **kw)
+    dest = parent.copy(order="F")
+    for _ in range(steps):
+        res = restated_map(parent, shape, R, offsets, bname, padval, halo, op, T, **kw)
+        dest[tuple(slice(R, R + n) for n in shape) if halo else ...] = res
+        parent, dest = dest, parent
+    return np.asfortranarray(parent[tuple(slice(R, R + n) for n in shape)] if halo else parent)
+
+
+@pytest.mark.parametrize("op,dt", OPS, ids=[f"{o}-{d}" for o, d in OPS])
+@pytest.mark.parametrize("name", STENCILS)
+def test_oracle_matches_restatement(st, orc, abi, name, op, dt):
+    ora = OracleBackend(st, orc, abi)
+    for bname, pname in BCPADS:
+        rng = np.random.default_rng(zlib.crc32(repr((name, op, dt, bname, pname)).encode()))
+        a, stencil, red, T, weights, code = _case_setup(st, abi, name, op, dt, rng)
+        if op == "life" and len(stencil) > 31:
+            continue
+        out_dtype = np.float64 if (op == "kernelproduct" or (op == "mean" and dt == "I64")) else None
+        want = _restated(a, stencil, op, dt, bname, pname, T, weights, 0, out_dtype)
+        got = ora.map(a, stencil, red, _boundary(st, bname, dt), _padding(st, pname), code=code)
+        assert got.dtype == want.dtype and got.shape == want.shape, (bname, pname, got.dtype, want.dtype)
+        assert got.tobytes(order="F") == want.tobytes(order="F"), (bname, pname)
+
+
+SWITCH_CASES = [("Moore1", "life", "U8"), ("VonNeumann1_3d", "diffusion", "F32"), ("Window1", "mean", "F64"),
+                ("Circle2", "sum", "F32"), ("Annulus2", "maximum", "F32")]
+
+
+@pytest.mark.parametrize("name,op,dt", SWITCH_CASES, ids=["-".join(c) for c in SWITCH_CASES])
+def test_oracle_switching_matches_restatement(st, orc, abi, name, op, dt):
+    """Three steps of A = mapstencil!(f, A) on a SwitchingStencilArray (src/gatherstencil.jl:77-83): each
+    step refreshes the source's ring (Halo) and writes the other parent's interior."""
+    ora = OracleBackend(st, orc, abi)
+    for bname, pname in BCPADS:
+        if pname == "halo_in":
+            continue      # a Halo{:in} switching pair shrinks nothing further; covered by halo_out
+        rng = np.random.default_rng(zlib.crc32(repr(("switch", name, op, dt, bname, pname)).encode()))
+        a, stencil, red, T, weights, code = _case_setup(st, abi, name, op, dt, rng)
+        want = _restated(a, stencil, op, dt, bname, pname, T, weights, 3, None)
+        got = ora.switch_map(a, stencil, red, _boundary(st, bname, dt), _padding(st, pname), steps=3, code=code)
+        assert got.tobytes(order="F") == want.tobytes(order="F"), (bname, pname)
