@@ -211,3 +211,81 @@ def test_oracle_switching_matches_restatement(st, orc, abi, name, op, dt):
         want = _restated(a, stencil, op, dt, bname, pname, T, weights, 3, None)
         got = ora.switch_map(a, stencil, red, _boundary(st, bname, dt), _padding(st, pname), steps=3, code=code)
         assert got.tobytes(order="F") == want.tobytes(order="F"), (bname, pname)
+
+
+# ------------------------------------------------------------------ scatterstencil!
+def restated_scatter(value, combine, dest, src, offsets, bname, T, c=None, weights=None):
+    """scatterstencil!(f, op, dest, source) run as the reference's pass schedule on one thread
+    (src/scatterstencil.jl:48-112): passes over columns j = pass, pass + (2R+1), ...; rows in order;
+    each source cell sends f(hood)[k] to (i + o0, j + o1) with Wrap mod1, Reflect 2 - i / 2n - i,
+    Remove / Use skipping targets outside."""
+    ny, nx = src.shape
+    R = max(max(abs(x) for x in o) for o in offsets)
+    stride = 2 * R + 1
+    out = dest.copy(order="F")
+    for pas in range(stride):
+        for j in range(pas, nx, stride):
+            for i in range(ny):
+                centre = T(src[i, j])
+                for k, o in enumerate(offsets):
+                    val = T(c) if value == "const" else (centre if value == "center" else T(centre * T(weights[k])))
+                    ti, tj = i + o[0], j + o[1]
+                    if bname == "wrap":
+                        ti, tj = ti % ny, tj % nx
+                    elif bname == "reflect":
+                        ti = -ti if ti < 0 else (2 * ny - 2 - ti if ti >= ny else ti)
+                        tj = -tj if tj < 0 else (2 * nx - 2 - tj if tj >= nx else tj)
+                    elif not (0 <= ti < ny and 0 <= tj < nx):
+                        continue
+                    cur = T(out[ti, tj])
+                    if combine == "add":
+                        out[ti, tj] = T(cur + val)
+                    elif combine == "max":
+                        out[ti, tj] = val if val > cur else cur
+                    else:
+                        out[ti, tj] = val if val < cur else cur
+    return out
+
+
+SCATTER_STENCILS = ["Moore1", "Moore2", "VonNeumann1", "Positional"]
+
+
+@pytest.mark.parametrize("dt", ["F64", "F32"])
+@pytest.mark.parametrize("sname", SCATTER_STENCILS)
+def test_oracle_scatter_matches_restatement(st, orc, abi, sname, dt):
+    import builtins
+    import operator
+    npdt = np.float64 if dt == "F64" else np.float32
+    T = float if dt == "F64" else np.float32
+    combines = {"add": operator.add, "max": builtins.max, "min": builtins.min}
+    for value in ("const", "center", "weighted"):
+        for cname, cop in combines.items():
+            for bname, pname in [(b, p) for b in ("remove", "wrap", "reflect", "use") for p in ("cond", "halo")
+                                 if not (b == "use" and p == "cond")]:
+                rng = np.random.default_rng(zlib.crc32(repr(("scatter", sname, dt, value, cname, bname, pname)).encode()))
+                stencil = {"Moore1": st.Moore(1), "Moore2": st.Moore(2), "VonNeumann1": st.VonNeumann(1),
+                           "Positional": st.Positional((-1, 0), (1, 1), (0, -1), (1, -1))}[sname]
+                shape = (7, 8) if sname != "Moore2" else (9, 11)
+                src = np.asfortranarray((rng.random(shape) * 2 - 1).astype(npdt))
+                dest0 = np.asfortranarray((rng.random(shape) * 2 - 1).astype(npdt))
+                weights = None
+                if value == "weighted":
+                    weights = rng.standard_normal(len(stencil))
+                    if dt == "F32":
+                        weights = weights.astype(np.float32)
+                    stencil = st.Kernel(stencil, weights, weight_dtype="f32" if dt == "F32" else "f64")
+                f = {"const": st.ScatterConst(0.3), "center": st.scatter_center, "weighted": st.scatter_weighted}[value]
+                bnd = _boundary(st, bname, dt)
+                R = stencil.radius
+                parent = src
+                pad = st.Conditional()
+                if pname == "halo":
+                    pad = st.Halo("out")
+                    parent = np.zeros((shape[0] + 2 * R, shape[1] + 2 * R), dtype=npdt, order="F")
+                    parent[R:-R, R:-R] = src
+                got = orc.scatter(f, cop, dest0.copy(order="F"), np.asfortranarray(parent), getattr(abi, dt), stencil,
+                                  bnd, pad)
+                offs = (stencil.stencil if hasattr(stencil, "stencil") else stencil).offsets()
+                want = restated_scatter(value, cname, dest0, src, offs, bname, T, c=0.3,
+                                        weights=None if weights is None else [float(w) for w in weights])
+                assert got.tobytes(order="F") == want.tobytes(order="F"), (value, cname, bname, pname)
