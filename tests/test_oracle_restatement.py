@@ -2,8 +2,10 @@
 against the C oracle on small seeded grids: 1D/2D/3D stencils (named shapes, Annulus, Rectangle,
 Positional) x boundaries (Remove, Wrap, Reflect, Use) x paddings (Conditional, Halo{:out}, Halo{:in}) x
 reductions (mean, sum, minimum, maximum, kernelproduct, Life, diffusion) in Float64, Float32, UInt8 and
-Int64, single maps and SwitchingStencilArray runs.  The reference's own goldens use integer-valued
-data; this pins the oracle's boundary handling and left-fold order on random floats as well.
+Int64, single maps and SwitchingStencilArray runs; scatterstencil! through the reference's pass schedule;
+maps over several arrays (sums of centre / sum / mean / kernelproduct / value terms).  The reference's
+own goldens use integer-valued data; this pins the oracle's boundary handling and fold order on random
+floats as well.
 
 Semantics restated here (reference file:line):
 * neighbour J = I + o: Conditional Remove reads padval outside the array (src/array.jl:133-135);
@@ -78,26 +80,31 @@ def restated_map(parent, shape, R, offsets, bname, padval, halo, red, T, weights
                  out_dtype=None):
     """One map of the logical array held by `parent` (ring of width R when halo); updates the ring first
     like the reference's gatherstencil! (update_boundary!) and returns the logical result."""
-    nd = parent.ndim
     if halo and bname != "use":
         _update_ring(parent, shape, R, bname, padval)
     out = np.empty(shape, dtype=out_dtype or parent.dtype, order="F")
     L = len(offsets)
     for I in np.ndindex(*shape):
-        vals = []
-        for o in offsets:
-            J = tuple(I[d] + (o[d] if d < len(o) else 0) for d in range(nd))
-            if halo:
-                vals.append(parent[tuple(j + R for j in J)])
-            elif all(0 <= j < n for j, n in zip(J, shape)):
-                vals.append(parent[J])
-            elif bname == "remove":
-                vals.append(padval)
-            else:
-                vals.append(parent[tuple(_bound(bname, j, n) for j, n in zip(J, shape))])
+        vals = _hood(parent, shape, R, offsets, bname, padval, halo, I)
         centre = parent[tuple(i + R for i in I)] if halo else parent[I]
         out[I] = _fold(red, vals, centre, T, L, weights, rule, alpha)
     return out
+
+
+def _hood(parent, shape, R, offsets, bname, padval, halo, I):
+    """The neighbour values of logical cell I in offset order."""
+    vals = []
+    for o in offsets:
+        J = tuple(I[d] + (o[d] if d < len(o) else 0) for d in range(parent.ndim))
+        if halo:
+            vals.append(parent[tuple(j + R for j in J)])
+        elif all(0 <= j < n for j, n in zip(J, shape)):
+            vals.append(parent[J])
+        elif bname == "remove":
+            vals.append(padval)
+        else:
+            vals.append(parent[tuple(_bound(bname, j, n) for j, n in zip(J, shape))])
+    return vals
 
 
 # ------------------------------------------------------------------ the matrix
@@ -289,3 +296,101 @@ def test_oracle_scatter_matches_restatement(st, orc, abi, sname, dt):
                 want = restated_scatter(value, cname, dest0, src, offs, bname, T, c=0.3,
                                         weights=None if weights is None else [float(w) for w in weights])
                 assert got.tobytes(order="F") == want.tobytes(order="F"), (value, cname, bname, pname)
+
+
+# ------------------------------------------------------------------ maps over several arrays
+def restated_terms(terms, args, T):
+    """dest[I] = t_1 + t_2 + ... (left to right), t_m = [alpha *] g_m with g_m the argument's centre,
+    neighbour sum / mean (fold from the first value), kernelproduct (from zero) or plain value at I; each
+    StencilArray argument's ring is refreshed first, as gatherstencil! does for every argument
+    (src/gatherstencil.jl:89-113)."""
+    prepared = []
+    shape = None
+    for (kind, alpha), arg in zip(terms, args):
+        if kind == "value":
+            prepared.append((kind, alpha, arg, None))
+            shape = shape or arg.shape
+            continue
+        parent, stencil, bname, padval, halo, weights = arg
+        R = stencil.radius
+        sh = tuple(n - 2 * R for n in parent.shape) if halo else parent.shape
+        if halo and bname != "use":
+            _update_ring(parent, sh, R, bname, padval)
+        shape = shape or sh
+        prepared.append((kind, alpha, arg, (sh, R, stencil.offsets())))
+    out = np.empty(shape, dtype=np.float64 if T is float else np.float32, order="F")
+    for I in np.ndindex(*shape):
+        acc = None
+        for kind, alpha, arg, geo in prepared:
+            if kind == "value":
+                g = T(arg[I])
+            else:
+                parent, _, bname, padval, halo, weights = arg
+                sh, R, offs = geo
+                if kind == "center":
+                    g = T(parent[tuple(i + R for i in I)] if halo else parent[I])
+                else:
+                    vals = [T(v) for v in _hood(parent, sh, R, offs, bname, padval, halo, I)]
+                    if kind == "kernelproduct":
+                        g = T(0)
+                        for v, w in zip(vals, weights):
+                            g = T(g + T(v * T(w)))
+                    else:
+                        g = vals[0]
+                        for v in vals[1:]:
+                            g = T(g + v)
+                        if kind == "mean":
+                            g = T(g / T(len(vals)))
+            if alpha is not None:
+                g = T(T(alpha) * g)
+            acc = g if acc is None else T(acc + g)
+        out[I] = acc
+    return out
+
+
+TERM_CASES = [
+    ("center+0.1sum", [("center", None), ("sum", 0.1)], ["Moore1", "Moore1"]),
+    ("mean+kdot", [("mean", None), ("kernelproduct", None)], ["Window2", "Cross1"]),
+    ("0.5center+sum+value", [("center", 0.5), ("sum", None), ("value", None)], ["Window1", "VonNeumann2", None]),
+    ("2mean-0.25mean", [("mean", 2.0), ("mean", -0.25)], ["Circle2", "Positional"]),
+]
+
+
+@pytest.mark.parametrize("dt", ["F64", "F32"])
+@pytest.mark.parametrize("cname,terms,snames", TERM_CASES, ids=[c[0] for c in TERM_CASES])
+def test_oracle_terms_match_restatement(st, orc, abi, cname, terms, snames, dt):
+    npdt = np.float64 if dt == "F64" else np.float32
+    T = float if dt == "F64" else np.float32
+    stencils = _stencils(st)
+    red = {"center": st.center, "sum": st.sum, "mean": st.mean, "kernelproduct": st.kernelproduct, "value": st.value}
+    f = st.Terms(*[red[k] if a is None else st.scaled(a, red[k]) for k, a in terms])
+    for combo in [("remove", "cond"), ("wrap", "cond"), ("reflect", "halo_out"), ("use", "halo_out"),
+                  ("wrap", "halo_out")]:
+        rng = np.random.default_rng(zlib.crc32(repr(("terms", cname, dt, combo)).encode()))
+        shape = (9, 8)
+        items, rargs = [], []
+        for (kind, _), sname in zip(terms, snames):
+            a = np.asfortranarray((rng.random(shape) * 2 - 1).astype(npdt))
+            if sname is None:
+                items.append(a)
+                rargs.append(a.copy(order="F"))
+                continue
+            stencil = stencils[sname][0]
+            weights = None
+            if kind == "kernelproduct":
+                weights = [float(x) for x in rng.standard_normal(len(stencil))]
+                if dt == "F32":
+                    weights = [float(np.float32(x)) for x in weights]
+                stencil = st.Kernel(stencil, np.array(weights, dtype=npdt), weight_dtype="f32" if dt == "F32" else "f64")
+            bname, pname = combo
+            R = stencil.radius
+            parent = a
+            if pname == "halo_out":
+                parent = np.zeros((shape[0] + 2 * R, shape[1] + 2 * R), dtype=npdt, order="F")
+                parent[R:-R, R:-R] = a
+            items.append((parent.copy(order="F"), stencil, _boundary(st, bname, dt), _padding(st, pname)))
+            base = stencil.stencil if hasattr(stencil, "stencil") else stencil
+            rargs.append((parent.copy(order="F"), base, bname, T(_padval(dt)), pname != "cond", weights))
+        got = orc.map_terms(f, items, getattr(abi, dt))
+        want = restated_terms(terms, rargs, T)
+        assert got.tobytes(order="F") == want.tobytes(order="F"), combo
