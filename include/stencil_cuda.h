@@ -49,7 +49,7 @@ typedef enum {
     STC_OK = 0,
     STC_ERR_SIZE_MISMATCH = -1,   /* "Source array sizes must match"  src/gatherstencil.jl:121 */
     STC_ERR_RADIUS = -2,          /* "stencil radius is larger than array axis"  src/array.jl:452, :578 */
-    STC_ERR_KERNEL_LENGTH = -3,   /* "Stencil length .. does not match kernel length"  src/stencils/kernel.jl:342 */
+    STC_ERR_KERNEL_LENGTH = -3,   /* "Stencil length .. does not match kernel length"  src/stencils/kernel.jl:114-116 */
     STC_ERR_UNSUPPORTED = -4,     /* shape / op / dtype / boundary combination not registered (a MethodError
                                      in the reference, e.g. Use with Conditional padding has no getneighbor) */
     STC_ERR_INVALID = -5,         /* malformed descriptor (null pointer, bad ndims, stride[0] != 1, ...), or a
@@ -72,7 +72,7 @@ typedef enum {
 /* ---- registered reductions `f` (the reference takes any Julia function) ----
  * MEAN     Statistics.mean(hood): left fold of `+` over the neighbours in offset order, / L
  * SUM      sum(hood): the same left fold
- * KDOT     kernelproduct(hood): s = 0; s += hood[i] * kernel[i] for i in 1:L   src/stencils/kernel.jl:264-270
+ * KDOT     kernelproduct(hood): s = 0; s += hood[i] * kernel[i] for i in 1:L   src/stencils/kernel.jl:37-43
  * MIN/MAX  minimum/maximum(hood): left fold of Julia's min/max (NaN-propagating, -0.0 < +0.0)
  * LIFE     outer-totalistic cellular automaton: n = count of nonzero neighbours, c = centre != 0,
  *          result = c ? (survive_mask >> n) & 1 : (birth_mask >> n) & 1   (B3/S23: birth 1<<3,
@@ -107,8 +107,8 @@ typedef struct {
 
 /* A stencil: the compile-time offsets Stencils.jl generates, lowered to a table.
  * offsets[k*ndims + d] is component d of offset k (component 0 along the contiguous axis), in
- * the reference's offset order (src/stencil.jl:224).  A stencil with fewer dims than the grid keeps
- * the trailing indices fixed (src/stencil.jl:220-223). */
+ * the reference's offset order (`offsets`, src/stencil.jl:73-75).  A stencil with fewer dims than the grid keeps
+ * the trailing indices fixed (src/stencil.jl:93-95). */
 typedef struct {
     int32_t ndims;            /* stencil dims, <= grid ndims */
     int32_t len;              /* L, 1..STC_MAX_LEN */
@@ -177,7 +177,7 @@ STC_API int stc_map_steps(const stc_grid* a, const stc_grid* b,
  * arithmetic is in the element type of the grids (Float64 or Float32, all the same; alpha is applied
  * in that type); sums fold in offset order exactly as stc_map.  Every StencilArray argument keeps its
  * own stencil, boundary and padding, and Halo arguments get update_boundary! first.  All logical
- * sizes must equal dest's (else STC_ERR_SIZE_MISMATCH, src/gatherstencil.jl:115-121). */
+ * sizes must equal dest's (else STC_ERR_SIZE_MISMATCH, src/gatherstencil.jl:118-124). */
 typedef enum {
     STC_TERM_CENTER = 0, STC_TERM_SUM = 1, STC_TERM_MEAN = 2, STC_TERM_KDOT = 3, STC_TERM_VALUE = 4
 } stc_term_kind;

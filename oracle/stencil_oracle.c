@@ -18,7 +18,7 @@
  *   gatherstencil!(f, ::SwitchingStencilArray) + switch   src/gatherstencil.jl:77-83, src/array.jl:610-611
  * The reductions fold left to right over the neighbours in offset order, as StaticArrays'
  * unrolled `_mapfoldl` does for `sum`/`mean`/`minimum`/`maximum` (first element taken as is,
- * `Base.reduce_first`), and as `kernelproduct` (src/stencils/kernel.jl:264-270) does from zero.
+ * `Base.reduce_first`), and as `kernelproduct` (src/stencils/kernel.jl:37-43) does from zero.
  * StaticArrays.jl and Statistics.jl (compat "1", Project.toml:29-30) are not vendored and no
  * Manifest pins their versions; the fold order above is their published algorithm.
  *

@@ -70,7 +70,7 @@ struct MapParams {
 
 // ---------------------------------------------------------------------------- reductions
 // Each op: Acc type; first(v) = Base.reduce_first; step(a, v, k); finish(a, centre).
-// KDOT starts from zero and steps every term (src/stencils/kernel.jl:264-270).
+// KDOT starts from zero and steps every term (src/stencils/kernel.jl:37-43).
 
 // Correctly rounded a / L with L a small positive integer.
 // Float32: q = RN(a*r), e = a - q*L (exact by FMA), q' = RN(q + e*r) with r = RN(1/L).  The host enables

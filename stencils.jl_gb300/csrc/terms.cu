@@ -175,7 +175,7 @@ int stc_map_terms(const stc_term* terms, int32_t nterms, const stc_grid* dst, in
             t.org += (int64_t)R * t.st[d];
             if (t.n[d] < 0) return STC_ERR_RADIUS;
         }
-        // every argument has the first one's logical size (src/gatherstencil.jl:115-121)
+        // every argument has the first one's logical size (src/gatherstencil.jl:118-124)
         for (int d = 0; d < 3; ++d) {
             if (m == 0) n[d] = t.n[d];
             else if (t.n[d] != n[d]) return STC_ERR_SIZE_MISMATCH;

@@ -35,7 +35,7 @@ class _Sum(Reduction):
 
 
 class _KernelProduct(Reduction):
-    """kernelproduct(hood): s = zero; s += hood[i] * kernel[i] (src/stencils/kernel.jl:264-270)."""
+    """kernelproduct(hood): s = zero; s += hood[i] * kernel[i] (src/stencils/kernel.jl:37-43)."""
     code, name = OP_KDOT, "kernelproduct"
 
 

@@ -27,7 +27,7 @@ def _box(R: int, N: int) -> Iterable[Offset]:
 
 
 class Stencil:
-    """Base of all shapes: `radius`, `ndims`, `offsets`, `len` (src/stencil.jl:145-233)."""
+    """Base of all shapes: `radius`, `ndims`, `offsets`, `len` (src/stencil.jl:17-98)."""
 
     shape_id = SHAPE_TABLE
 
@@ -52,14 +52,14 @@ class Stencil:
         return 2 * self.radius + 1
 
     def distances(self) -> Tuple[float, ...]:
-        """sqrt(sum(o^2)) per offset, in Float64 (src/stencil.jl:244-248)."""
+        """sqrt(sum(o^2)) per offset, in Float64 (src/stencil.jl:116-120)."""
         return tuple(math.sqrt(sum(c * c for c in o)) for o in self._offsets)
 
     def distance_zones(self) -> Tuple[int, ...]:
         return tuple(sum(abs(c) for c in o) for o in self._offsets)
 
     def indices(self, I: Sequence[int]) -> Tuple[Offset, ...]:
-        """Offsets added to I; trailing indices beyond the stencil's N are kept (src/stencil.jl:220-224)."""
+        """Offsets added to I; trailing indices beyond the stencil's N are kept (src/stencil.jl:93-96)."""
         I = tuple(I)
         n = self.ndims
         head, tail = I[:n], I[n:]
@@ -85,7 +85,7 @@ class Stencil:
 
 
 class _Shape(Stencil):
-    """Shapes defined by a predicate over the (2R+1)^N box (the `@stencil` macro, src/stencil.jl:363-405)."""
+    """Shapes defined by a predicate over the (2R+1)^N box (the `@stencil` macro, src/stencil.jl:235-277)."""
 
     def __init__(self, radius: int = 1, ndims: int = 2):
         if radius < 0 or ndims < 1:
@@ -240,7 +240,7 @@ class Annulus(Stencil):
 
 
 def _positional_radius(offsets: Sequence[Offset]) -> int:
-    """`maximum(map(maximum, O))` (src/stencils/positional.jl:225-227).
+    """`maximum(map(maximum, O))` (src/stencils/positional.jl:74-76).
 
     This is the reference's radius, NOT the largest absolute offset: a table whose offsets are all
     negative gets too small a radius and the reference's Conditional fast path then reads out of
@@ -250,7 +250,7 @@ def _positional_radius(offsets: Sequence[Offset]) -> int:
 
 
 class Positional(Stencil):
-    """Arbitrary offsets (src/stencils/positional.jl:182-217)."""
+    """Arbitrary offsets (src/stencils/positional.jl:31-56)."""
 
     def __init__(self, *offsets):
         if len(offsets) == 1 and isinstance(offsets[0], (tuple, list)) and offsets[0] \
@@ -262,7 +262,7 @@ class Positional(Stencil):
 
 
 class Rectangle(Stencil):
-    """Per-axis (lo, hi) box (src/stencils/rectangle.jl:188-223); radius is the max-abs bound."""
+    """Per-axis (lo, hi) box (src/stencils/rectangle.jl:13-45); radius is the max-abs bound."""
 
     def __init__(self, *bounds):
         if len(bounds) == 1 and isinstance(bounds[0][0], (tuple, list)):
@@ -306,7 +306,7 @@ def _default_names(base: Stencil):
 
 
 class Kernel(Stencil):
-    """A stencil plus weights (src/stencils/kernel.jl:320-343).
+    """A stencil plus weights (src/stencils/kernel.jl:93-116).
 
     `Kernel(stencil, weights)` takes weights in the stencil's offset order (a column-major
     flattening of an array); `Kernel(f, stencil)` computes `map(f, distances(stencil))`.
@@ -346,7 +346,7 @@ def stencil_radius_ok(st: Stencil) -> bool:
 
 
 class Layered:
-    """Several stencils used together over one array (src/stencils/layered.jl:13-60).
+    """Several stencils used together over one array (src/stencils/layered.jl:13-57).
 
     `Layered(a, b)` or `Layered(name=a, ...)`; layers may themselves be Layered.  The radius is the
     largest layer radius (so a Halo parent is padded for every layer); `offsets`, `indices`,

@@ -10,7 +10,7 @@ floats as well.
 Semantics restated here (reference file:line):
 * neighbour J = I + o: Conditional Remove reads padval outside the array (src/array.jl:133-135);
   Conditional Wrap / Reflect read the per-axis bounded index (src/array.jl:150-175: Wrap i +- s,
-  Reflect 2 - i and 2s - i in 1-based indices); Halo reads parent[J + R] (src/array.jl:186-188).
+  Reflect 2 - i and 2s - i in 1-based indices); Halo reads parent[J + R] (src/array.jl:347-349, 368-373).
 * update_boundary! before each map (src/array.jl:195-239): a ring cell of logical index J gets padval
   (Remove) or the interior value at the per-axis bounded index of J (Wrap / Reflect, `halo_val`);
   Use and Conditional leave the parent alone.

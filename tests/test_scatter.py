@@ -1,5 +1,5 @@
 """scatterstencil! (src/scatterstencil.jl:36-133): the oracle against the reference's own scatter tests
-(test/array.jl:403-511), and the GPU (stc_scatter, a deterministic gather) bit for bit against the
+(test/array.jl:385-493), and the GPU (stc_scatter, a deterministic gather) bit for bit against the
 oracle, which runs the reference's pass schedule on one thread.
 
 The reference's "directional scatter" test needs a two-array value function (water and elevation),
@@ -28,7 +28,7 @@ def _scatter_oracle(st, orc, abi, f, op, src, stencil, boundary=None, padding=No
 
 # ------------------------------------------------------------------ the reference's tests, on the oracle
 def test_basic_scatter_add(st, orc, abi):
-    """test/array.jl:404-420: each cell scatters 0.1 to its 8 Moore neighbours, Remove(0.0)."""
+    """test/array.jl:386-404: each cell scatters 0.1 to its 8 Moore neighbours, Remove(0.0)."""
     d = _scatter_oracle(st, orc, abi, st.ScatterConst(0.1), operator.add, np.ones((5, 5), order="F"), st.Moore(1))
     assert d[2, 2] == pytest.approx(0.8)
     assert d[0, 2] == pytest.approx(0.5) and d[2, 0] == pytest.approx(0.5)
@@ -36,7 +36,7 @@ def test_basic_scatter_add(st, orc, abi):
 
 
 def test_scatter_max(st, orc, abi):
-    """test/array.jl:422-434: each cell scatters its centre value; max keeps the largest."""
+    """test/array.jl:406-421: each cell scatters its centre value; max keeps the largest."""
     src = np.asfortranarray(np.array([[i + j for j in range(1, 6)] for i in range(1, 6)], dtype=np.float64))
     d = _scatter_oracle(st, orc, abi, st.scatter_center, builtins.max, src, st.Moore(1))
     assert d[2, 2] == 8.0
@@ -44,7 +44,7 @@ def test_scatter_max(st, orc, abi):
 
 
 def test_vonneumann_scatter(st, orc, abi):
-    """test/array.jl:458-472: 0.25 to each VonNeumann(1) neighbour."""
+    """test/array.jl:450-465: 0.25 to each VonNeumann(1) neighbour."""
     d = _scatter_oracle(st, orc, abi, st.ScatterConst(0.25), operator.add, np.ones((5, 5), order="F"),
                         st.VonNeumann(1))
     assert d[2, 2] == pytest.approx(1.0)
@@ -53,7 +53,7 @@ def test_vonneumann_scatter(st, orc, abi):
 
 
 def test_larger_radius_scatter(st, orc, abi):
-    """test/array.jl:474-484: Moore(2), 0.01 to each of 24 neighbours."""
+    """test/array.jl:467-478: Moore(2), 0.01 to each of 24 neighbours."""
     d = _scatter_oracle(st, orc, abi, st.ScatterConst(0.01), operator.add, np.ones((7, 7), order="F"), st.Moore(2))
     assert d[3, 3] == pytest.approx(0.24)
 
@@ -113,7 +113,7 @@ def test_scatter_gpu_matches_oracle(cuda, st, orc, abi, dt, shape, stencil_name,
 
 @pytest.mark.gpu
 def test_scatter_switching_on_gpu(cuda, st, orc, abi):
-    """test/array.jl:486-500 on the GPU: SwitchingStencilArray, 0.1 to each Moore(1) neighbour; the dest
+    """test/array.jl:480-492 on the GPU: SwitchingStencilArray, 0.1 to each Moore(1) neighbour; the dest
     is cleared first and the switched array returned."""
     import torch
     S = st.SwitchingStencilArray(st.to_device(np.ones((5, 5), order="F")), st.Moore(1), st.Remove(0.0))

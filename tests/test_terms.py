@@ -1,6 +1,6 @@
 """Maps over several arrays, mapstencil(f, A, B, ...) with f a registered sum of terms
 (src/gatherstencil.jl:84-113): the oracle against the reference's own multi-array tests
-(test/array.jl:310-366), and the GPU (stc_map_terms) bit for bit against the oracle.
+(test/array.jl:312-383), and the GPU (stc_map_terms) bit for bit against the oracle.
 
 All these sums run in the element type with every operation rounded, in the reference's left-to-right
 order, so parity is exact.
@@ -15,7 +15,7 @@ from _backends import GpuBackend
 
 # ------------------------------------------------------------------ the reference's tests, on the oracle
 def test_two_stencil_arrays_centers(st, orc, abi):
-    """test/array.jl:311-324: center(hood_a) + center(hood_b) == A .+ B."""
+    """test/array.jl:313-324: center(hood_a) + center(hood_b) == A .+ B."""
     A = np.asfortranarray(np.array([[1, 2, 3], [4, 5, 6], [7, 8, 9]], dtype=np.float64))
     B = np.asfortranarray(np.array([[10, 20, 30], [40, 50, 60], [70, 80, 90]], dtype=np.float64))
     f = st.Terms(st.center, st.center)
@@ -37,7 +37,7 @@ def test_two_stencil_arrays_neighbour_sums(st, orc, abi):
 
 
 def test_switching_with_stencil_array(st, orc, abi):
-    """test/array.jl:333-350: three steps of c + 0.1 * sum(neighbors(hood_r)) grow the centre."""
+    """test/array.jl:333-353: three steps of c + 0.1 * sum(neighbors(hood_r)) grow the centre."""
     mutable = np.asfortranarray(np.array([[0, 0, 0], [0, 1, 0], [0, 0, 0]], dtype=np.float64))
     readonly = np.asfortranarray(np.array([[1, 1, 1], [1, 0, 1], [1, 1, 1]], dtype=np.float64))
     f = st.Terms(st.center, st.scaled(0.1, st.sum))
@@ -54,7 +54,7 @@ def test_switching_with_stencil_array(st, orc, abi):
 
 
 def test_three_stencil_arrays(st, orc, abi):
-    """test/array.jl:352-365: center(a) + center(b) + center(c) == 6 on the interior."""
+    """test/array.jl:355-369: center(a) + center(b) + center(c) == 6 on the interior."""
     A, B, C = np.ones((5, 5), order="F"), 2 * np.ones((5, 5), order="F"), 3 * np.ones((5, 5), order="F")
     f = st.Terms(st.center, st.center, st.center)
     out = orc.map_terms(f, [(np.asfortranarray(a), st.Moore(1), st.Remove(0.0), st.Conditional()) for a in (A, B, C)],
@@ -63,7 +63,7 @@ def test_three_stencil_arrays(st, orc, abi):
 
 
 def test_mixed_stencil_and_plain_array(st, orc, abi):
-    """test/array.jl:367-378: center(hood_a) + b_val == A .+ B (B a plain array)."""
+    """test/array.jl:371-382: center(hood_a) + b_val == A .+ B (B a plain array)."""
     A = np.asfortranarray(np.array([[1, 2, 3], [4, 5, 6], [7, 8, 9]], dtype=np.float64))
     B = np.asfortranarray(np.array([[10, 20, 30], [40, 50, 60], [70, 80, 90]], dtype=np.float64))
     f = st.Terms(st.center, st.value)
