@@ -679,9 +679,9 @@ def run_terms(args):
 
 
 def run_scatter(args):
-    """scatterstencil!(f, +, dest, source): every cell scatters 0.1 to its Moore(1) neighbours, Float64
+    """scatterstencil!(f, +, dest, source): every cell scatters its centre value to its Moore(1) neighbours, Float64
     4096x4096, Remove(0), dest accumulated in place; bit-exact against the oracle (the reference's pass
-    schedule on one thread), which is also the CPU baseline."""
+    schedule, the columns of each pass on all host threads), which is also the CPU baseline."""
     import operator
     import torch
     entry.build()
@@ -705,16 +705,17 @@ def run_scatter(args):
     st.scatterstencil_(f, operator.add, d1, sa)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    thr = orc.max_threads()
     want = orc.scatter(f, operator.add, np.zeros((n, n), order="F"), src.copy(order="F"), A.F64, st.Moore(1),
-                       st.Remove(0.0), st.Conditional())
+                       st.Remove(0.0), st.Conditional(), nthreads=thr)
     cpu_s = time.perf_counter() - t0
     exact = st.to_host(d1).tobytes(order="F") == want.tobytes(order="F")
     line = {"workload": "scatterstencil! centre value to Moore(1) neighbours with +, Float64 4096x4096, Remove(0)",
             "metric": METRIC, "unit": UNIT, "value": args.steps * n * n / t / 1e9, "us_per_call": 1e6 * t / args.steps,
             "bit_exact_vs_oracle_one_call": bool(exact), "calls_accumulated": calls,
             "kernel": _kernel_roofline(prof, _peaks()["hbm_gbs"]),
-            "cpu_baseline": {"value": n * n / cpu_s / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": "one full scatter (the oracle's schedule is sequential)"}}
+            "cpu_baseline": {"value": n * n / cpu_s / 1e9, "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": "one full scatter, the columns of each pass on threads as the reference's"}}
     print(json.dumps(line), flush=True)
 
 

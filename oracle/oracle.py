@@ -40,7 +40,7 @@ def lib():
                                        C.c_int64, C.c_int, P(C.c_int)]
         _lib.orc_update_boundary.argtypes = [P(A.Grid), C.c_int, P(A.BcDesc)]
         _lib.orc_map_terms.argtypes = [P(A.TermDesc), C.c_int, P(A.Grid), C.c_int, C.c_int]
-        _lib.orc_scatter.argtypes = [P(A.Grid), P(A.Grid), P(A.StencilDesc), C.c_void_p, P(A.BcDesc)]
+        _lib.orc_scatter.argtypes = [P(A.Grid), P(A.Grid), P(A.StencilDesc), C.c_void_p, P(A.BcDesc), C.c_int]
         _lib.orc_mass.argtypes = [P(A.Grid), C.c_int, C.c_int]
         _lib.orc_mass.restype = C.c_double
         _lib.orc_result_dtype.argtypes = [C.c_int, C.c_int, C.c_int]
@@ -173,7 +173,8 @@ def map_terms(f, args, code: int, *, dst_padded: bool = False, nthreads: int = 1
     return dst
 
 
-def scatter(f, op, dest: np.ndarray, src: np.ndarray, code: int, stencil, boundary, padding) -> np.ndarray:
+def scatter(f, op, dest: np.ndarray, src: np.ndarray, code: int, stencil, boundary, padding, *,
+            nthreads: int = 1) -> np.ndarray:
     """scatterstencil!(f, op, dest, StencilArray(src parent, ...)) in place on `dest` (returned)."""
     from stencils_gb300 import _abi as A
     from stencils_gb300.scatter import ScatterOpDesc, _combine_code
@@ -184,5 +185,6 @@ def scatter(f, op, dest: np.ndarray, src: np.ndarray, code: int, stencil, bounda
     lst = A.LoweredStencil(stencil)
     bc = A.lower_bc(boundary, padding)
     gs, gd = _grid(src, code), _grid(dest, code)
-    _check(lib().orc_scatter(C.byref(gs), C.byref(gd), C.byref(lst.desc), C.byref(d), C.byref(bc)), "scatter")
+    _check(lib().orc_scatter(C.byref(gs), C.byref(gd), C.byref(lst.desc), C.byref(d), C.byref(bc), int(nthreads)),
+           "scatter")
     return dest

@@ -643,9 +643,11 @@ static int scatter_target(int boundary, int64_t t, int64_t n, int64_t* out) {
 #define ORC_SCATTER_BODY(T, ADDF, MAXF, MINF)                                                          \
     do {                                                                                               \
         T* d = (T*)dst->data;                                                                          \
-        for (int64_t p = 0; p < stride; ++p)                                                           \
-            for (int64_t j = p; j < nx; j += stride)                                                   \
-                for (int64_t i = 0; i < ny; ++i) {                                                     \
+        for (int64_t p = 0; p < stride; ++p) {                                                         \
+            const int64_t ncol = p < nx ? (nx - p + stride - 1) / stride : 0;                          \
+            _Pragma("omp parallel for num_threads(nt) schedule(static)")                               \
+            for (int64_t cj = 0; cj < ncol; ++cj)                                                      \
+                for (int64_t i = 0, j = p + cj * stride; i < ny; ++i) {                                \
                     const int64_t I[3] = {i, j, 0};                                                    \
                     const T c = (T)load_f(v.data, v.dt, poff(&v, I));                                  \
                     for (int k = 0; k < st->len; ++k) {                                                \
@@ -662,13 +664,19 @@ static int scatter_target(int boundary, int64_t t, int64_t n, int64_t* out) {
                         else *q = MINF(*q, val);                                                       \
                     }                                                                                  \
                 }                                                                                      \
+        }                                                                                              \
     } while (0)
 
 static double add_d(double a, double b) { return a + b; }
 static float add_f(float a, float b) { return a + b; }
 
+/* The reference runs the columns of one pass on threads (src/scatterstencil.jl:56-57).  Columns of a
+ * pass are 2R + 1 apart, so they write disjoint target columns and every dest cell still receives its
+ * contributions in (pass, row, offset) order: the threaded run equals the one-thread run bit for bit.
+ * Under Wrap that holds only when the column count is a multiple of 2R + 1 (otherwise the seam columns
+ * of one pass meet, a race in the reference); those grids run on one thread. */
 int orc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* st, const stc_scatter_op* op,
-                const stc_bc* bc) {
+                const stc_bc* bc, int nthreads) {
     if (!src || !dst || !st || !op || !bc || src->ndims != 2 || dst->ndims != 2 || st->ndims != 2)
         return STC_ERR_UNSUPPORTED;
     if (src->dtype != dst->dtype || (src->dtype != STC_F64 && src->dtype != STC_F32)) return STC_ERR_UNSUPPORTED;
@@ -682,6 +690,7 @@ int orc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* st,
     const int64_t ny = v.n[0], nx = v.n[1];
     if (dst->size[0] != ny || dst->size[1] != nx) return STC_ERR_SIZE_MISMATCH;
     const int64_t stride = 2 * (int64_t)st->radius + 1;
+    const int nt = (nthreads > 1 && (bc->boundary != STC_WRAP || nx % stride == 0)) ? nthreads : 1;
     if (src->dtype == STC_F64) ORC_SCATTER_BODY(double, add_d, jl_max, jl_min);
     else ORC_SCATTER_BODY(float, add_f, jl_maxf, jl_minf);
     return STC_OK;

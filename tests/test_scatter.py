@@ -1,6 +1,6 @@
 """scatterstencil! (src/scatterstencil.jl:36-133): the oracle against the reference's own scatter tests
 (test/array.jl:385-493), and the GPU (stc_scatter, a deterministic gather) bit for bit against the
-oracle, which runs the reference's pass schedule on one thread.
+oracle, which runs the reference's pass schedule (its delivery order is that of a one-thread run).
 
 The reference's "directional scatter" test needs a two-array value function (water and elevation),
 which is not a registered scatter value, so it is not restated here.
@@ -124,3 +124,25 @@ def test_scatter_switching_on_gpu(cuda, st, orc, abi):
     want = _scatter_oracle(st, orc, abi, st.ScatterConst(0.1), operator.add, np.ones((5, 5), order="F"), st.Moore(1))
     assert out[2, 2] == pytest.approx(0.8)
     assert np.array_equal(out, want)
+
+
+@pytest.mark.parametrize("bname,nx", [("remove0", 40), ("reflect", 41), ("wrap", 39), ("wrap", 40), ("use", 37)])
+def test_threaded_oracle_scatter_equals_one_thread(st, orc, abi, bname, nx):
+    """The oracle runs the columns of each pass on threads as the reference does (src/scatterstencil.jl:56-57);
+    the result equals the one-thread schedule bit for bit (Wrap with a column count that is not a multiple
+    of 2R + 1 runs on one thread)."""
+    rng = np.random.default_rng(zlib.crc32(repr(("threads", bname, nx)).encode()))
+    for stencil in (st.Moore(1), st.Moore(2), st.VonNeumann(2)):
+        src = np.asfortranarray(rng.random((33, nx)) * 2 - 1)
+        dest0 = np.asfortranarray(rng.random((33, nx)))
+        pad = st.Halo("out") if bname == "use" else st.Conditional()
+        one = _scatter_oracle(st, orc, abi, st.scatter_center, operator.add, src, stencil, _bc(st, bname), pad,
+                              dest=dest0.copy(order="F"))
+        R = stencil.radius
+        parent = src
+        if bname == "use":
+            parent = np.zeros((33 + 2 * R, nx + 2 * R), order="F")
+            parent[R:-R, R:-R] = src
+        many = orc.scatter(st.scatter_center, operator.add, dest0.copy(order="F"), np.asfortranarray(parent), abi.F64,
+                           stencil, _bc(st, bname), pad, nthreads=4)
+        assert many.tobytes(order="F") == one.tobytes(order="F")
