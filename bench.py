@@ -12,8 +12,9 @@ seed 2, Moore(1) B3/S23, Wrap boundary, Halo padding, SwitchingStencilArray: 100
              the initial grid host->device, runs the 1000 generations, and copies the result back.
 `roofline`   the dominant kernel's algorithmic bytes (1 B read + 1 B written per cell update) per
              launch over its CUDA-event launch time, against the measured HBM copy bandwidth.
-`cpu_baseline` the oracle (a C restatement of the reference's gather, OpenMP) on the host cores, on
-             a bounded number of generations of the same grid.
+`cpu_baseline` the oracle (a C restatement of the reference's gather, OpenMP; for Moore(1) Life on
+             UInt8 Halo parents the specialised loop the reference's compiled kernel amounts to) on
+             the host cores, on a bounded number of generations of the same grid.
 --impl reference times that CPU implementation as the reference arm (rank 0 only).
 N > 1 runs N independent replicas (the path has no data exchange between GPUs).
 """
@@ -198,14 +199,17 @@ def run_reference(args):
             times.append(dt)
     total = sum(times)
     value = args.steps * gens * SIDE * SIDE / total / 1e9
-    sample = f"{gens} generations of the 4096x4096 grid per step, OpenMP {threads} threads"
+    sample = (f"{gens} generations of the 4096x4096 grid per step, OpenMP {threads} threads, "
+              "specialised Moore(1) loop")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
             "config": CONFIG,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "CPU restatement of the reference's gather (oracle/stencil_oracle.c); the reference is "
+            "note": "CPU restatement of the reference's gather (oracle/stencil_oracle.c: a vectorised Moore(1) "
+                    "loop reading the Halo parent directly, as the reference's kernel specialised on the stencil "
+                    "type does); the reference is "
                     "Julia and no julia binary exists on this host"}
     print(json.dumps(line), flush=True)
     return 0
@@ -322,7 +326,8 @@ def run_gpu(args):
     if not args.no_cpu_baseline:
         rate, threads, gens, dt = cpu_life_rate(args.cpu_seconds)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{gens} generations of the 4096x4096 grid ({dt:.1f} s), oracle OpenMP {threads} threads"}
+               "sample": f"{gens} generations of the 4096x4096 grid ({dt:.1f} s), oracle OpenMP {threads} threads, "
+                         "specialised Moore(1) loop"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": CONFIG,

@@ -47,7 +47,14 @@ def lib():
         _lib.orc_max_threads.restype = C.c_int
         _lib.orc_f32_to_bf16.argtypes = [C.c_float]
         _lib.orc_f32_to_bf16.restype = C.c_uint16
+        _lib.orc_set_fast_paths.argtypes = [C.c_int]
     return _lib
+
+
+def set_fast_paths(on: bool):
+    """Enable (default) or disable the specialised Moore(1) Life path; with it off every map runs the
+    generic gather (the tests compare the two)."""
+    lib().orc_set_fast_paths(1 if on else 0)
 
 
 def max_threads() -> int:

@@ -441,12 +441,68 @@ int orc_update_boundary(const stc_grid* parent, int R, const stc_bc* bc) {
 
 /* ---------------------------------------------------------------- the map */
 
+/* Specialised restatement for Moore(1) outer-totalistic rules on UInt8 / Bool Halo parents: what the
+ * reference's compiled kernel does for that stencil type (compile-time offsets, neighbours read straight
+ * from the padded parent, src/array.jl:347-349), so the CPU baseline is not a generic interpreter.
+ * Integer counts, so the result equals the generic gather's bit for bit (tested). */
+static int g_fast_paths = 1;
+void orc_set_fast_paths(int on) { g_fast_paths = on != 0; }
+
+static int is_moore1_table(const stc_stencil* st) {
+    if (st->ndims != 2 || st->len != 8 || st->radius != 1) return 0;
+    int seen = 0;
+    for (int k = 0; k < 8; ++k) {
+        const int x = st->offsets[2 * k], y = st->offsets[2 * k + 1];
+        if (x < -1 || x > 1 || y < -1 || y > 1 || (x == 0 && y == 0)) return 0;
+        const int bit = 1 << ((y + 1) * 3 + (x + 1));
+        if (seen & bit) return 0;
+        seen |= bit;
+    }
+    return 1;
+}
+
+static int life_fast(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_op* op, int nthreads) {
+    const int64_t n0 = src->size[0] - 2, n1 = src->size[1] - 2;
+    const int64_t ps = src->stride[1], ds = dst->stride[1];
+    const uint8_t* P = (const uint8_t*)src->data;
+    uint8_t* D = (uint8_t*)dst->data + (dst_padded ? 1 + ds : 0);
+    /* next state = bit n of the survive (alive) or birth (dead) mask, n = live neighbours (0..8): formed
+     * as nine compare / select steps on 8-bit lanes so the row loop vectorises */
+    uint8_t bm[9], sm[9];
+    for (int v = 0; v < 9; ++v) {
+        bm[v] = (uint8_t)((op->birth_mask >> v) & 1u);
+        sm[v] = (uint8_t)((op->survive_mask >> v) & 1u);
+    }
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+    for (int64_t j = 0; j < n1; ++j) {
+        const uint8_t* up = P + j * ps;     /* parent row of logical j - 1 */
+        const uint8_t* mid = up + ps;
+        const uint8_t* dn = mid + ps;
+        uint8_t* out = D + j * ds;
+        for (int64_t i = 0; i < n0; ++i) {
+            const uint8_t n = (uint8_t)((up[i] != 0) + (up[i + 1] != 0) + (up[i + 2] != 0) + (mid[i] != 0) +
+                                        (mid[i + 2] != 0) + (dn[i] != 0) + (dn[i + 1] != 0) + (dn[i + 2] != 0));
+            const uint8_t alive = mid[i + 1] != 0;
+            uint8_t o = 0;
+#pragma GCC unroll 9
+            for (int v = 0; v < 9; ++v) o |= (uint8_t)((n == v) & (alive ? sm[v] : bm[v]));
+            out[i] = o;
+        }
+    }
+    return STC_OK;
+}
+
 int orc_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
             const stc_op* op, const stc_bc* bc, int nthreads) {
     int rc = check_args(src, dst, dst_padded, st, op, bc);
     if (rc) return rc;
     rc = orc_update_boundary(src, st->radius, bc);
     if (rc) return rc;
+    if (g_fast_paths && op->code == STC_OP_LIFE && src->ndims == 2 && src->dtype == dst->dtype &&
+        (src->dtype == STC_U8 || src->dtype == STC_BOOL) && bc->padding != STC_CONDITIONAL &&
+        is_moore1_table(st) && src->stride[0] == 1 && (dst->size[0] <= 1 || dst->stride[0] == 1))
+        return life_fast(src, dst, dst_padded, op, nthreads);
     gather_t g;
     rc = make_view(src, st->radius, bc->padding, &g.src);
     if (rc) return rc;

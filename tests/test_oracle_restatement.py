@@ -394,3 +394,30 @@ def test_oracle_terms_match_restatement(st, orc, abi, cname, terms, snames, dt):
         got = orc.map_terms(f, items, getattr(abi, dt))
         want = restated_terms(terms, rargs, T)
         assert got.tobytes(order="F") == want.tobytes(order="F"), combo
+
+
+# ------------------------------------------------------------------ the oracle's specialised Life path
+@pytest.mark.parametrize("bname,pname", [("wrap", "halo_out"), ("remove", "halo_out"), ("reflect", "halo_in"),
+                                         ("use", "halo_in"), ("wrap", "halo_in")])
+def test_oracle_life_fast_path_equals_generic(st, orc, abi, bname, pname):
+    """Moore(1) Life on UInt8 / Bool Halo parents runs a specialised loop in the oracle (the CPU baseline);
+    it equals the generic gather bit for bit for several rules, sizes and step counts."""
+    ora = OracleBackend(st, orc, abi)
+    rules = [st.life, st.LifeRule((3, 6), (2, 3)), st.LifeRule((1,), (0, 8)), st.LifeRule((), (1, 2, 3, 4))]
+    for shape, steps in (((37, 29), 5), ((8, 70), 3), ((64, 64), 12)):
+        for rule in rules:
+            for dt in ("U8", "BOOL"):
+                rng = np.random.default_rng(zlib.crc32(repr((bname, pname, shape, rule.name, dt)).encode()))
+                a = np.asfortranarray((rng.random(shape) < 0.35).astype(np.uint8))
+                bnd = st.Remove(0) if bname == "remove" else _boundary(st, bname, "U8")
+                code = getattr(abi, dt)
+                try:
+                    orc.set_fast_paths(False)
+                    want = ora.switch_map(a, st.Moore(1), rule, bnd, _padding(st, pname), steps=steps, code=code)
+                    want1 = ora.map(a, st.Moore(1), rule, bnd, _padding(st, pname), code=code)
+                finally:
+                    orc.set_fast_paths(True)
+                got = ora.switch_map(a, st.Moore(1), rule, bnd, _padding(st, pname), steps=steps, code=code)
+                got1 = ora.map(a, st.Moore(1), rule, bnd, _padding(st, pname), code=code)
+                assert got.tobytes(order="F") == want.tobytes(order="F"), (shape, rule.name, dt)
+                assert got1.tobytes(order="F") == want1.tobytes(order="F"), (shape, rule.name, dt)
