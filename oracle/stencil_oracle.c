@@ -527,19 +527,73 @@ int orc_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_
         for (int d = 0; d < dst->ndims; ++d) dorg += (int64_t)st->radius * dst->stride[d];
     int64_t dst_st[3] = {dst->stride[0], dst->ndims > 1 ? dst->stride[1] : 0, dst->ndims > 2 ? dst->stride[2] : 0};
     if (nthreads < 1) nthreads = 1;
+    /* Float64 / Float32 sum and mean: cells whose whole stencil lies inside the parent's valid data
+     * (every cell under Halo padding; the interior under Conditional, the reference's unchecked corner
+     * path, src/array.jl:104-114) fold straight from the parent through constant linear offsets, in
+     * table order and the same arithmetic as the generic gather; the other cells take the gather. */
+    const int ffast = g_fast_paths && (op->code == STC_OP_MEAN || op->code == STC_OP_SUM) &&
+                      acc == src->dtype && dst->dtype == src->dtype &&
+                      (src->dtype == STC_F64 || src->dtype == STC_F32) && st->len <= STC_MAX_LEN;
+    int64_t lo[3] = {0, 0, 0}, hi[3] = {n0, n1, n2};
+    int64_t* loff = NULL;
+    if (ffast) {
+        loff = (int64_t*)malloc(sizeof(int64_t) * (size_t)st->len);
+        for (int k = 0; k < st->len; ++k) {
+            loff[k] = 0;
+            for (int d = 0; d < st->ndims; ++d) loff[k] += (int64_t)st->offsets[k * st->ndims + d] * g.src.st[d];
+        }
+        if (!halo)
+            for (int d = 0; d < g.src.nd; ++d) {
+                lo[d] = st->radius;
+                hi[d] = g.src.n[d] - st->radius;
+            }
+    }
 #pragma omp parallel num_threads(nthreads)
     {
         val_t* vals = (val_t*)malloc(sizeof(val_t) * (size_t)st->len);
 #pragma omp for schedule(static)
-        for (int64_t lin = 0; lin < total; ++lin) {
-            int64_t I[3] = {lin % n0, (lin / n0) % n1, lin / (n0 * n1)};
-            val_t centre;
-            gather(&g, I, vals, &centre);
-            int64_t doff = dorg + I[0] * dst_st[0] + I[1] * dst_st[1] + I[2] * dst_st[2];
-            reduce_store(op, st, acc, src->dtype, vals, centre, dst->data, dst->dtype, doff);
+        for (int64_t row = 0; row < n1 * n2; ++row) {
+            const int64_t y = row % n1, z = row / n1;
+            const int inner_row = ffast && y >= lo[1] && y < hi[1] && z >= lo[2] && z < hi[2];
+            const int64_t xa = inner_row ? (lo[0] < n0 ? lo[0] : n0) : n0;
+            const int64_t xb = inner_row ? (hi[0] > xa ? hi[0] : xa) : n0;
+            for (int64_t x = 0; x < n0; ++x) {
+                if (x == xa && xb > xa) {
+                    const int64_t I0[3] = {xa, y, z};
+                    const int64_t pb = poff(&g.src, I0);
+                    const int64_t db = dorg + xa * dst_st[0] + y * dst_st[1] + z * dst_st[2];
+                    const int L = st->len;
+                    if (src->dtype == STC_F64) {
+                        const double* sp = (const double*)g.src.data + pb;
+                        double* dp = (double*)dst->data + db;
+                        for (int64_t t = 0; t < xb - xa; ++t) {
+                            double a = sp[t + loff[0]];
+                            for (int k = 1; k < L; ++k) a = a + sp[t + loff[k]];
+                            dp[t] = op->code == STC_OP_MEAN ? a / (double)L : a;
+                        }
+                    } else {
+                        const float* sp = (const float*)g.src.data + pb;
+                        float* dp = (float*)dst->data + db;
+                        for (int64_t t = 0; t < xb - xa; ++t) {
+                            float a = sp[t + loff[0]];
+                            for (int k = 1; k < L; ++k) a = a + sp[t + loff[k]];
+                            dp[t] = op->code == STC_OP_MEAN ? a / (float)L : a;
+                        }
+                    }
+                    x = xb - 1;
+                    continue;
+                }
+                int64_t I[3] = {x, y, z};
+                val_t centre;
+                gather(&g, I, vals, &centre);
+                int64_t doff = dorg + I[0] * dst_st[0] + I[1] * dst_st[1] + I[2] * dst_st[2];
+                reduce_store(op, st, acc, src->dtype, vals, centre, dst->data, dst->dtype, doff);
+            }
         }
         free(vals);
     }
+    free(loff);
+    (void)total;
     return STC_OK;
 }
 

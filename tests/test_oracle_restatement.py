@@ -421,3 +421,32 @@ def test_oracle_life_fast_path_equals_generic(st, orc, abi, bname, pname):
                 got1 = ora.map(a, st.Moore(1), rule, bnd, _padding(st, pname), code=code)
                 assert got.tobytes(order="F") == want.tobytes(order="F"), (shape, rule.name, dt)
                 assert got1.tobytes(order="F") == want1.tobytes(order="F"), (shape, rule.name, dt)
+
+
+@pytest.mark.parametrize("name", ["Window1", "Circle2", "Annulus2", "Rectangle", "Positional", "Moore1_3d",
+                                  "Cross1_3d", "Window2_1d"])
+@pytest.mark.parametrize("op,dt", [("mean", "F64"), ("sum", "F64"), ("mean", "F32"), ("sum", "F32")])
+def test_oracle_float_fast_path_equals_generic(st, orc, abi, name, op, dt):
+    """Float sum / mean fold the interior (Conditional) or every cell (Halo) from constant offsets in the
+    oracle; that equals the generic gather bit for bit, including grids too small to have an interior."""
+    ora = OracleBackend(st, orc, abi)
+    stencil, nd = _stencils(st)[name]
+    sizes = {1: [(11,), (3,)], 2: [(9, 8), (3, 40), (40, 3)], 3: [(6, 5, 5), (3, 9, 4)]}[nd]
+    red = st.mean if op == "mean" else st.sum
+    npdt = np.float64 if dt == "F64" else np.float32
+    for shape in sizes:
+        if min(shape) <= stencil.radius:
+            continue
+        for bname, pname in BCPADS:
+            if pname == "halo_in" and min(shape) <= 3 * stencil.radius:
+                continue
+            rng = np.random.default_rng(zlib.crc32(repr(("ffast", name, op, dt, shape, bname, pname)).encode()))
+            a = np.asfortranarray((rng.random(shape) * 2 - 1).astype(npdt))
+            bnd, pad = _boundary(st, bname, dt), _padding(st, pname)
+            try:
+                orc.set_fast_paths(False)
+                want = ora.map(a, stencil, red, bnd, pad, code=getattr(abi, dt))
+            finally:
+                orc.set_fast_paths(True)
+            got = ora.map(a, stencil, red, bnd, pad, code=getattr(abi, dt))
+            assert got.tobytes(order="F") == want.tobytes(order="F"), (shape, bname, pname)
