@@ -740,9 +740,11 @@ int orc_map_terms(const stc_term* terms, int nterms, const stc_grid* dst, int ds
 }
 
 /* ---------------------------------------------------------------- scatterstencil! */
-/* scatterstencil!(f, op, dest, source) (src/scatterstencil.jl:36-74) run on one thread: passes over the
- * columns j = p, p + stride, ... (stride = 2R + 1), rows in order, offsets in order; targets mapped by
- * _scatter_to! (src/scatterstencil.jl:76-112): Remove/Use skip, Wrap mod1, Reflect 2 - i / 2n - i. */
+/* scatterstencil!(f, op, dest, source) (src/scatterstencil.jl:36-74): passes over the columns
+ * j = p, p + stride, ... (stride = 2R + 1), rows in order, offsets in order; targets mapped by
+ * _scatter_to! (src/scatterstencil.jl:76-112): Remove/Use skip, Wrap mod1, Reflect 2 - i / 2n - i.
+ * The columns of a pass may run on threads (orc_scatter below); every dest cell still receives its
+ * contributions in the order of a one-thread run. */
 static int scatter_target(int boundary, int64_t t, int64_t n, int64_t* out) {
     if (t >= 0 && t < n) { *out = t; return 1; }
     if (boundary == STC_WRAP) { int64_t m = t % n; *out = m < 0 ? m + n : m; return 1; }
