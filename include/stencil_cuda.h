@@ -76,7 +76,10 @@ typedef enum {
  * MIN/MAX  minimum/maximum(hood): left fold of Julia's min/max (NaN-propagating, -0.0 < +0.0)
  * LIFE     outer-totalistic cellular automaton: n = count of nonzero neighbours, c = centre != 0,
  *          result = c ? (survive_mask >> n) & 1 : (birth_mask >> n) & 1   (B3/S23: birth 1<<3,
- *          survive 1<<2 | 1<<3).  Equals the closure `s == 3 || (c && s == 2)` on 0/1 states.
+ *          survive 1<<2 | 1<<3).  Equals the closure `s == 3 || (c && s == 2)` on 0/1 states, which is
+ *          what a Bool grid or a 0/1 integer grid holds.  On other states it differs from a closure
+ *          over s = sum(hood): the library counts nonzero neighbours (a 2 counts as one live cell),
+ *          and results are 0/1.  A caller whose states are not 0/1 must keep the reference path.
  * DIFFUSE  c + alpha * (sum(hood) - L * c): explicit diffusion step, c = centre value.
  */
 typedef enum {
@@ -231,19 +234,22 @@ STC_API int stc_update_boundary(const stc_grid* parent, int32_t radius, const st
 STC_API int stc_mass(const stc_grid* g, int32_t radius, const stc_bc* bc, double* out_total, void* stream);
 
 /* ---- no-allocation variant of the bit-packed Life path ----
- * No counterpart in the reference.  For callers that must not allocate device memory: code running
- * inside a stream capture or a caller-managed memory pool, embedded hosts that own every byte of the
- * device, or a Julia/C host whose allocator must stay the only one.  It runs the same bit-packed,
- * temporally blocked Moore(1) kernels as stc_map_steps, but keeps the packed copies in a fixed
- * device array that is part of the library image (4 MiB, held on every GPU that loads the library
- * until the process exits) instead of allocating them.  The caller still owns and passes both
- * parents.  Accepts only what that path runs: a 2D Moore(1) LIFE rule, UInt8/Bool/Int32/Int64
- * grids whose width is a multiple of 32 cells, Wrap or Remove(0), at most 4096*4096 logical cells
- * (larger grids return STC_ERR_TOO_LARGE, other inputs STC_ERR_UNSUPPORTED).  The first call on a
- * device looks up the array's device address, so make that first call before any stream capture.
- * All calls share the one array: calls whose work overlaps on the GPU (other streams, other host
- * threads) race and must be serialised by the caller.  Same results and parent switching as
- * stc_map_steps. */
+ * No counterpart in the reference.  For callers that cannot allocate device memory: a host whose
+ * device memory is all handed out by its own allocator (a Julia CUDA.jl memory pool, a framework's
+ * caching allocator, an embedded host that reserved every byte of the device up front), where an
+ * allocation by the library would fail or would take memory the owner has already promised
+ * elsewhere.  It runs the same bit-packed, temporally blocked Moore(1) kernels as stc_map_steps, but
+ * keeps the packed copies in a fixed device array that is part of the library image (4 MiB, held on
+ * every GPU that loads the library until the process exits) instead of allocating them.  The caller
+ * still owns and passes both parents.  Accepts only what that path runs: a 2D Moore(1) LIFE rule,
+ * UInt8/Bool/Int32/Int64 grids whose width is a multiple of 32 cells and at most 16384 cells,
+ * Wrap or Remove(0), at most 4096*4096 logical cells (larger grids return STC_ERR_TOO_LARGE, other
+ * inputs STC_ERR_UNSUPPORTED).  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it for the life of the process, so make that first call before
+ * any stream capture; a device reset (cudaDeviceReset) after it is not supported.  All calls share
+ * the one array and each call overwrites it: calls whose work overlaps on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  The call waits for its stream
+ * before returning.  Same results and parent switching as stc_map_steps. */
 STC_API int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, const stc_stencil* stencil,
                                    const stc_op* op, const stc_bc* bc, int64_t nsteps,
                                    int32_t* out_src_is_b, void* stream);

@@ -742,6 +742,7 @@ namespace stc {
 
 constexpr int64_t kNoAllocMaxCells = 4096ll * 4096ll;
 constexpr int64_t kNoAllocWords = kNoAllocMaxCells / 32;   // one packed copy
+constexpr int kNoAllocMaxWords = 512;                        // widest row: 512 words = 16384 cells
 
 // Two packed copies, 4 MiB in total.  In host code this name is only a stand-in for the device
 // array; the kernels get its device address from cudaGetSymbolAddress.
@@ -811,6 +812,9 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     if (!wrap && !remove0) return STC_ERR_UNSUPPORTED;
     const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
     if (n0 < 32 || n0 % 32 != 0 || n1 < 1) return STC_ERR_UNSUPPORTED;
+    // life_block_kernel gives each thread at most one packed column once rows are 64 words or wider, so
+    // rows wider than the CTA (kNoAllocMaxWords words) would leave columns uncomputed
+    if (n0 / 32 > kNoAllocMaxWords || n0 / 32 > life_threads()) return STC_ERR_UNSUPPORTED;
     if (n0 * n1 > kNoAllocMaxCells) return STC_ERR_TOO_LARGE;
     if (nsteps > 0 && a->data == b->data) return STC_ERR_INVALID;
     if (nsteps == 0) {

@@ -1,7 +1,8 @@
 """Extract the golden vectors of Stencils.jl's own test suite into reference_goldens.json.
 
-Run in a checkout that has the reference mounted (it reads the Julia test files as text; nothing
-is executed):  python tests/golden/extract_reference_goldens.py [/path/to/Stencils.jl]
+Run where a Stencils.jl checkout is available (it reads the Julia test files as text; nothing is
+executed):  python tests/golden/extract_reference_goldens.py /path/to/Stencils.jl
+(or set STENCILS_JL_DIR to that path).
 
 Each entry records the reference file and line range it came from.  Matrix literals are
 parsed from Julia syntax (`[a b; c d]` or rows on separate lines) into row-major nested lists,
@@ -10,11 +11,11 @@ so entry[i][j] is the Julia element [i+1, j+1].  The parity tests read only the 
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 from pathlib import Path
 
-DEFAULT_REF = "/root/reference"
 
 # (name, file, first line, last line, kind)  kind: matrix | vector | tuples
 ENTRIES = [
@@ -97,7 +98,10 @@ def parse_matrix(src: str):
     return rows
 
 
-def main(ref_dir: str = DEFAULT_REF):
+def main(ref_dir: str | None = None):
+    ref_dir = ref_dir or os.environ.get("STENCILS_JL_DIR")
+    if not ref_dir:
+        raise SystemExit("usage: extract_reference_goldens.py /path/to/Stencils.jl (or set STENCILS_JL_DIR)")
     ref = Path(ref_dir)
     out = {"source": "Stencils.jl test suite (test/array.jl, test/stencils.jl), extracted as text",
            "entries": {}}
