@@ -142,6 +142,17 @@ typedef struct {
 } stc_bc;
 
 /* stc_map flags */
+/* stc_map_steps flag, BFloat16 / Float16 state only: the precision mode for long runs of 16-bit state.
+ * The state is held in memory in the 16-bit type, but between the rounding points it stays Float32.
+ * With s = 1..n the steps of this call and m = 4 * floor((n - 1) / 4), the state after step s <= m is
+ * rounded to the storage type only when s is a multiple of 4: BFloat16 stochastically (round up with
+ * probability equal to the distance from the value below; the bits come from a hash of the cell's
+ * column-major linear index and s, so results are deterministic), Float16 to nearest.  The last n - m
+ * steps (1 to 4) run as separate maps, each rounded to nearest.  Results then differ from n maps of
+ * 16-bit state (each rounded to nearest); their error against an FP64 run is stated by the benchmark.
+ * Runs the temporally blocked 3D path only (3D VonNeumann(1,3) diffusion / mean, Cross(1,3) sum, Wrap
+ * or Remove); other runs return STC_ERR_UNSUPPORTED.  Ignored for Float32 / Float64 / integer state. */
+#define STC_KEEP_F32 2u
 #define STC_ASYNC 1u          /* do not synchronise the stream before returning (errors from the
                                  kernel's own checks surface at the next synchronising call) */
 
@@ -149,6 +160,12 @@ typedef struct {
 STC_API int         stc_abi_version(void);
 STC_API const char* stc_strerror(int status);
 STC_API int         stc_last_cuda_error(void);              /* the cudaError_t behind the last STC_ERR_CUDA */
+/* No counterpart in the reference.  Multi-step runs that work on an internal padded pair (3D grids:
+ * the temporally blocked path and the edge-patching path) keep that pair's device memory per device
+ * for the next run (stream-ordered: a run on another stream waits for the previous one to finish
+ * with it).  This frees it on every device, waiting for the device; STC_ERR_BUSY if a run on another
+ * host thread holds it at that moment. */
+STC_API int         stc_release_workspace(void);
 
 /* Output element type the reference would infer for (op, source dtype, weight dtype)
  * (Base._return_type, src/gatherstencil.jl:41-56), or a negative status. */

@@ -141,6 +141,86 @@ def map_steps(a: np.ndarray, b: np.ndarray, code: int, stencil, red, boundary, p
     return bool(out.value)
 
 
+def _mix32(x: np.ndarray) -> np.ndarray:
+    """The "lowbias32" integer hash (Chris Wellons' hash-prospector, public domain), on uint32 arrays."""
+    x = x.astype(np.uint32, copy=True)
+    x ^= x >> np.uint32(16)
+    x *= np.uint32(0x7FEB352D)
+    x ^= x >> np.uint32(15)
+    x *= np.uint32(0x846CA68B)
+    x ^= x >> np.uint32(16)
+    return x
+
+
+def bf16_stochastic_bits(x: np.ndarray, step: int) -> np.ndarray:
+    """Float32 (column-major array of the logical grid) -> BFloat16 bits, rounded stochastically: the 16
+    bits below the BFloat16 mantissa are added to the magnitude and the sum truncated; the bits are the
+    hash of the cell's column-major linear index and `step`.  Infinities and NaN round to nearest."""
+    with np.errstate(over="ignore"):
+        b = np.asfortranarray(x, dtype=np.float32).ravel(order="F").view(np.uint32)
+        lin = np.arange(b.size, dtype=np.uint64)
+        s = _mix32(np.array([np.uint32(step) ^ np.uint32(0x9E3779B9)], dtype=np.uint32))[0]
+        h = _mix32((lin & np.uint64(0xFFFFFFFF)).astype(np.uint32) ^
+                   _mix32((lin >> np.uint64(32)).astype(np.uint32) ^ s))
+        special = (b & np.uint32(0x7F800000)) == np.uint32(0x7F800000)
+        r = ((b + (h & np.uint32(0xFFFF))) >> np.uint32(16)).astype(np.uint16)
+    if special.any():
+        r[special] = f32_to_bf16_bits(b[special].view(np.float32))
+    return r.reshape(x.shape, order="F")
+
+
+def keep_f32_schedule(nsteps: int):
+    """The STC_KEEP_F32 precision mode's rounding schedule: m = 4 * floor((nsteps - 1) / 4) steps in
+    passes of 4 held in Float32 and rounded at the end of each pass, then the last nsteps - m steps as
+    separate maps (each rounded to nearest).  Returns (number of 4-step passes, per-step tail length)."""
+    m = (nsteps - 1) // 4 * 4 if nsteps >= 1 else 0
+    return m // 4, nsteps - m
+
+
+def map_steps_keep_f32(a: np.ndarray, code: int, stencil, red, boundary, padding, nsteps: int,
+                       *, nthreads: int = 1):
+    """The STC_KEEP_F32 precision mode restated: 16-bit state `a` (BFloat16 bits or float16).  Each 4-step
+    pass runs as Float32 maps (the oracle's Float32 gather) from the widened state, then rounds (BFloat16
+    stochastically with the step number reached, Float16 to nearest); the tail steps are plain 16-bit
+    maps.  Returns (state n, state n - 1) as 16-bit arrays of a's type."""
+    from stencils_gb300 import _abi as A
+    from stencils_gb300.boundary import Remove
+    if code == A.BF16:
+        widen = bf16_bits_to_f32
+
+        def narrow(x, s):
+            return bf16_stochastic_bits(x, s)
+    else:
+        def widen(x):
+            return np.asarray(x, dtype=np.float16).astype(np.float32)
+
+        def narrow(x, s):
+            return x.astype(np.float16)
+    bnd = boundary
+    if isinstance(boundary, Remove):
+        # the padval a 16-bit grid's getneighbor returns, widened
+        if code == A.BF16:
+            pv = widen(f32_to_bf16_bits(np.array([np.float32(boundary.padval)])))
+        else:
+            pv = np.float32(np.float16(boundary.padval))
+        bnd = Remove(float(np.asarray(pv).ravel()[0]))
+    passes, tail = keep_f32_schedule(nsteps)
+    cur = np.asfortranarray(a)
+    prev = cur
+    step = 0
+    for _ in range(passes):
+        pa = np.asfortranarray(widen(cur))
+        pb = pa.copy(order="F")
+        in_b = map_steps(pa, pb, A.F32, stencil, red, bnd, padding, 4, nthreads=nthreads)
+        step += 4
+        prev, cur = cur, np.asfortranarray(narrow(pb if in_b else pa, step))
+    if tail:
+        pa, pb = cur.copy(order="F"), cur.copy(order="F")
+        in_b = map_steps(pa, pb, code, stencil, red, boundary, padding, tail, nthreads=nthreads)
+        cur, prev = (pb, pa) if in_b else (pa, pb)
+    return cur, prev
+
+
 def update_boundary(parent: np.ndarray, code: int, radius: int, boundary, padding):
     from stencils_gb300 import _abi as A
     bc = A.lower_bc(boundary, padding)

@@ -23,6 +23,7 @@ STATUS_NAMES = {
 }
 STC_ERR_BUSY = -10
 STC_ASYNC = 1
+STC_KEEP_F32 = 2
 
 F64, F32, BF16, F16, U8, BOOL, I32, I64 = range(8)
 DTYPE_SIZE = {F64: 8, F32: 4, BF16: 2, F16: 2, U8: 1, BOOL: 1, I32: 4, I64: 8}

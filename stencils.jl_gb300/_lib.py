@@ -47,6 +47,7 @@ def load(path: str | Path | None = None):
         "stc_abi_version": ([], C.c_int),
         "stc_strerror": ([C.c_int], C.c_char_p),
         "stc_last_cuda_error": ([], C.c_int),
+        "stc_release_workspace": ([], C.c_int),
         "stc_result_dtype": ([C.c_int32, C.c_int32, C.c_int32], C.c_int),
         "stc_map": ([P(A.Grid), P(A.Grid), C.c_int32, P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc), vp, C.c_uint32],
                     C.c_int),

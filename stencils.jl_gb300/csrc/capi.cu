@@ -106,6 +106,76 @@ int device_ctx(DeviceCtx** out) {
     return STC_OK;
 }
 
+// ---------------------------------------------------------------------------- workspace
+// The internal padded pair of a multi-step run is large (two grids plus their rings), and mapping fresh
+// pages for it on every call costs as much as tens of steps.  Each device keeps the last one; a call
+// takes it in stream order (waiting on the event the previous user recorded) and gives it back with an
+// event on its own stream, so calls on different streams never overlap on it.  A call that finds it
+// taken by another host thread gets a private stream-ordered allocation instead.
+struct Workspace {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+};
+static std::mutex g_ws_mu;
+static Workspace g_ws[64];
+
+int workspace_acquire(size_t bytes, cudaStream_t s, void** out, bool* cached) {
+    *out = nullptr;
+    *cached = false;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) return STC_ERR_NO_DEVICE;
+    {
+        std::lock_guard<std::mutex> g(g_ws_mu);
+        Workspace& w = g_ws[dev];
+        if (!w.busy) {
+            if (w.bytes < bytes) {
+                if (w.ptr) {
+                    cudaFree(w.ptr);   // waits for the device: no earlier user still reads it
+                    w.ptr = nullptr;
+                    w.bytes = 0;
+                }
+                if (cudaMalloc(&w.ptr, bytes) != cudaSuccess) {
+                    cudaGetLastError();
+                    w.ptr = nullptr;
+                    return STC_ERR_CUDA;
+                }
+                w.bytes = bytes;
+            } else if (w.done) {
+                if ((e = cudaStreamWaitEvent(s, w.done, 0)) != cudaSuccess) return cuda_fail(e);
+            }
+            if (!w.done && (e = cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming)) != cudaSuccess)
+                return cuda_fail(e);
+            w.busy = true;
+            *out = w.ptr;
+            *cached = true;
+            return STC_OK;
+        }
+    }
+    if ((e = cudaMallocAsync(out, bytes, s)) != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return STC_ERR_CUDA;
+    }
+    return STC_OK;
+}
+
+void workspace_release(void* ptr, bool cached, cudaStream_t s) {
+    if (!ptr) return;
+    if (!cached) {
+        cudaFreeAsync(ptr, s);
+        return;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> g(g_ws_mu);
+    Workspace& w = g_ws[dev];
+    cudaEventRecord(w.done, s);
+    w.busy = false;
+}
+
 // reads and clears the status word after the stream finished
 static int finish_sync(cudaStream_t s, DeviceCtx* ctx) {
     cudaError_t e = cudaStreamSynchronize(s);
@@ -490,6 +560,24 @@ const char* stc_strerror(int status) {
 
 int stc_last_cuda_error(void) { return g_last_cuda_error; }
 
+int stc_release_workspace(void) {
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return STC_ERR_NO_DEVICE;
+    std::lock_guard<std::mutex> g(g_ws_mu);
+    int rc = STC_OK;
+    for (int d = 0; d < 64; ++d) {
+        Workspace& w = g_ws[d];
+        if (!w.ptr && !w.done) continue;
+        if (w.busy) { rc = STC_ERR_BUSY; continue; }
+        cudaSetDevice(d);
+        if (w.ptr) cudaFree(w.ptr);   // waits for the device
+        if (w.done) cudaEventDestroy(w.done);
+        w = Workspace{};
+    }
+    cudaSetDevice(cur);
+    return rc;
+}
+
 int stc_result_dtype(int32_t opcode, int32_t src_dtype, int32_t weight_dtype) {
     return result_dtype(opcode, src_dtype, weight_dtype);
 }
@@ -541,10 +629,8 @@ static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil*
     const int64_t pitch = (lead + P[0] + line - 1) / line * line;
     const size_t cells = (size_t)pitch * P[1] * P[2];
     void* mem = nullptr;
-    if (cudaMallocAsync(&mem, 2 * cells * es, s) != cudaSuccess) {
-        cudaGetLastError();
-        return STC_OK;
-    }
+    bool cached = false;
+    if (workspace_acquire(2 * cells * es, s, &mem, &cached) != STC_OK) return STC_OK;
     stc_grid pg[2];
     for (int i = 0; i < 2; ++i) {
         pg[i].ndims = 3;
@@ -574,7 +660,7 @@ static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil*
     const bool res_in_b = (nsteps & 1) != 0;
     if (!rc) rc = launch_grid_copy(&pg[cur], inner, res_in_b ? b : a, 0, n, s);
     if (!rc) rc = launch_grid_copy(&pg[1 - cur], inner, res_in_b ? a : b, 0, n, s);
-    cudaFreeAsync(mem, s);
+    workspace_release(mem, cached, s);
     if (rc) return rc;
     *src_is_b = res_in_b ? 1 : 0;
     *done = nsteps;
@@ -600,14 +686,16 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
     // Cellular automata on bit-packable grids run temporally blocked on a packed copy.
     rc = life_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
     if (rc) return rc;
-    // 3D grids whose boundary needs edge patching: steps on an internal Halo-padded pair
+    // 3D radius-1 float maps: k steps per pass over HBM (temporal blocking)
     if (done == 0) {
-        rc = padded_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
+        rc = tb3d_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, flags, &done);
         if (rc) return rc;
     }
-    // 3D radius-1 float maps: k steps per pass over HBM; the last step runs below
+    if (done == 0 && (flags & STC_KEEP_F32) && (a->dtype == STC_BF16 || a->dtype == STC_F16) && nsteps > 0)
+        return STC_ERR_UNSUPPORTED;
+    // other 3D grids whose boundary needs edge patching: steps on an internal Halo-padded pair
     if (done == 0) {
-        rc = tb3d_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
+        rc = padded_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
         if (rc) return rc;
     }
     const stc_grid* grids[2] = {a, b};

@@ -49,6 +49,11 @@ int device_ctx(DeviceCtx** out);
 // remembers the CUDA error behind an STC_ERR_CUDA
 int cuda_fail(cudaError_t e);
 
+// The per-device workspace kept between multi-step runs, in stream order on `s`: a buffer of at least
+// `bytes`; *cached tells workspace_release whether it is the kept one or a private allocation.
+int workspace_acquire(size_t bytes, cudaStream_t s, void** out, bool* cached);
+void workspace_release(void* ptr, bool cached, cudaStream_t s);
+
 int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
                  const stc_op* op, const stc_bc* bc);
 // true if the two grids' element byte ranges intersect

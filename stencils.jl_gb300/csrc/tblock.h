@@ -5,12 +5,16 @@
 
 namespace stc {
 
-// If the run qualifies (3D grid, radius-1 registered shape, float state, Wrap or Remove, TMA-aligned
-// parents), advance nsteps-1 steps with the temporally blocked kernel, leaving state nsteps-1 in the
-// parent where the reference's loop leaves it; the caller runs the last step with the per-step map.
-// *done reports the steps run (0 when the path does not apply).
+// True if the blocked kernel is compiled for (grid, stencil, op, boundary): a 3D grid, a radius-1
+// VonNeumann / Cross table with a registered float op, Wrap or Remove.
+bool tb3d_applies(const stc_grid* a, const stc_stencil* st, const stc_op* op, const stc_bc* bc);
+
+// If the run qualifies, advance all nsteps on an internal padded pair (blocked passes of 4 steps, the
+// last 1 to 4 steps as per-step maps) and copy states n and n - 1 to the parents where the reference's
+// loop leaves them.  *done reports the steps run (0 when the path does not apply); with STC_KEEP_F32
+// in `flags` a run the path cannot take returns STC_ERR_UNSUPPORTED instead.
 int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op,
                    const stc_bc* bc, int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx,
-                   int64_t* done);
+                   uint32_t flags, int64_t* done);
 
 }  // namespace stc

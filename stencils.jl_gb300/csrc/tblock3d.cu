@@ -1,17 +1,33 @@
-// tblock3d.cu — K6: temporally blocked multi-step maps on 3D grids (plane-streaming wavefront).
+// tblock3d.cu — K6: temporally blocked multi-step maps on 3D grids.
 //
-// Replaces k iterations of  A = mapstencil!(f, A)  (src/gatherstencil.jl:77-83) for 3D radius-1
-// stencils with float state (the 7-point diffusion of VonNeumann(1,3), 3D Moore/Cross(1) means/sums).
+// Replaces k iterations of  A = mapstencil!(f, A)  (src/gatherstencil.jl:77-83, switch src/array.jl:610-611)
+// for 3D radius-1 stencils whose off-plane taps are the two cells straight above and below
+// (VonNeumann(1,3): the 7-point diffusion; Cross(1,3)), on Float32 / BFloat16 / Float16 state.
 //
-// A CTA owns an (x, y) tile of TX x TY outputs with a k-cell halo and a chunk of z.  It streams the
-// input planes z0-k .. z1+k-1 through a TMA ring in shared memory (cp.async.bulk.tensor.3d, one plane
-// per copy, no multicast); after plane i lands, time level t = 1..k computes its plane i-t from the
-// three level t-1 planes below, above and at it (each level keeps a 4-plane ring, skewed so one
-// barrier per plane suffices), the valid region
-// shrinking by one cell per level in x and y.  Level k planes are the outputs.  So one pass over HBM
-// advances the grid k steps.  Wrap: cells outside the grid are wrapped copies and evolve like the
-// cells they copy.  Remove: cells outside the grid are reset to padval at every level.  Every cell
-// update is the single-map fold (same op structs), so results are bit-identical to k separate maps.
+// The run works on an internal pair of parents padded by a ring of H cells (H >= k, the row start of
+// the interior on a 128-byte line); before every pass the ring holds the boundary's values (Wrap:
+// refreshed by K2 from the interior; Remove: padval, written once), so every input box arrives whole
+// from TMA and no tile needs patching.
+//
+// A CTA owns an (x, y) tile of TX x TY outputs plus a halo (XH columns, K rows each side: the plane
+// box BX x BY) and a chunk of ZC output planes.  Input planes stream through a 5-slot TMA ring
+// (cp.async.bulk.tensor.3d, one plane per copy, two planes ahead, no multicast).  At iteration i time
+// level t computes its plane i - t from level t-1's planes i-t-1, i-t and i-t+1.  Every thread owns
+// the same 4 x RPT block of each level's plane.  The plane at a cell's own height is read from shared
+// memory (two parity buffers per level, so one barrier per iteration suffices); the plane below is the
+// one the thread read there in the previous iteration (kept in registers); the plane above is the one
+// the level below produced earlier in the same iteration (registers).  Left / right neighbours arrive
+// by warp shuffle from the adjacent lanes.  Level 1 reads the input planes from the ring.  Level k
+// writes the tile's interior to the other parent, so a pass over HBM advances the grid k steps.
+//
+// Cells outside the grid: with Wrap the ring is the periodic extension of the grid and evolves
+// exactly like the cells it copies (same inputs, same fold), so nothing is patched; with Remove every
+// level writes padval there, as getneighbor does at every step (src/array.jl:129-137).  Every cell
+// update is the single-map fold (the same op structs over Float32, widened as in K1's vector path), and
+// in the default mode every level is rounded to the storage type, so results are bit-identical to k
+// separate maps.  With STC_KEEP_F32 (16-bit storage only) the levels inside a pass stay Float32 and
+// only the states written to memory are rounded (BFloat16: stochastically, from a hash of the cell and
+// the step; Float16: to nearest), on the schedule the header states.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -27,29 +43,32 @@
 
 namespace stc {
 
-constexpr int kTbThreads = 256;
-constexpr int kTbRing0 = 6;          // input planes in flight (prefetch distance kTbRing0 - 3)
-constexpr int kTbRingL = 4;          // planes kept per intermediate time level (skewed schedule)
+constexpr int kTbK = 4;              // time levels per pass (the STC_KEEP_F32 rounding period)
+constexpr int kTbRPT = 2;            // rows per thread block (the thread owns 4 x kTbRPT cells of a plane)
+constexpr int kTbRing = 5;           // input planes resident: i-2 .. i (read) and i+1, i+2 (in flight)
+constexpr int kTbMaxThreads = 512;   // 16 warps: four per SM sub-partition, up to 128 registers each
 
-struct TBParams {
-    CUtensorMap tmap;                // source parent (rank 3)
-    const void* src;
-    void* dst;
-    int64_t sst[3], dstr[3];
-    int64_t src_org, dst_org;
-    int64_t n[3];
-    int32_t hx[3];                   // parent coordinate of logical 0 (R for Halo parents)
-    int32_t boundary;
-    double padf;
-    int32_t k;                       // time levels this launch
-    int32_t TX, TY, ZC;              // tile and z chunk
-    int32_t PX, PY, padl;            // plane box (x pitch, rows) and shared-memory x of the tile's first column
-    int32_t ntx, nty, nzc;
-    uint32_t plane_bytes;            // PX*PY*sizeof(T) rounded to 128
-    int32_t fixup;                   // edge tiles need patching after TMA
-    int32_t aligned;                 // dst rows allow 4-element vector stores (vector variant)
+struct TB6Params {
+    CUtensorMap tmap;                // the padded source buffer (rank 3), box BX x BY x 1
+    void* dst;                       // padded destination buffer: element of logical (0, 0, 0)
+    int64_t dstr1, dstr2;            // its strides (elements)
+    int32_t n[3];                    // logical size
+    int32_t H;                       // ring width: tensor-map coordinate of logical 0 on every axis
+    int32_t BX, BY;                  // plane box
+    int32_t XH;                      // box column of the tile's first column (>= kTbK, multiple of 4)
+    int32_t TX, TY, ZC;              // tile and z chunk (outputs)
+    int32_t ntx, nty, nzc, nitems;
+    int32_t remove;                  // Remove: cells outside the grid hold padval at every level
+    float padf;                      // padval in the storage type, widened
+    uint32_t box_bytes;              // BX * BY * sizeof(T): one TMA transaction
+    uint32_t ring_off, ring_stride;  // byte offset of ring slot 0 and bytes per slot
+    uint32_t lvl_off, lvl_stride;    // byte offset of the level buffers and bytes per buffer
+    uint32_t bar_off;
+    int32_t keep_f32;                // levels inside the pass stay Float32 (16-bit storage only)
+    int32_t stochastic;              // round the stored level stochastically (BFloat16)
+    uint32_t round_step;             // the step number the stored level reaches (hash input)
     int32_t* status;
-    // op parameters (the fields the op structs read)
+    // the fields the op structs read
     int32_t L;
     uint32_t birth, survive;
     double alpha;
@@ -58,116 +77,68 @@ struct TBParams {
     float Lf;
     double Ld;
     float alpha_f;
-    float wf[64];
-    double w[64];
 };
 
-template <class T> __device__ __forceinline__ T tb_pad(const TBParams& p);
-template <> __device__ __forceinline__ float tb_pad<float>(const TBParams& p) { return (float)p.padf; }
-template <> __device__ __forceinline__ __nv_bfloat16 tb_pad<__nv_bfloat16>(const TBParams& p) {
-    return __float2bfloat16_rn((float)p.padf);
-}
-template <> __device__ __forceinline__ double tb_pad<double>(const TBParams& p) { return p.padf; }
+// The same op over Float32 inputs and Float32 results (no rounding to the storage type).
+template <class Op> struct TbF32;
+template <class Tin, class Tout> struct TbF32<OpDiffuse<Tin, Tout, float>> { using type = OpDiffuse<float, float, float>; };
+template <class Tin, class Tout> struct TbF32<OpMean<Tin, Tout, float>> { using type = OpMean<float, float, float>; };
+template <class Tin, class Tout> struct TbF32<OpSumF<Tin, Tout, float>> { using type = OpSumF<float, float, float>; };
 
-// i mod n for the coordinates a plane box can hold (within one period of the grid almost always)
-__device__ __forceinline__ int64_t tb_wrap(int64_t i, int64_t n) {
-    if (i < 0) i += n;
-    else if (i >= n) i -= n;
-    if (i < 0 || i >= n) {
-        i %= n;
-        if (i < 0) i += n;
-    }
-    return i;
-}
-
-// value of logical cell (x, y, z) for the plane fix-up (Conditional rules: Wrap or Remove)
-template <class T>
-__device__ __forceinline__ T tb_load(const TBParams& p, int64_t x, int64_t y, int64_t z) {
-    const T* s = (const T*)p.src;
-    if (p.boundary == STC_WRAP) {
-        x = tb_wrap(x, p.n[0]);
-        y = tb_wrap(y, p.n[1]);
-        z = tb_wrap(z, p.n[2]);
-    } else if (x < 0 || x >= p.n[0] || y < 0 || y >= p.n[1] || z < 0 || z >= p.n[2]) {
-        return tb_pad<T>(p);
-    }
-    return s[p.src_org + x + y * p.sst[1] + z * p.sst[2]];
-}
-
-// fold of one cell from the three planes below / at / above it (compile-time table, table order)
-template <class T, class Op, class Sh>
-__device__ __forceinline__ T tb_fold(const T* lo, const T* mid, const T* hi, int PX, const TBParams& p) {
-    constexpr auto Tb = Sh::table;
-    typename Op::A acc;
-    if constexpr (Op::kZeroInit) acc = Op::first(mid[0], 0);
-#pragma unroll
-    for (int k = 0; k < Sh::L; ++k) {
-        const T* pl = Tb.o[k].z < 0 ? lo : (Tb.o[k].z > 0 ? hi : mid);
-        const T v = pl[Tb.o[k].y * PX + Tb.o[k].x];
-        if (!Op::kZeroInit && k == 0) acc = Op::first(v, 0);
-        else acc = Op::step(acc, v, k, p);
-    }
-    return Op::finish(acc, mid[0], p);
-}
-
-// ---- vector columns: one work item = 4 adjacent cells of a plane row ----
-// Which rows of the three planes the generated table reads, and whether it reads their x - 1 / x + 1,
-// as compile-time bit masks over the 3 x 3 (z, y) rows (scalars, so device code never reads the table
-// object itself at run time).
-template <class Sh> struct TbUse {
-    static constexpr unsigned mask(int dx, bool any_x) {
-        unsigned m = 0;
+// Which taps the table has, as compile-time scalars: the kernel reads only those neighbours.
+template <class Sh> struct TbTaps {
+    static constexpr bool has(int x, int y, int z) {
         for (int k = 0; k < Sh::L; ++k)
-            if (any_x || Sh::table.o[k].x == dx) m |= 1u << ((Sh::table.o[k].z + 1) * 3 + (Sh::table.o[k].y + 1));
-        return m;
+            if (Sh::table.o[k].x == x && Sh::table.o[k].y == y && Sh::table.o[k].z == z) return true;
+        return false;
     }
-    static constexpr unsigned kRows = mask(0, true), kXm = mask(-1, false), kXp = mask(1, false);
+    static constexpr bool only_axis_taps() {
+        for (int k = 0; k < Sh::L; ++k) {
+            const auto o = Sh::table.o[k];
+            const int nz = (o.x != 0) + (o.y != 0) + (o.z != 0);
+            if (nz > 1 || o.x < -1 || o.x > 1 || o.y < -1 || o.y > 1 || o.z < -1 || o.z > 1) return false;
+        }
+        return true;
+    }
+    static constexpr bool kUp = has(0, -1, 0), kDn = has(0, 1, 0), kLf = has(-1, 0, 0), kRt = has(1, 0, 0);
 };
 
-template <class V, class T> __device__ __forceinline__ V tb_widen(T v) {
-    if constexpr (std::is_same_v<V, T>) return v;
-    else return __bfloat162float(v);
+template <class T> __device__ __forceinline__ float tb_widen(T v) {
+    if constexpr (std::is_same_v<T, float>) return v;
+    else if constexpr (std::is_same_v<T, __nv_bfloat16>) return __bfloat162float(v);
+    else return __half2float(v);
 }
 
-// The four cells at shared-memory offset `off` (a multiple of 4) of level t from the level t-1 planes
-// (lo, mid, hi): each row the table reads is one aligned 4-wide load, plus its left / right neighbour
-// when the table reads x - 1 / x + 1; every cell then folds its neighbours in table order (the same
-// op structs, widened as in the single-map vector kernel), so results equal the one-cell fold.
-template <class T, class Op, class Sh>
-__device__ __forceinline__ void tb_cells4(const T* lo, const T* mid, const T* hi, int off, int PX, const TBParams& p,
-                                          T* res) {
-    using OpV = typename Widen<Op>::type;
-    using V = std::conditional_t<Widen<Op>::kWide, float, T>;
-    using U = TbUse<Sh>;
-    constexpr auto Tb = Sh::table;
-    V w[3][3][6];
-#pragma unroll
-    for (int zz = 0; zz < 3; ++zz)
-#pragma unroll
-        for (int yy = 0; yy < 3; ++yy) {
-            const unsigned bit = 1u << (zz * 3 + yy);
-            if (!(U::kRows & bit)) continue;
-            const T* pl = (zz == 0 ? lo : (zz == 1 ? mid : hi)) + off + (yy - 1) * PX;
-            ld_row_vec<T, V, 4>(pl, &w[zz][yy][1]);
-            if (U::kXm & bit) w[zz][yy][0] = tb_widen<V>(pl[-1]);
-            if (U::kXp & bit) w[zz][yy][5] = tb_widen<V>(pl[4]);
-        }
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        typename OpV::A acc;
-        if constexpr (OpV::kZeroInit) acc = OpV::first(V(0), 0);
-#pragma unroll
-        for (int k = 0; k < Sh::L; ++k) {
-            const V v = w[Tb.o[k].z + 1][Tb.o[k].y + 1][c + Tb.o[k].x + 1];
-            if (!OpV::kZeroInit && k == 0) acc = OpV::first(v, 0);
-            else acc = OpV::step(acc, v, k, p);
-        }
-        if (!(U::kRows & (1u << 4))) w[1][1][c + 1] = tb_widen<V>(mid[off + c]);   // the centre, if the table skipped it
-        res[c] = OpV::finish(acc, w[1][1][c + 1], p);
-    }
+// "lowbias32" integer hash (Chris Wellons, hash-prospector; public domain): the source of the rounding
+// bits of the stochastic BFloat16 store.  The oracle computes the same bits.
+__device__ __forceinline__ uint32_t tb_mix(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
 }
 
-template <class T> __device__ __forceinline__ void sts4(T* d, const T* v) {
+// Float32 -> BFloat16 with stochastic rounding: the 16 bits below the BFloat16 mantissa are added to
+// the magnitude and the sum truncated, so a value rounds up with probability equal to its distance
+// from the value below.  The 16 random bits come from the hash of the cell's column-major linear index
+// and the step number.  Infinities and NaN round to nearest.
+__device__ __forceinline__ __nv_bfloat16 tb_bf16_stochastic(float v, uint64_t lin, uint32_t step) {
+    uint32_t b = __float_as_uint(v);
+    if ((b & 0x7f800000u) == 0x7f800000u) return __float2bfloat16_rn(v);
+    const uint32_t h = tb_mix((uint32_t)lin ^ tb_mix((uint32_t)(lin >> 32) ^ tb_mix(step ^ 0x9e3779b9u)));
+    b += h & 0xffffu;
+    return __ushort_as_bfloat16((unsigned short)(b >> 16));
+}
+
+template <class T> __device__ __forceinline__ T tb_round(float v);
+template <> __device__ __forceinline__ float tb_round<float>(float v) { return v; }
+template <> __device__ __forceinline__ __nv_bfloat16 tb_round<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ __half tb_round<__half>(float v) { return __float2half_rn(v); }
+
+// four consecutive storage elements (an aligned 4 * sizeof(T)-byte group) to global memory
+template <class T> __device__ __forceinline__ void tb_st4(T* d, const T* v) {
     if constexpr (sizeof(T) == 4) {
         uint4 u;
         memcpy(&u, v, 16);
@@ -179,187 +150,320 @@ template <class T> __device__ __forceinline__ void sts4(T* d, const T* v) {
     }
 }
 
-template <class T, class Op, class Sh, bool VEC>
-__global__ void __launch_bounds__(kTbThreads) tb3d_kernel(const __grid_constant__ TBParams p) {
-    extern __shared__ __align__(128) unsigned char tsm[];
-    const int k = p.k, PX = p.PX, PY = p.PY;
-    const size_t pb = p.plane_bytes;
-    // layout: level-0 ring (kTbRing0 planes), levels 1..k-1 (kTbRingL planes each), mbarriers
-    auto plane0 = [&](int j) { return (T*)(tsm + (size_t)(j % kTbRing0) * pb); };
-    auto planeL = [&](int t, int j) {
-        return (T*)(tsm + (size_t)(kTbRing0 + kTbRingL * (t - 1) + (j % kTbRingL)) * pb);
-    };
-    uint64_t* bars = (uint64_t*)(tsm + (size_t)(kTbRing0 + kTbRingL * (k - 1)) * pb);
-
-    int64_t t_id = blockIdx.x;
-    const int tx = (int)(t_id % p.ntx);
-    t_id /= p.ntx;
-    const int ty = (int)(t_id % p.nty);
-    const int tz = (int)(t_id / p.nty);
-    const int64_t x0 = (int64_t)tx * p.TX, y0 = (int64_t)ty * p.TY, z0 = (int64_t)tz * p.ZC;
-    const int64_t z1 = min(z0 + p.ZC, p.n[2]);
-    const int NI = (int)(z1 - z0) + 2 * k;          // input planes z0-k .. z1+k-1
-    const bool wrapb = p.boundary == STC_WRAP;
-    const T pv = tb_pad<T>(p);
-    // input plane j covers z = z0 - k + j; TMA when it lies in the grid or Wrap maps it there
-    auto plane_z = [&](int j) { return z0 - k + j; };
-    auto issue = [&](int j) {
-        const int64_t z = plane_z(j);
-        uint64_t* bar = &bars[j % kTbRing0];
-        if (!wrapb && (z < 0 || z >= p.n[2])) {
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-            return;
+// One level's RPT x 4 cells.  M: the cells at their own height (level t-1), LO / HI: the cells below /
+// above; UP / DN: the row above / below the block, LF / RT: the column left / right of it (all level
+// t-1, plane p).  Every cell folds its taps in table order.
+template <class OpF, class Sh, class P>
+__device__ __forceinline__ void tb_fold_block(const float (&M)[kTbRPT][4], const float (&LO)[kTbRPT][4],
+                                              const float (&HI)[kTbRPT][4], const float (&UP)[4], const float (&DN)[4],
+                                              const float (&LF)[kTbRPT], const float (&RT)[kTbRPT], const P& p,
+                                              float (&res)[kTbRPT][4]) {
+    constexpr auto Tb = Sh::table;
+#pragma unroll
+    for (int r = 0; r < kTbRPT; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            typename OpF::A acc;
+            if constexpr (OpF::kZeroInit) acc = OpF::first(0.0f, 0);
+#pragma unroll
+            for (int k = 0; k < Sh::L; ++k) {
+                const int dx = Tb.o[k].x, dy = Tb.o[k].y, dz = Tb.o[k].z;
+                float v;
+                if (dz < 0) v = LO[r][c];
+                else if (dz > 0) v = HI[r][c];
+                else if (dy < 0) v = r == 0 ? UP[c] : M[r - 1][c];
+                else if (dy > 0) v = r == kTbRPT - 1 ? DN[c] : M[r + 1][c];
+                else if (dx < 0) v = c == 0 ? LF[r] : M[r][c - 1];
+                else if (dx > 0) v = c == 3 ? RT[r] : M[r][c + 1];
+                else v = M[r][c];
+                if (!OpF::kZeroInit && k == 0) acc = OpF::first(v, 0);
+                else acc = OpF::step(acc, v, k, p);
+            }
+            res[r][c] = OpF::finish(acc, M[r][c], p);
         }
-        const int64_t zz = wrapb ? tb_wrap(z, p.n[2]) : z;
-        mbar_arrive_expect_tx(bar, (uint32_t)((size_t)PX * PY * sizeof(T)));
-        tma_load_3d(plane0(j), &p.tmap, bar, (int)(x0 + p.hx[0] - p.padl), (int)(y0 + p.hx[1] - k),
-                    (int)(zz + p.hx[2]));
+}
+
+// The same fold two cells at a time for the ops whose every step is an add or a multiply: the packed
+// Float32 instructions (add.rn.f32x2 / mul.rn.f32x2) round each lane exactly as the scalar ones, so the
+// results are bit-identical while the instruction count halves.  Pairs are the cells (0, 1) and (2, 3)
+// of a row; x - y is formed as x + (-y), which rounds identically.
+template <class OpF> struct TbPairOp { static constexpr bool kPair = false; };
+template <> struct TbPairOp<OpDiffuse<float, float, float>> {
+    static constexpr bool kPair = true;
+    template <class P> __device__ static float2 finish(float2 s, float2 c, const P& p) {
+        const float2 L2 = make_float2(p.Lf, p.Lf), a2 = make_float2(p.alpha_f, p.alpha_f);
+        float2 t = __fmul2_rn(L2, c);
+        t = __fadd2_rn(s, make_float2(-t.x, -t.y));
+        t = __fmul2_rn(a2, t);
+        return __fadd2_rn(c, t);
+    }
+};
+template <> struct TbPairOp<OpSumF<float, float, float>> {
+    static constexpr bool kPair = true;
+    template <class P> __device__ static float2 finish(float2 s, float2, const P&) { return s; }
+};
+
+template <class OpF, class Sh, class P>
+__device__ __forceinline__ void tb_fold_block2(const float (&M)[kTbRPT][4], const float (&LO)[kTbRPT][4],
+                                               const float (&HI)[kTbRPT][4], const float (&UP)[4], const float (&DN)[4],
+                                               const float (&LF)[kTbRPT], const float (&RT)[kTbRPT], const P& p,
+                                               float (&res)[kTbRPT][4]) {
+    constexpr auto Tb = Sh::table;
+#pragma unroll
+    for (int r = 0; r < kTbRPT; ++r)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = 2 * h;
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int k = 0; k < Sh::L; ++k) {
+                const int dx = Tb.o[k].x, dy = Tb.o[k].y, dz = Tb.o[k].z;
+                float2 v;
+                if (dz < 0) v = make_float2(LO[r][c], LO[r][c + 1]);
+                else if (dz > 0) v = make_float2(HI[r][c], HI[r][c + 1]);
+                else if (dy < 0) v = r == 0 ? make_float2(UP[c], UP[c + 1]) : make_float2(M[r - 1][c], M[r - 1][c + 1]);
+                else if (dy > 0) v = r == kTbRPT - 1 ? make_float2(DN[c], DN[c + 1]) : make_float2(M[r + 1][c], M[r + 1][c + 1]);
+                else if (dx < 0) v = make_float2(c == 0 ? LF[r] : M[r][c - 1], M[r][c]);
+                else if (dx > 0) v = make_float2(M[r][c + 1], c == 2 ? RT[r] : M[r][c + 2]);
+                else v = make_float2(M[r][c], M[r][c + 1]);
+                acc = k == 0 ? v : __fadd2_rn(acc, v);
+            }
+            const float2 o = TbPairOp<OpF>::finish(acc, make_float2(M[r][c], M[r][c + 1]), p);
+            res[r][c] = o.x;
+            res[r][c + 1] = o.y;
+        }
+}
+
+// The block's rows above / below on plane `pl` (row pitch BX elements of type S), and the one column
+// each end lane of a warp needs beyond its block (edge_off: lane 31 reads right of its block, every
+// other lane left of lane 0's block, so the load is a broadcast).  Rows above / below the plane and the
+// columns beyond its ends read slack memory: those cells lie outside every level's valid region.
+template <class S, class Sh>
+__device__ __forceinline__ void tb_edges(const S* pl, int BX, int cx, int cy, int edge_off, float (&UP)[4],
+                                         float (&DN)[4], float (&EDGE)[kTbRPT]) {
+    using U = TbTaps<Sh>;
+    if constexpr (U::kUp) ld_row_vec<S, float, 4>(pl + (cy - 1) * BX + cx, UP);
+    if constexpr (U::kDn) ld_row_vec<S, float, 4>(pl + (cy + kTbRPT) * BX + cx, DN);
+    if constexpr (U::kLf || U::kRt) {
+#pragma unroll
+        for (int r = 0; r < kTbRPT; ++r) EDGE[r] = tb_widen<S>(pl[edge_off + r * BX]);
+    }
+}
+
+template <class S>
+__device__ __forceinline__ void tb_own(const S* pl, int BX, int cx, int cy, float (&V)[kTbRPT][4]) {
+#pragma unroll
+    for (int r = 0; r < kTbRPT; ++r) ld_row_vec<S, float, 4>(pl + (cy + r) * BX + cx, V[r]);
+}
+
+// left / right columns of the block from the neighbouring lanes' cells (lanes hold consecutive blocks of
+// a row band), the warp's end lanes from EDGE
+template <class Sh>
+__device__ __forceinline__ void tb_sides(const float (&M)[kTbRPT][4], const float (&EDGE)[kTbRPT], int lane,
+                                         float (&LF)[kTbRPT], float (&RT)[kTbRPT]) {
+    using U = TbTaps<Sh>;
+#pragma unroll
+    for (int r = 0; r < kTbRPT; ++r) {
+        if constexpr (U::kLf) {
+            const float v = __shfl_up_sync(0xffffffffu, M[r][3], 1);
+            LF[r] = lane == 0 ? EDGE[r] : v;
+        }
+        if constexpr (U::kRt) {
+            const float v = __shfl_down_sync(0xffffffffu, M[r][0], 1);
+            RT[r] = lane == 31 ? EDGE[r] : v;
+        }
+    }
+}
+
+template <class T, class Op, class Sh>
+__global__ void __launch_bounds__(kTbMaxThreads, 1) tb6_kernel(const __grid_constant__ TB6Params p) {
+    static_assert(TbTaps<Sh>::only_axis_taps(), "taps must be the centre or one step along one axis");
+    using OpF = typename TbF32<Op>::type;
+    extern __shared__ __align__(128) unsigned char tsm[];
+    const int BX = p.BX, QX = BX >> 2;
+    constexpr int k = kTbK;
+    auto ring = [&](uint32_t g) { return (const T*)(tsm + p.ring_off + (size_t)(g % kTbRing) * p.ring_stride); };
+    // level buffer (t, parity): plane pointer (one slack row precedes it)
+    auto lvl = [&](int t, int par) {
+        return (float*)(tsm + p.lvl_off + (size_t)(2 * (t - 1) + par) * p.lvl_stride) + BX;
     };
-    if (threadIdx.x == 0) {
+    uint64_t* bars = (uint64_t*)(tsm + p.bar_off);
+
+    // Threads past the last block compute a copy of a real block (so that every lane of a warp takes
+    // part in the shuffles) and store nothing.
+    const int nqy = p.BY / kTbRPT;
+    const int nblk = QX * nqy;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const bool act = tid < nblk;
+    const int qx = tid % QX, qy = min(tid / QX, nqy - 1);
+    const int cx = 4 * qx, cy = kTbRPT * qy;
+    const int t0 = tid & ~31;
+    const int cx0 = 4 * (t0 % QX), cy0 = kTbRPT * min(t0 / QX, nqy - 1);
+    const int edge_off = lane == 31 ? cy * BX + cx + 4 : cy0 * BX + cx0 - 1;
+
+    if (tid == 0) {
         prefetch_tensormap(&p.tmap);
-        for (int s = 0; s < kTbRing0; ++s) mbar_init(&bars[s], 1);
+        for (int s = 0; s < kTbRing; ++s) mbar_init(&bars[s], 1);
         fence_barrier_init();
     }
     __syncthreads();
-    const int ahead = kTbRing0 - 3;
-    if (threadIdx.x == 0)
-        for (int j = 0; j < min(ahead, NI); ++j) issue(j);
-    // region of the box holding real tile columns/rows
-    const bool edge_xy = x0 - k < 0 || y0 - k < 0 || x0 + p.TX + k > p.n[0] || y0 + p.TY + k > p.n[1];
-    // Skewed wavefront: at iteration i, level t computes its plane j = i - 2t + 1.  Level 1 reads
-    // level-0 planes i-2 .. i (plane i just landed); level t >= 2 reads level t-1 planes j-1 .. j+1,
-    // all finished in earlier iterations.  So every level of an iteration is independent of the
-    // others and one barrier per iteration suffices.  Iterations continue past the last input plane
-    // until level k has produced every output plane.
-    const int iters = NI + 2 * k - 1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (int i = 0; i < iters; ++i) {
-        if (i < NI) {
-            if (threadIdx.x == 0 && i + ahead < NI) {
+
+    uint32_t gplane = 0;   // planes this CTA has consumed so far (ring slot and phase)
+    for (int item = blockIdx.x; item < p.nitems; item += gridDim.x) {
+        const int txi = item % p.ntx;
+        const int rest = item / p.ntx;
+        const int tyi = rest % p.nty, tzi = rest / p.nty;
+        const int x0 = txi * p.TX, y0 = tyi * p.TY, z0 = tzi * p.ZC;
+        const int z1 = min(z0 + p.ZC, p.n[2]);
+        const int NI = (z1 - z0) + 2 * k;       // input planes z0-k .. z1+k-1
+        const int gx0 = x0 - p.XH, gy0 = y0 - kTbK, gz0 = z0 - k;   // global coords of box (0, 0, plane 0)
+        auto issue = [&](int j) {
+            const uint32_t g = gplane + (uint32_t)j;
+            uint64_t* bar = &bars[g % kTbRing];
+            mbar_arrive_expect_tx(bar, p.box_bytes);
+            tma_load_3d((void*)ring(g), &p.tmap, bar, gx0 + p.H, gy0 + p.H, gz0 + j + p.H);
+        };
+        if (tid == 0) {
+            fence_proxy_async();
+            issue(0);
+            if (NI > 1) issue(1);
+        }
+        // per-thread constants: which of the block's cells lie outside the grid (Remove masks) and
+        // whether it lies in the tile's interior (the stored outputs)
+        int xout = 0, yout = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) xout |= (gx0 + cx + c < 0 || gx0 + cx + c >= p.n[0]) ? (1 << c) : 0;
+#pragma unroll
+        for (int r = 0; r < kTbRPT; ++r) yout |= (gy0 + cy + r < 0 || gy0 + cy + r >= p.n[1]) ? (1 << r) : 0;
+        const bool own_out = act && cx >= p.XH && cx < p.XH + p.TX && cy >= kTbK && cy < kTbK + p.TY &&
+                             gx0 + cx < p.n[0] && gy0 + cy < p.n[1];
+        const bool full4 = gx0 + cx + 3 < p.n[0];
+
+        // S[t-2][u]: level t's own-height plane (level t-1's cells at plane i - t, read from shared
+        // memory for the fold) of the iterations with i mod 2 == u, t = 2 .. K.  The one read in the
+        // previous iteration is this iteration's plane below (LO): its shared-memory buffer has been
+        // overwritten by then.  Iterations run in pairs, so the set index is a compile-time constant and
+        // nothing is copied between registers.  Level 1 reads its three planes from the input ring.
+        float S[kTbK - 1][2][kTbRPT][4];
+        bool failed = false;
+        auto iteration = [&](const int i, auto u_c) {
+            constexpr int U = decltype(u_c)::value;
+            if (tid == 0 && i + 2 < NI) {
                 fence_proxy_async();
-                issue(i + ahead);
+                issue(i + 2);
             }
-            const bool ok = mbar_wait_bounded(&bars[i % kTbRing0], (uint32_t)((i / kTbRing0) & 1));
+            const uint32_t gi = gplane + (uint32_t)i;
+            const bool ok = mbar_wait_bounded(&bars[gi % kTbRing], (gi / kTbRing) & 1u);
             if (!__syncthreads_and(ok)) {
-                if (threadIdx.x == 0) {
+                if (tid == 0) {
                     atomicOr(p.status, DEV_ERR_TIMEOUT);
-                    for (int j = i; j < min(i + ahead, NI); ++j)
-                        mbar_wait_bounded(&bars[j % kTbRing0], (uint32_t)((j / kTbRing0) & 1), 100000000ll);
+                    for (int j = i; j < min(i + 3, NI); ++j) {
+                        const uint32_t g = gplane + (uint32_t)j;
+                        mbar_wait_bounded(&bars[g % kTbRing], (g / kTbRing) & 1u, 100000000ll);
+                    }
                 }
+                failed = true;
                 return;
             }
-            // level-0 plane i: patch cells outside the grid (Wrap copies / Remove padval)
-            T* P0 = plane0(i);
-            const int64_t z = plane_z(i);
-            const bool zout = z < 0 || z >= p.n[2];
-            if (!wrapb && zout) {
-                for (int c = threadIdx.x; c < PX * PY; c += blockDim.x) P0[c] = pv;
-                fence_proxy_async();   // generic writes before a later TMA refill of this slot
-                __syncthreads();
-            } else if (p.fixup && edge_xy) {
-                // rows outside in y: every cell (a warp per row); rows inside: only the x cells beyond
-                // either end, one per thread so that their loads are in flight together
-                const int64_t gx0 = x0 - p.padl;
-                const int xl = (int)max((int64_t)0, min((int64_t)PX, -gx0));             // bx < xl: gx < 0
-                const int xr0 = (int)max((int64_t)xl, min((int64_t)PX, p.n[0] - gx0));   // bx >= xr0: gx >= n0
-                const int nxo = xl + (PX - xr0);
-                for (int it = threadIdx.x; it < PY * nxo; it += blockDim.x) {
-                    const int by = it / nxo, c = it - by * nxo;
-                    const int64_t gy = y0 - k + by;
-                    if (gy < 0 || gy >= p.n[1]) continue;
-                    const int bx = c < xl ? c : xr0 + (c - xl);
-                    P0[by * PX + bx] = tb_load<T>(p, gx0 + bx, gy, z);
-                }
-                for (int by = warp; by < PY; by += nwarps) {
-                    const int64_t gy = y0 - k + by;
-                    if (gy >= 0 && gy < p.n[1]) continue;
-                    for (int bx = lane; bx < PX; bx += 32) P0[by * PX + bx] = tb_load<T>(p, gx0 + bx, gy, z);
-                }
-                fence_proxy_async();
-                __syncthreads();
-            }
-        }
-        for (int t = 1; t <= k; ++t) {
-            const int j = i - 2 * t + 1;               // plane index at level t
-            if (j < t || j > NI - 1 - t) continue;     // uniform across the CTA
-            const T* lo = (t == 1) ? plane0(j - 1) : planeL(t - 1, j - 1);
-            const T* mid = (t == 1) ? plane0(j) : planeL(t - 1, j);
-            const T* hi = (t == 1) ? plane0(j + 1) : planeL(t - 1, j + 1);
-            const int64_t z = plane_z(j);
-            const int xa = p.padl - k + t, xb = p.padl + p.TX + k - t;
-            const int ya = t, yb = p.TY + 2 * k - t;
-            if constexpr (VEC) {
-                // work items: 4-cell groups from the multiple of 4 at or below xa (the extra cells left
-                // of the valid region are computed and never read); padl and PX leave a spare column
-                // group on each side, so the x - 1 / x + 1 reads stay inside the plane.
-                const bool last = t == k;
-                const int gx0 = last ? p.padl : (xa & ~3);
-                const int ngx = last ? (p.TX >> 2) : ((xb - gx0 + 3) >> 2);
-                const int row0 = last ? k : ya, nrows = last ? p.TY : yb - ya;
-                const int nit = ngx * nrows;
-                const float inv = 1.0f / (float)ngx;
-                const bool zout = z < 0 || z >= p.n[2];
-                T* out = last ? nullptr : planeL(t, j);
-                T* dst = (T*)p.dst;
-                const int nvx = (int)min((int64_t)p.TX, p.n[0] - x0), nvy = (int)min((int64_t)p.TY, p.n[1] - y0);
-                for (int it = threadIdx.x; it < nit; it += blockDim.x) {
-                    const int r = __float2int_rz(((float)it + 0.5f) * inv);   // it / ngx, exact (ngx <= 64)
-                    const int g = it - r * ngx;
-                    const int by = row0 + r, bx = gx0 + 4 * g;
-                    const int off = by * PX + bx;
-                    T res[4];
-                    tb_cells4<T, Op, Sh>(lo, mid, hi, off, PX, p, res);
-                    if (!last) {
-                        if (!wrapb) {
-                            // Remove: cells outside the grid hold padval at every level
-                            const int64_t gy = y0 - k + by, gxa = x0 - p.padl + bx;
-                            const bool row_out = zout || gy < 0 || gy >= p.n[1];
-                            if (row_out || gxa < 0 || gxa + 3 >= p.n[0]) {
+            float prev[kTbRPT][4];   // the plane the level below produced this iteration (this level's HI)
 #pragma unroll
-                                for (int c = 0; c < 4; ++c)
-                                    if (row_out || gxa + c < 0 || gxa + c >= p.n[0]) res[c] = pv;
-                            }
+            for (int t = 1; t <= kTbK; ++t) {
+                if (!(i >= 2 * t - 1)) continue;   // uniform across the CTA
+                const int pz = i - t;              // this level's plane (input-plane numbering)
+                float LO[kTbRPT][4], HI[kTbRPT][4], UP[4], DN[4], EDGE[kTbRPT], LF[kTbRPT], RT[kTbRPT];
+                float (&M)[kTbRPT][4] = S[t == 1 ? 0 : t - 2][t == 1 ? 0 : U];
+                float M1[kTbRPT][4];
+                float (&MM)[kTbRPT][4] = t == 1 ? M1 : M;
+                if (i == 2 * t - 1) {
+                    // the iteration before this level's first plane: read level t-1's plane below it
+                    if (t >= 2) tb_own<float>(lvl(t - 1, pz & 1), BX, cx, cy, MM);
+                    continue;
+                }
+                if (t == 1) {
+                    const T* mid = ring(gplane + (uint32_t)pz);
+                    tb_own<T>(mid, BX, cx, cy, MM);
+                    tb_edges<T, Sh>(mid, BX, cx, cy, edge_off, UP, DN, EDGE);
+                    if constexpr (TbTaps<Sh>::has(0, 0, -1)) tb_own<T>(ring(gplane + (uint32_t)pz - 1), BX, cx, cy, LO);
+                    if constexpr (TbTaps<Sh>::has(0, 0, 1)) tb_own<T>(ring(gplane + (uint32_t)pz + 1), BX, cx, cy, HI);
+                } else {
+                    const float* mid = lvl(t - 1, pz & 1);
+                    tb_own<float>(mid, BX, cx, cy, MM);
+                    tb_edges<float, Sh>(mid, BX, cx, cy, edge_off, UP, DN, EDGE);
+#pragma unroll
+                    for (int r = 0; r < kTbRPT; ++r)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            LO[r][c] = S[t - 2][1 - U][r][c];
+                            HI[r][c] = prev[r][c];
                         }
-                        sts4<T>(out + off, res);
-                    } else {
-                        const int ly = r, lx = 4 * g;
-                        if (ly < nvy && lx < nvx)
-                            st_row_vec<T, 4>(dst + p.dst_org + z * p.dstr[2] + (y0 + ly) * p.dstr[1] + x0 + lx, res,
-                                             p.aligned != 0, nvx - lx);
+                }
+                tb_sides<Sh>(MM, EDGE, lane, LF, RT);
+                float res[kTbRPT][4];
+                if constexpr (TbPairOp<OpF>::kPair) tb_fold_block2<OpF, Sh>(MM, LO, HI, UP, DN, LF, RT, p, res);
+                else tb_fold_block<OpF, Sh>(MM, LO, HI, UP, DN, LF, RT, p, res);
+                const int gz = gz0 + pz;
+                if (t < k) {
+                    if (p.remove) {
+                        const bool zo = gz < 0 || gz >= p.n[2];
+#pragma unroll
+                        for (int r = 0; r < kTbRPT; ++r)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)
+                                if (zo || ((yout >> r) & 1) || ((xout >> c) & 1)) res[r][c] = p.padf;
+                    }
+                    if (!(std::is_same_v<T, float>) && !p.keep_f32) {
+#pragma unroll
+                        for (int r = 0; r < kTbRPT; ++r)
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) res[r][c] = tb_widen<T>(tb_round<T>(res[r][c]));
+                    }
+                    if (act) {
+                        float* out = lvl(t, pz & 1);
+#pragma unroll
+                        for (int r = 0; r < kTbRPT; ++r)
+                            *(float4*)(out + (cy + r) * BX + cx) = make_float4(res[r][0], res[r][1], res[r][2], res[r][3]);
+                    }
+#pragma unroll
+                    for (int r = 0; r < kTbRPT; ++r)
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) prev[r][c] = res[r][c];
+                } else if (own_out) {
+                    T* drow = (T*)p.dst + (int64_t)gz * p.dstr2 + gx0 + cx;
+#pragma unroll
+                    for (int r = 0; r < kTbRPT; ++r) {
+                        const int gy = gy0 + cy + r;
+                        if (gy >= p.n[1]) break;
+                        T o[4];
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            if constexpr (std::is_same_v<T, __nv_bfloat16>) {
+                                if (p.stochastic) {
+                                    const uint64_t lin = (uint64_t)(gx0 + cx + c) +
+                                                         (uint64_t)p.n[0] * ((uint64_t)gy + (uint64_t)p.n[1] * (uint64_t)gz);
+                                    o[c] = tb_bf16_stochastic(res[r][c], lin, p.round_step);
+                                    continue;
+                                }
+                            }
+                            o[c] = tb_round<T>(res[r][c]);
+                        }
+                        T* d = drow + (int64_t)gy * p.dstr1;
+                        if (full4) tb_st4<T>(d, o);
+                        else
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)
+                                if (gx0 + cx + c < p.n[0]) d[c] = o[c];
                     }
                 }
-                continue;
             }
-            if (t < k) {
-                T* out = planeL(t, j);
-                const bool zout = z < 0 || z >= p.n[2];
-                for (int by = ya + warp; by < yb; by += nwarps) {
-                    const int64_t gy = y0 - k + by;
-                    const bool row_out = !wrapb && (zout || gy < 0 || gy >= p.n[1]);
-                    for (int bx = xa + lane; bx < xb; bx += 32) {
-                        const int off = by * PX + bx;
-                        const int64_t gx = x0 - p.padl + bx;
-                        T v;
-                        if (row_out || (!wrapb && (gx < 0 || gx >= p.n[0]))) v = pv;
-                        else v = tb_fold<T, Op, Sh>(lo + off, mid + off, hi + off, PX, p);
-                        out[off] = v;
-                    }
-                }
-            } else {
-                // level k: the outputs, tile interior only
-                T* dst = (T*)p.dst;
-                const int nvx = (int)min((int64_t)p.TX, p.n[0] - x0), nvy = (int)min((int64_t)p.TY, p.n[1] - y0);
-                T* dplane = dst + p.dst_org + z * p.dstr[2] + x0;
-                for (int ly = warp; ly < nvy; ly += nwarps) {
-                    T* drow = dplane + (y0 + ly) * p.dstr[1];
-                    for (int lx = lane; lx < nvx; lx += 32) {
-                        const int off = (ly + k) * PX + lx + p.padl;
-                        drow[lx] = tb_fold<T, Op, Sh>(lo + off, mid + off, hi + off, PX, p);
-                    }
-                }
-            }
+            __syncthreads();
+        };
+        for (int i0 = 0; i0 < NI && !failed; i0 += 2) {
+            iteration(i0, std::integral_constant<int, 0>{});
+            if (failed || i0 + 1 >= NI) break;
+            iteration(i0 + 1, std::integral_constant<int, 1>{});
         }
-        __syncthreads();
+        if (failed) return;
+        gplane += (uint32_t)NI;
     }
 }
 
@@ -381,158 +485,240 @@ static TbEncodeFn tb_encoder() {
     return fn;
 }
 
-using TbLaunch = cudaError_t (*)(const TBParams&, int grid, size_t smem, cudaStream_t);
+using TbLaunch = cudaError_t (*)(const TB6Params&, int grid, int threads, size_t smem, cudaStream_t);
 
-template <class T, class Op, class Sh, bool VEC>
-static cudaError_t tb_launch_v(const TBParams& p, int grid, size_t smem, cudaStream_t s) {
+template <class T, class Op, class Sh>
+static cudaError_t tb6_launch(const TB6Params& p, int grid, int threads, size_t smem, cudaStream_t s) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [&] {
-        attr = cudaFuncSetAttribute(tb3d_kernel<T, Op, Sh, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        attr = cudaFuncSetAttribute(tb6_kernel<T, Op, Sh>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
     if (attr != cudaSuccess) return attr;
-    tb3d_kernel<T, Op, Sh, VEC><<<grid, kTbThreads, smem, s>>>(p);
+    tb6_kernel<T, Op, Sh><<<grid, threads, smem, s>>>(p);
     return cudaGetLastError();
-}
-
-// the vector variant for Conditional grids (tile columns on 16-byte boundaries), else one cell per lane
-template <class T, class Op, class Sh>
-static cudaError_t tb_launch(const TBParams& p, int grid, size_t smem, cudaStream_t s) {
-    return (p.hx[0] % 4 == 0 && p.padl % 4 == 0) ? tb_launch_v<T, Op, Sh, true>(p, grid, smem, s)
-                                                  : tb_launch_v<T, Op, Sh, false>(p, grid, smem, s);
 }
 
 struct TbEntry { int dt, opv, shape; TbLaunch fn; };
 
+using VN3 = Shape<STC_SHAPE_VONNEUMANN, 1, 3>;
+using CR3 = Shape<STC_SHAPE_CROSS, 1, 3>;
 static const TbEntry kTbTable[] = {
-    {STC_F32, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb_launch<float, OpDiffuse<float, float, float>, Shape<STC_SHAPE_VONNEUMANN, 1, 3>>},
-    {STC_BF16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN,
-     &tb_launch<__nv_bfloat16, OpDiffuse<__nv_bfloat16, __nv_bfloat16, float>, Shape<STC_SHAPE_VONNEUMANN, 1, 3>>},
-    {STC_F32, OPV_MEAN, STC_SHAPE_VONNEUMANN, &tb_launch<float, OpMean<float, float, float>, Shape<STC_SHAPE_VONNEUMANN, 1, 3>>},
-    {STC_F32, OPV_MEAN, STC_SHAPE_MOORE, &tb_launch<float, OpMean<float, float, float>, Shape<STC_SHAPE_MOORE, 1, 3>>},
-    {STC_F32, OPV_SUM, STC_SHAPE_CROSS, &tb_launch<float, OpSumF<float, float, float>, Shape<STC_SHAPE_CROSS, 1, 3>>},
+    {STC_F32, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<float, OpDiffuse<float, float, float>, VN3>},
+    {STC_BF16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<__nv_bfloat16, OpDiffuse<__nv_bfloat16, __nv_bfloat16, float>, VN3>},
+    {STC_F16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<__half, OpDiffuse<__half, __half, float>, VN3>},
+    {STC_F32, OPV_MEAN, STC_SHAPE_VONNEUMANN, &tb6_launch<float, OpMean<float, float, float>, VN3>},
+    {STC_F32, OPV_SUM, STC_SHAPE_CROSS, &tb6_launch<float, OpSumF<float, float, float>, CR3>},
 };
 
 static CUtensorMapDataType tb_dtype(int dt) {
-    return dt == STC_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    return dt == STC_F32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+           : dt == STC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 }
 
-int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
-                   int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx, int64_t* done) {
-    *done = 0;
-    if (nsteps < 3 || a->ndims != 3 || st->ndims != 3 || st->radius != 1) return STC_OK;
-    // Opt-in (STC_TBLOCK=1): at its present instruction count per cell update the blocked kernel is
-    // slower on GB300 than one K1 pass per step, which runs near the HBM roofline.
-    const char* e = getenv("STC_TBLOCK");
-    if (!(e && e[0] == '1')) return STC_OK;
-    if (!(bc->boundary == STC_WRAP || bc->boundary == STC_REMOVE)) return STC_OK;
-    int opv = op->code == STC_OP_DIFFUSE ? OPV_DIFFUSE : op->code == STC_OP_MEAN ? OPV_MEAN
-              : op->code == STC_OP_SUM ? OPV_SUM : -1;
-    TbLaunch fn = nullptr;
+static TbLaunch tb_find(const stc_grid* a, const stc_stencil* st, const stc_op* op) {
+    const int opv = op->code == STC_OP_DIFFUSE ? OPV_DIFFUSE : op->code == STC_OP_MEAN ? OPV_MEAN
+                    : op->code == STC_OP_SUM ? OPV_SUM : -1;
     for (const TbEntry& e : kTbTable)
-        if (e.dt == a->dtype && e.opv == opv && table_matches_shape(e.shape, 1, 3, st->offsets, st->len)) fn = e.fn;
-    if (!fn || !tb_encoder()) return STC_OK;
-    const int es = dtype_size(a->dtype), V = 16 / es;
-    for (const stc_grid* g : {a, b}) {
-        if ((uintptr_t)g->data % 16) return STC_OK;
-        for (int d = 1; d < 3; ++d)
-            if ((g->stride[d] * es) % 16) return STC_OK;
-    }
+        if (e.dt == a->dtype && e.opv == opv && table_matches_shape(e.shape, 1, 3, st->offsets, st->len)) return e.fn;
+    return nullptr;
+}
+
+bool tb3d_applies(const stc_grid* a, const stc_stencil* st, const stc_op* op, const stc_bc* bc) {
+    if (a->ndims != 3 || st->ndims != 3 || st->radius != 1) return false;
+    if (!(bc->boundary == STC_WRAP || bc->boundary == STC_REMOVE)) return false;
+    if (!tb_find(a, st, op) || !tb_encoder()) return false;
+    return true;
+}
+
+// Steps of the run taken by blocked passes: the largest multiple of kTbK below nsteps; the rest (1 to
+// kTbK steps, so that the pair holds states n - 1 and n at the end) run as per-step maps on the pair.
+static int64_t tb_blocked_steps(int64_t nsteps) { return nsteps >= 1 ? (nsteps - 1) / kTbK * kTbK : 0; }
+
+int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
+                   int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx, uint32_t flags, int64_t* done) {
+    *done = 0;
+    const bool keep = (flags & STC_KEEP_F32) != 0 && (a->dtype == STC_BF16 || a->dtype == STC_F16);
+    if (nsteps < 1) return STC_OK;
+    const char* env = getenv("STC_TBLOCK");   // tuning / test override: 0 disables the blocked path
+    const bool disabled = env && env[0] == '0';
+    if (!tb3d_applies(a, st, op, bc) || disabled) return keep ? STC_ERR_UNSUPPORTED : STC_OK;
+    if (!keep && nsteps < 8) return STC_OK;   // copies in and out would outweigh the saving
+    TbLaunch fn = tb_find(a, st, op);
+    const int es = dtype_size(a->dtype);
     const bool halo = bc->padding != STC_CONDITIONAL;
-    TBParams p;
+    int64_t n[3];
+    for (int d = 0; d < 3; ++d) n[d] = a->size[d] - (halo ? 2 : 0);
+    const int XH = std::max(kTbK, 16 / es);   // tile's first column on a 16-byte boundary of the box
+    const int H = XH;
+    for (int d = 0; d < 3; ++d)
+        if (n[d] < H || n[d] + 2 * H + 256 >= (1ll << 31)) return keep ? STC_ERR_UNSUPPORTED : STC_OK;
+
+    // geometry: a tile of TX = 64 or 128 columns and the box height (rows a multiple of kTbRPT) with at
+    // most 16 warps whose ring and level buffers fit, choosing the pair that computes the fewest box
+    // cells per plane of the grid
+    TB6Params p;
     memset(&p, 0, sizeof(p));
-    for (int d = 0; d < 3; ++d) {
-        p.n[d] = a->size[d] - (halo ? 2 : 0);
-        p.hx[d] = halo ? 1 : 0;
-        p.sst[d] = a->stride[d];
-        p.dstr[d] = b->stride[d];
-        if (p.n[d] < 1) return STC_OK;
+    p.XH = XH;
+    p.H = H;
+    const size_t smem_cap = (size_t)ctx->max_smem_optin;
+    auto smem_for = [&](int BX, int BY, uint32_t* ring_off, uint32_t* ring_stride, uint32_t* lvl_off,
+                        uint32_t* lvl_stride, uint32_t* bar_off) {
+        const uint32_t slack = (uint32_t)((BX * es + 127) / 128 * 128);
+        const uint32_t rs = (uint32_t)(((size_t)BX * BY * es + 127) / 128 * 128);
+        const uint32_t ls = (uint32_t)(((size_t)BX * (BY + 2) * 4 + 127) / 128 * 128);
+        *ring_off = slack;
+        *ring_stride = rs;
+        *lvl_off = slack + kTbRing * rs;
+        *lvl_stride = ls;
+        *bar_off = *lvl_off + 2 * (kTbK - 1) * ls;
+        return (size_t)*bar_off + 8 * kTbRing;
+    };
+    int best_by = 0, best_tx = 0;
+    int64_t best_cost = INT64_MAX;
+    for (int TX : {64, 128}) {
+        const int BX = TX + 2 * XH;
+        for (int BY = 2 * kTbK + 8; BY <= 256; BY += kTbRPT) {
+            uint32_t a0, a1, a2, a3, a4;
+            if (smem_for(BX, BY, &a0, &a1, &a2, &a3, &a4) > smem_cap) break;
+            const int threads = (BX / 4) * (BY / kTbRPT);
+            if (threads > kTbMaxThreads) break;
+            const int TY = BY - 2 * kTbK;
+            const int64_t cost = (n[0] + TX - 1) / TX * BX * ((n[1] + TY - 1) / TY * BY);
+            if (cost < best_cost) {
+                best_cost = cost;
+                best_by = BY;
+                best_tx = TX;
+            }
+        }
     }
-    p.boundary = bc->boundary;
-    p.padf = bc->padval;
+    if (!best_by) return keep ? STC_ERR_UNSUPPORTED : STC_OK;
+    p.TX = best_tx;
+    p.BX = p.TX + 2 * XH;
+    p.BY = best_by;
+    p.TY = p.BY - 2 * kTbK;
+    const size_t smem = smem_for(p.BX, p.BY, &p.ring_off, &p.ring_stride, &p.lvl_off, &p.lvl_stride, &p.bar_off);
+    const int threads = ((p.BX / 4) * (p.BY / kTbRPT) + 31) / 32 * 32;
+    p.box_bytes = (uint32_t)((size_t)p.BX * p.BY * es);
+    for (int d = 0; d < 3; ++d) p.n[d] = (int32_t)n[d];
+    p.ntx = (int)((n[0] + p.TX - 1) / p.TX);
+    p.nty = (int)((n[1] + p.TY - 1) / p.TY);
+    // z chunks: the count whose waves of one CTA per SM (time ~ chunk planes + 2k) finish soonest
+    {
+        const int64_t xy = (int64_t)p.ntx * p.nty;
+        int64_t best = INT64_MAX;
+        int bz = 1;
+        for (int c = 1; c <= std::max<int64_t>(1, n[2] / 8); ++c) {
+            const int64_t zc = (n[2] + c - 1) / c;
+            const int64_t waves = (xy * c + ctx->num_sms - 1) / ctx->num_sms;
+            const int64_t cost = waves * (zc + 2 * kTbK);
+            if (cost < best) { best = cost; bz = c; }
+        }
+        p.ZC = (int)((n[2] + bz - 1) / bz);
+        p.nzc = (int)((n[2] + p.ZC - 1) / p.ZC);
+    }
+    p.nitems = p.ntx * p.nty * p.nzc;
+    const int grid = (int)std::min<int64_t>(p.nitems, ctx->num_sms);
+    p.remove = bc->boundary == STC_REMOVE;
+    {
+        // padval in the storage type (as the reference's getneighbor returns it), widened
+        const double pv = bc->padval;
+        if (a->dtype == STC_F32) p.padf = (float)pv;
+        else if (a->dtype == STC_BF16) { __nv_bfloat16 h = __float2bfloat16_rn((float)pv); p.padf = __bfloat162float(h); }
+        else { __half h = __double2half(pv); p.padf = __half2float(h); }
+    }
+    p.keep_f32 = keep;
+    p.stochastic = keep && a->dtype == STC_BF16;
     p.status = ctx->status;
     p.L = st->len;
     p.alpha = op->alpha;
     p.rcp_f = (float)(1.0 / (double)st->len);
-    p.fastdiv_f = (opv == OPV_MEAN && a->dtype != STC_F64) ? (int)fastdiv_f_exact(st->len) : 0;
+    p.fastdiv_f = op->code == STC_OP_MEAN ? (int)fastdiv_f_exact(st->len) : 0;
     p.Lf = (float)st->len;
     p.Ld = (double)st->len;
     p.alpha_f = (float)op->alpha;
-    p.TX = 64;
-    p.TY = 16;
-    const int smem_cap = 200 * 1024;
-    // Halo parents are treated with the boundary applied on the fly (their rings are not refreshed
-    // between the blocked steps); the patch after each plane copy covers every cell outside the grid.
-    p.fixup = halo || !(bc->boundary == STC_REMOVE && bc->padval == 0.0 && !std::signbit(bc->padval));
-    p.ntx = (int)((p.n[0] + p.TX - 1) / p.TX);
-    p.nty = (int)((p.n[1] + p.TY - 1) / p.TY);
-    const int64_t xy = (int64_t)p.ntx * p.nty;
-    p.nzc = (int)std::max<int64_t>(1, std::min<int64_t>(p.n[2] / 32, (4 * ctx->num_sms + xy - 1) / xy));
-    p.ZC = (int)((p.n[2] + p.nzc - 1) / p.nzc);
-    p.nzc = (int)((p.n[2] + p.ZC - 1) / p.ZC);
-    // launches: the first nsteps-1 steps, split so that state nsteps-1 ends in the parent the reference
-    // leaves it in (a after an odd number of steps... i.e. m launches with m = nsteps-1 (mod 2))
-    // deepest k <= 4 whose rings keep two CTAs per SM (<= 110 KB of shared memory)
-    // Box geometry: the vector variant (Conditional grids, hx = 0) keeps the tile's first column at a
-    // multiple of 4 and 16 bytes (padl = 8 >= k + 4) with room for its aligned 4-cell groups and their
-    // x +- 1 reads on both sides; the one-cell variant needs only k columns of halo.
-    const bool vec = p.hx[0] % 4 == 0;
-    auto padl_for = [&](int kk) { return vec ? 8 : kk + (((p.hx[0] - kk) % V) + V) % V; };
-    auto px_for = [&](int kk, int padl) { return (padl + p.TX + kk + (vec ? 7 : 0) + V - 1) / V * V; };
-    int kmax = 4;
-    {
-        while (kmax > 1) {
-            const int padl = padl_for(kmax);
-            const int PX = px_for(kmax, padl);
-            const size_t pbytes = ((size_t)PX * (p.TY + 2 * kmax) * es + 127) / 128 * 128;
-            if ((size_t)(kTbRing0 + kTbRingL * (kmax - 1)) * pbytes <= 110 * 1024) break;
-            --kmax;
-        }
+
+    // the padded pair: rows of `pitch` elements, interior x = 0 on a 128-byte line
+    const int64_t line = 128 / es;
+    const int64_t lead = (H + line - 1) / line * line - H;   // unused elements before the ring
+    const int64_t P0 = n[0] + 2 * H, P1 = n[1] + 2 * H, P2 = n[2] + 2 * H;
+    const int64_t pitch = (lead + P0 + line - 1) / line * line;
+    const size_t cells = (size_t)pitch * P1 * P2;
+    char* mem = nullptr;
+    bool cached = false;
+    if (workspace_acquire(2 * cells * es + 256, stream, (void**)&mem, &cached) != STC_OK)
+        return keep ? STC_ERR_CUDA : STC_OK;
+    stc_grid pg[2];
+    for (int i = 0; i < 2; ++i) {
+        pg[i].ndims = 3;
+        pg[i].dtype = a->dtype;
+        pg[i].size[0] = P0;
+        pg[i].size[1] = P1;
+        pg[i].size[2] = P2;
+        pg[i].stride[0] = 1;
+        pg[i].stride[1] = pitch;
+        pg[i].stride[2] = pitch * P1;
+        pg[i].data = mem + (i * cells + lead) * es;
     }
-    const int64_t blocked = nsteps - 1;
-    int64_t m = (blocked + kmax - 1) / kmax;
-    if ((m - blocked) % 2 != 0) ++m;
-    if (m > blocked) m = blocked;
-    std::vector<int> ks;
-    for (int64_t i = 0; i < m; ++i) ks.push_back((int)(blocked / m + (i < blocked % m ? 1 : 0)));
+    stc_bc hb = *bc;
+    hb.padding = STC_HALO_OUT;
+    const int64_t inner = H + H * pitch + H * pitch * P1;    // offset of logical (0, 0, 0) in a padded buffer
+    const int64_t org_a = halo ? 1 + a->stride[1] + a->stride[2] : 0;
+    const int64_t org_b = halo ? 1 + b->stride[1] + b->stride[2] : 0;
     const stc_grid* par[2] = {a, b};
-    int cur = *src_is_b;
-    for (int kk : ks) {
-        const stc_grid* sg = par[cur];
-        const stc_grid* dg = par[1 - cur];
-        p.k = kk;
-        p.padl = padl_for(kk);
-        p.PX = px_for(kk, p.padl);
-        p.PY = p.TY + 2 * kk;
-        p.plane_bytes = (uint32_t)(((size_t)p.PX * p.PY * es + 127) / 128 * 128);
-        const size_t smem = (size_t)(kTbRing0 + kTbRingL * (kk - 1)) * p.plane_bytes + 8 * kTbRing0;
-        if (smem > (size_t)smem_cap || p.PX > 256 || p.PY > 256) return *done ? STC_ERR_UNSUPPORTED : STC_OK;
-        p.src = sg->data;
-        p.dst = dg->data;
-        p.src_org = halo ? 1 + sg->stride[1] + sg->stride[2] : 0;
-        p.dst_org = halo ? 1 + dg->stride[1] + dg->stride[2] : 0;
-        {
-            const int VA = std::min(16, 4 * es);
-            p.aligned = ((uintptr_t)dg->data + (uintptr_t)p.dst_org * es) % VA == 0 && (dg->stride[1] * es) % VA == 0 &&
-                        (dg->stride[2] * es) % VA == 0;
-        }
-        for (int d = 0; d < 3; ++d) { p.sst[d] = sg->stride[d]; p.dstr[d] = dg->stride[d]; }
-        cuuint64_t gdim[3] = {(cuuint64_t)sg->size[0], (cuuint64_t)sg->size[1], (cuuint64_t)sg->size[2]};
-        cuuint64_t gstr[2] = {(cuuint64_t)(sg->stride[1] * es), (cuuint64_t)(sg->stride[2] * es)};
-        cuuint32_t box[3] = {(cuuint32_t)p.PX, (cuuint32_t)p.PY, 1}, est[3] = {1, 1, 1};
-        if (tb_encoder()(&p.tmap, tb_dtype(sg->dtype), 3, sg->data, gdim, gstr, box, est, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    const int64_t org[2] = {org_a, org_b};
+    int rc = launch_grid_copy(par[*src_is_b], org[*src_is_b], &pg[0], inner, n, stream);
+    if (!rc && p.remove) rc = launch_halo_fill(&pg[0], H, &hb, stream);
+    if (!rc && p.remove) rc = launch_halo_fill(&pg[1], H, &hb, stream);
+    const int64_t blocked = tb_blocked_steps(nsteps);
+    int cur = 0;
+    int64_t step = 0;
+    while (step < blocked && !rc) {
+        if (!p.remove && (rc = launch_halo_fill(&pg[cur], H, &hb, stream))) break;
+        step += kTbK;
+        p.round_step = (uint32_t)step;
+        p.dst = (char*)pg[1 - cur].data + inner * es;
+        p.dstr1 = pitch;
+        p.dstr2 = pitch * P1;
+        cuuint64_t gdim[3] = {(cuuint64_t)P0, (cuuint64_t)P1, (cuuint64_t)P2};
+        cuuint64_t gstr[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)(pitch * P1 * es)};
+        cuuint32_t box[3] = {(cuuint32_t)p.BX, (cuuint32_t)p.BY, 1}, est[3] = {1, 1, 1};
+        if (tb_encoder()(&p.tmap, tb_dtype(a->dtype), 3, pg[cur].data, gdim, gstr, box, est, CU_TENSOR_MAP_INTERLEAVE_NONE,
                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return *done ? STC_ERR_UNSUPPORTED : STC_OK;
-        const int grid = p.ntx * p.nty * p.nzc;
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+            rc = STC_ERR_UNSUPPORTED;
+            break;
+        }
         void* prof = prof_begin(stream);
-        cudaError_t e = fn(p, grid, smem, stream);
-        prof_end(prof, stream, "tblock3d", 2.0 * es * p.n[0] * p.n[1] * p.n[2] * kk, (double)p.n[0] * p.n[1] * p.n[2] * kk);
-        if (e != cudaSuccess) return cuda_fail(e);
+        cudaError_t e = fn(p, grid, threads, smem, stream);
+        prof_end(prof, stream, "tblock3d", 2.0 * es * n[0] * n[1] * n[2] * kTbK, (double)n[0] * n[1] * n[2] * kTbK);
+        if (e != cudaSuccess) rc = cuda_fail(e);
         cur = 1 - cur;
-        *done += kk;
     }
-    *src_is_b = cur;
+    // the remaining steps: per-step maps (K2 ring refresh, K1) on the pair seen as parents with a
+    // one-cell Halo ring, each rounded to the storage type as a separate map is
+    stc_grid view[2];
+    for (int v = 0; v < 2; ++v) {
+        view[v] = pg[v];
+        view[v].data = (char*)pg[v].data + (inner - 1 - pitch - pitch * P1) * es;
+        for (int d = 0; d < 3; ++d) view[v].size[d] = n[d] + 2;
+    }
+    for (; step < nsteps && !rc; ++step) {
+        if ((rc = launch_halo_fill(&view[cur], 1, &hb, stream))) break;
+        if ((rc = launch_map(&view[cur], &view[1 - cur], 1, st, op, &hb, stream, ctx))) break;
+        cur = 1 - cur;
+    }
+    // state n to the parent the reference leaves it in, state n - 1 to the other
+    const int res_b = (*src_is_b) ^ (int)(nsteps & 1);
+    if (!rc) rc = launch_grid_copy(&pg[cur], inner, par[res_b], org[res_b], n, stream);
+    if (!rc && nsteps > 1) rc = launch_grid_copy(&pg[1 - cur], inner, par[1 - res_b], org[1 - res_b], n, stream);
+    workspace_release(mem, cached, stream);
+    if (rc) return rc;
+    *src_is_b = res_b;
+    *done = nsteps;
     return STC_OK;
 }
 

@@ -159,7 +159,7 @@ def mapstencil(f, *args, boundary=None, padding=None):
     return _run_map(red, dest, sa, dst_padded=False)
 
 
-def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
+def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True, keep_f32: bool = False):
     """mapstencil!(f, dest, source) or mapstencil!(f, A::SwitchingStencilArray).
 
     For a SwitchingStencilArray, runs `steps` maps (default 1) and returns the switched array, as
@@ -167,6 +167,10 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
     reference (KernelAbstractions.synchronize, src/gatherstencil.jl:100) the call waits for the GPU;
     `sync=False` returns once the work is queued on the current CUDA stream (errors a kernel reports
     then surface at the next synchronising call), so consecutive calls keep the GPU busy.
+
+    `keep_f32=True` (BFloat16 / Float16 state of a 3D multi-step run, STC_KEEP_F32) is the precision
+    mode: the state stays Float32 inside 4-step passes and is rounded to the 16-bit type at their ends
+    (BFloat16 stochastically, from deterministic hashed bits), instead of to nearest after every step.
     """
     if isinstance(f, Terms):
         if isinstance(dest, SwitchingStencilArray):
@@ -186,7 +190,7 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
     if more:
         raise NotImplementedError("extra array arguments need a registered Terms f")
     if isinstance(dest, SwitchingStencilArray):
-        return _run_steps(red, dest, int(steps), sync)
+        return _run_steps(red, dest, int(steps), sync, keep_f32)
     if not isinstance(source, AbstractStencilArray):
         raise TypeError("mapstencil_(f, dest, source) needs a StencilArray source")
     if tuple(dest.shape) != tuple(source.shape):
@@ -198,7 +202,8 @@ def mapstencil_(f, dest, source=None, *more, steps: int = 1, sync: bool = True):
     return _run_map(red, dest, source, dst_padded=False, sync=sync)
 
 
-def _run_steps(red, S: SwitchingStencilArray, steps: int, sync: bool = True) -> SwitchingStencilArray:
+def _run_steps(red, S: SwitchingStencilArray, steps: int, sync: bool = True,
+               keep_f32: bool = False) -> SwitchingStencilArray:
     if steps < 0:
         raise ValueError("steps must be >= 0")
     lib = _lib.load()
@@ -212,8 +217,9 @@ def _run_steps(red, S: SwitchingStencilArray, steps: int, sync: bool = True) -> 
     ga, gb = _grid(a), _grid(b)
     out = C.c_int32(0)
     stream = _lib.current_stream_handle()
+    flags = _flags(sync, stage) | (A.STC_KEEP_F32 if keep_f32 else 0)
     _lib.check(lib.stc_map_steps(C.byref(ga), C.byref(gb), C.byref(st.desc), C.byref(op), C.byref(bc), steps,
-                                 C.byref(out), stream, _flags(sync, stage)), "mapstencil!")
+                                 C.byref(out), stream, flags), "mapstencil!")
     stage.done()
     if out.value:
         return S.switch()
