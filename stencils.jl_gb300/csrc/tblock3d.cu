@@ -183,25 +183,28 @@ __device__ __forceinline__ void tb_fold_block(const float (&M)[kTbRPT][4], const
         }
 }
 
-// The same fold two cells at a time for the ops whose every step is an add or a multiply: the packed
-// Float32 instructions (add.rn.f32x2 / mul.rn.f32x2) round each lane exactly as the scalar ones, so the
-// results are bit-identical while the instruction count halves.  Pairs are the cells (0, 1) and (2, 3)
-// of a row; x - y is formed as x + (-y), which rounds identically.
+// Packed Float32 add (two lanes per instruction, add.rn.f32x2): each lane rounds exactly as __fadd_rn.
+// Only the tap sums use it.  A packed multiply followed by a packed add was measured to come out fused
+// (one rounding) even with an explicit rounding modifier and -fmad=false, so the finishing arithmetic
+// (which multiplies) stays on the scalar __fmul_rn / __fadd_rn intrinsics, which are never fused.
+__device__ __forceinline__ float2 tb_add2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+
+// Ops whose fold is a left fold of adds from the first tap (sum, mean, diffusion): their tap sums can
+// run two cells at a time.  Pairs are the cells (0, 1) and (2, 3) of a row.
 template <class OpF> struct TbPairOp { static constexpr bool kPair = false; };
-template <> struct TbPairOp<OpDiffuse<float, float, float>> {
-    static constexpr bool kPair = true;
-    template <class P> __device__ static float2 finish(float2 s, float2 c, const P& p) {
-        const float2 L2 = make_float2(p.Lf, p.Lf), a2 = make_float2(p.alpha_f, p.alpha_f);
-        float2 t = __fmul2_rn(L2, c);
-        t = __fadd2_rn(s, make_float2(-t.x, -t.y));
-        t = __fmul2_rn(a2, t);
-        return __fadd2_rn(c, t);
-    }
-};
-template <> struct TbPairOp<OpSumF<float, float, float>> {
-    static constexpr bool kPair = true;
-    template <class P> __device__ static float2 finish(float2 s, float2, const P&) { return s; }
-};
+template <> struct TbPairOp<OpDiffuse<float, float, float>> { static constexpr bool kPair = true; };
+template <> struct TbPairOp<OpSumF<float, float, float>> { static constexpr bool kPair = true; };
+template <> struct TbPairOp<OpMean<float, float, float>> { static constexpr bool kPair = true; };
 
 template <class OpF, class Sh, class P>
 __device__ __forceinline__ void tb_fold_block2(const float (&M)[kTbRPT][4], const float (&LO)[kTbRPT][4],
@@ -226,11 +229,10 @@ __device__ __forceinline__ void tb_fold_block2(const float (&M)[kTbRPT][4], cons
                 else if (dx < 0) v = make_float2(c == 0 ? LF[r] : M[r][c - 1], M[r][c]);
                 else if (dx > 0) v = make_float2(M[r][c + 1], c == 2 ? RT[r] : M[r][c + 2]);
                 else v = make_float2(M[r][c], M[r][c + 1]);
-                acc = k == 0 ? v : __fadd2_rn(acc, v);
+                acc = k == 0 ? v : tb_add2(acc, v);
             }
-            const float2 o = TbPairOp<OpF>::finish(acc, make_float2(M[r][c], M[r][c + 1]), p);
-            res[r][c] = o.x;
-            res[r][c + 1] = o.y;
+            res[r][c] = OpF::finish(acc.x, M[r][c], p);
+            res[r][c + 1] = OpF::finish(acc.y, M[r][c + 1], p);
         }
 }
 
@@ -543,10 +545,14 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     *done = 0;
     const bool keep = (flags & STC_KEEP_F32) != 0 && (a->dtype == STC_BF16 || a->dtype == STC_F16);
     if (nsteps < 1) return STC_OK;
-    const char* env = getenv("STC_TBLOCK");   // tuning / test override: 0 disables the blocked path
-    const bool disabled = env && env[0] == '0';
+    // tuning / test override: STC_TBLOCK=0 disables the blocked path, =1 takes it for 16-bit state too
+    const char* env = getenv("STC_TBLOCK");
+    const bool disabled = env && env[0] == '0', forced = env && env[0] == '1';
     if (!tb3d_applies(a, st, op, bc) || disabled) return keep ? STC_ERR_UNSUPPORTED : STC_OK;
     if (!keep && nsteps < 8) return STC_OK;   // copies in and out would outweigh the saving
+    // 16-bit state rounded every step: the per-step vector map moves half the bytes of Float32 and was
+    // measured faster than the blocked kernel (711 against 557 Gcell/s on 512^3 x 200 BFloat16)
+    if (!keep && !forced && a->dtype != STC_F32) return STC_OK;
     TbLaunch fn = tb_find(a, st, op);
     const int es = dtype_size(a->dtype);
     const bool halo = bc->padding != STC_CONDITIONAL;
