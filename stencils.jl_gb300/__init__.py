@@ -11,7 +11,8 @@ from .array import (AbstractStencilArray, StencilArray, SwitchingStencilArray, c
 from ._abi import ArgumentError
 from .batch import Batch
 from .boundary import Conditional, Halo, Reflect, Remove, Use, Wrap
-from .gather import gatherstencil, gatherstencil_, mapstencil, mapstencil_, mass, update_boundary_
+from .gather import (copy_to_device_, copy_to_host_, gatherstencil, gatherstencil_, mapstencil, mapstencil_, mass,
+                     update_boundary_)
 from .ops import Diffusion, LifeRule, Scaled, Terms, center, kernelproduct, life, maximum, mean, minimum, scaled, value
 from .ops import sum  # noqa: A004
 from .scatter import ScatterConst, scatter_center, scatter_weighted, scatterstencil_
@@ -25,6 +26,7 @@ __all__ = [
     "AbstractStencilArray", "StencilArray", "SwitchingStencilArray", "switch", "colmajor_empty", "colmajor_like",
     "colmajor_zeros", "to_device", "to_host", "ArgumentError", "Conditional", "Halo", "Reflect", "Remove", "Use",
     "Wrap", "gatherstencil", "gatherstencil_", "mapstencil", "mapstencil_", "mass", "update_boundary_",
+    "copy_to_device_", "copy_to_host_",
     "Diffusion", "LifeRule", "kernelproduct", "life", "maximum", "mean", "minimum", "sum", "Terms", "Scaled",
     "scaled", "center", "value", "scatterstencil_", "ScatterConst", "scatter_center", "scatter_weighted",
     "AngledCross",

@@ -54,6 +54,8 @@ def load(path: str | Path | None = None):
         "stc_map_steps": ([P(A.Grid), P(A.Grid), P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc), C.c_int64,
                            P(C.c_int32), vp, C.c_uint32], C.c_int),
         "stc_update_boundary": ([P(A.Grid), C.c_int32, P(A.BcDesc), vp, C.c_uint32], C.c_int),
+        "stc_grid_upload": ([P(A.Grid), vp, vp, C.c_uint32], C.c_int),
+        "stc_grid_download": ([vp, P(A.Grid), vp, C.c_uint32], C.c_int),
         "stc_map_terms": ([P(A.TermDesc), C.c_int32, P(A.Grid), C.c_int32, vp, C.c_uint32], C.c_int),
         "stc_scatter": ([P(A.Grid), P(A.Grid), P(A.StencilDesc), vp, P(A.BcDesc), vp, C.c_uint32], C.c_int),
         "stc_mass": ([P(A.Grid), C.c_int32, P(A.BcDesc), P(C.c_double), vp], C.c_int),

@@ -711,6 +711,47 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
     return rc;
 }
 
+// Host <-> device copies of a grid whose device side may be a strided view (the interior of a Halo
+// parent): one pitched copy (2D: cudaMemcpy2DAsync, 3D: cudaMemcpy3DAsync), no staging kernel.
+static int host_grid_copy(const stc_grid* g, void* host, bool upload, void* stream, uint32_t flags) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!host) return STC_ERR_INVALID;
+    const size_t es = (size_t)dtype_size(g->dtype);
+    const size_t w = (size_t)g->size[0] * es;
+    const size_t h = g->ndims >= 2 ? (size_t)g->size[1] : 1, d = g->ndims >= 3 ? (size_t)g->size[2] : 1;
+    if (!w || !h || !d) return STC_OK;
+    if (!g->data) return STC_ERR_INVALID;
+    const size_t dpitch = g->ndims >= 2 ? (size_t)g->stride[1] * es : w;
+    if (g->ndims >= 2 && dpitch < w) return STC_ERR_INVALID;
+    if (g->ndims == 3 && (size_t)g->stride[2] != (size_t)g->stride[1] * h) {
+        // planes not stacked at one pitch: one 2D copy per plane
+        for (size_t z = 0; z < d && !rc; ++z) {
+            char* dp = (char*)g->data + z * (size_t)g->stride[2] * es;
+            char* hp = (char*)host + z * w * h;
+            cudaError_t e = upload ? cudaMemcpy2DAsync(dp, dpitch, hp, w, w, h, cudaMemcpyHostToDevice, (cudaStream_t)stream)
+                                   : cudaMemcpy2DAsync(hp, w, dp, dpitch, w, h, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+            rc = cuda_fail(e);
+        }
+    } else {
+        cudaError_t e = upload
+            ? cudaMemcpy2DAsync(g->data, dpitch, host, w, w, h * d, cudaMemcpyHostToDevice, (cudaStream_t)stream)
+            : cudaMemcpy2DAsync(host, w, g->data, dpitch, w, h * d, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+        rc = cuda_fail(e);
+    }
+    if (rc) return rc;
+    if (!(flags & STC_ASYNC)) rc = cuda_fail(cudaStreamSynchronize((cudaStream_t)stream));
+    return rc;
+}
+
+int stc_grid_upload(const stc_grid* dst, const void* host, void* stream, uint32_t flags) {
+    return host_grid_copy(dst, (void*)host, true, stream, flags);
+}
+
+int stc_grid_download(void* host, const stc_grid* src, void* stream, uint32_t flags) {
+    return host_grid_copy(src, host, false, stream, flags);
+}
+
 int stc_update_boundary(const stc_grid* parent, int32_t radius, const stc_bc* bc, void* stream, uint32_t flags) {
     int rc = check_grid(parent);
     if (rc) return rc;

@@ -240,6 +240,47 @@ def update_boundary_(A_: AbstractStencilArray):
     return A_
 
 
+def _host_ptr(host, nbytes: int) -> int:
+    if _is_torch(host):
+        if host.device.type != "cpu" or not host.is_contiguous():
+            raise TypeError("host tensor must be a contiguous CPU tensor")
+        ptr, size = host.data_ptr(), host.numel() * host.element_size()
+    else:
+        a = np.asarray(host)
+        if not a.flags.f_contiguous:
+            raise TypeError("host array must be column-major contiguous (order='F')")
+        ptr, size = a.ctypes.data, a.nbytes
+    if size != nbytes:
+        raise ValueError(f"host buffer holds {size} bytes, the grid {nbytes}")
+    return ptr
+
+
+def copy_to_device_(dst, host, sync: bool = True):
+    """Copy host data into the device grid `dst` (a column-major tensor, or a strided view of one such as
+    a Halo parent's interior) as one pitched copy (stc_grid_upload).  `host` is a column-major numpy
+    array of dst's size and type, or a contiguous CPU tensor holding the same bytes (pinned memory makes
+    the copy asynchronous; with sync=False it must stay valid until the stream reaches the copy)."""
+    _require_device(dst)
+    lib = _lib.load()
+    g = _grid(dst)
+    ptr = _host_ptr(host, dst.numel() * dst.element_size())
+    _lib.check(lib.stc_grid_upload(C.byref(g), C.c_void_p(ptr), _lib.current_stream_handle(),
+                                   0 if sync else A.STC_ASYNC), "copy_to_device_")
+    return dst
+
+
+def copy_to_host_(host, src, sync: bool = True):
+    """Copy the device grid `src` (possibly a strided view) into host memory laid out column-major
+    (stc_grid_download); the counterpart of copy_to_device_."""
+    _require_device(src)
+    lib = _lib.load()
+    g = _grid(src)
+    ptr = _host_ptr(host, src.numel() * src.element_size())
+    _lib.check(lib.stc_grid_download(C.c_void_p(ptr), C.byref(g), _lib.current_stream_handle(),
+                                     0 if sync else A.STC_ASYNC), "copy_to_host_")
+    return host
+
+
 def mass(x, radius: int = 0, padding=None) -> float:
     """FP64 compensated total of a device grid's logical cells."""
     lib = _lib.load()
