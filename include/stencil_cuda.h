@@ -42,7 +42,7 @@ extern "C" {
 #define STC_API
 #endif
 
-#define STC_ABI_VERSION 1
+#define STC_ABI_VERSION 2
 
 /* ---- status codes (the reference's ArgumentError sites in comments) ---- */
 typedef enum {
@@ -60,7 +60,9 @@ typedef enum {
     STC_ERR_BUDGET = -9,          /* request exceeds the server's HBM budget */
     STC_ERR_BUSY = -10,           /* result not ready / queue full */
     STC_ERR_CANCELLED = -11,      /* job was cancelled before it finished */
-    STC_ERR_TOO_LARGE = -12       /* grid larger than the fixed scratch of stc_life_steps_noalloc */
+    STC_ERR_TOO_LARGE = -12,      /* grid larger than the fixed scratch of stc_life_steps_noalloc */
+    STC_ERR_INEXACT = -13         /* a result does not convert exactly to the destination element type
+                                     (the reference's InexactError on setindex!) */
 } stc_status;
 
 /* ---- element types ---- */
@@ -139,6 +141,12 @@ typedef struct {
     int32_t padding;          /* stc_padding */
     double  padval;           /* Remove(padval) for float grids */
     int64_t padval_int;       /* Remove(padval) for integer / Bool grids */
+    int32_t padval_type;      /* Remove: the type of padval, 1 + stc_dtype, or 0 for the grid's own element type
+                                 (the reference's default Remove(zero(eltype)), src/array.jl:463).  A padval of
+                                 another type promotes the neighbours: they are read as
+                                 promote_type(eltype, typeof(padval)) (src/gatherstencil.jl:41-56, :50), so the
+                                 fold runs in that type and the result type follows it (stc_neighbor_dtype). */
+    int32_t reserved;
 } stc_bc;
 
 /* stc_map flags */
@@ -167,9 +175,15 @@ STC_API int         stc_last_cuda_error(void);              /* the cudaError_t b
  * host thread holds it at that moment. */
 STC_API int         stc_release_workspace(void);
 
-/* Output element type the reference would infer for (op, source dtype, weight dtype)
+/* Output element type the reference would infer for (op, neighbour dtype, weight dtype)
  * (Base._return_type, src/gatherstencil.jl:41-56), or a negative status. */
 STC_API int stc_result_dtype(int32_t opcode, int32_t src_dtype, int32_t weight_dtype);
+/* The element type a grid's neighbours are read as: promote_type(src_dtype, typeof(padval)) for Remove
+ * with a padval_type (src/gatherstencil.jl:50), else src_dtype; a negative status for a bad padval_type.
+ * stc_map writes the result type of that type; stc_map_steps converts each step's result back to the
+ * parents' type (STC_ERR_INEXACT where a value does not convert exactly, as the reference's setindex!
+ * throws).  The other entry points take grids whose padval needs no promotion (else STC_ERR_UNSUPPORTED). */
+STC_API int stc_neighbor_dtype(int32_t src_dtype, const stc_bc* bc);
 
 /* One map: dst[I] = f(stencil(src, I)) for every logical index I.  `src` is the parent array;
  * its logical size is size - 2R per axis for Halo padding.  `dst` is either the logical size

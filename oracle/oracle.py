@@ -97,13 +97,70 @@ def _grid(a: np.ndarray, code: int):
     return grid_from_numpy(a, code)
 
 
+# Julia's promote_type over the element types the oracle takes (Bool gives way to anything; an integer and a
+# float give the float; integers the wider, UInt8 < Int32 < Int64; floats the wider, BFloat16 with Float16 giving
+# Float32), restated here for the padval promotion of src/gatherstencil.jl:50.
+def promote_code(a: int, b: int) -> int:
+    from stencils_gb300 import _abi as A
+    if a == b:
+        return a
+    if a == A.BOOL:
+        return b
+    if b == A.BOOL:
+        return a
+    fa, fb = a in A.FLOAT_DTYPES, b in A.FLOAT_DTYPES
+    if fa != fb:
+        return a if fa else b
+    if not fa:
+        rank = {A.U8: 1, A.I32: 2, A.I64: 3}
+        return a if rank[a] >= rank[b] else b
+    if A.F64 in (a, b):
+        return A.F64
+    return A.F32
+
+
+def neighbor_code(src_code: int, boundary) -> int:
+    """promote_type(eltype, typeof(padval)) for Remove (src/gatherstencil.jl:41-56, :50), else eltype; the
+    padval's type follows the Python layer's lowering rule (stencils_gb300._abi.padval_type_code)."""
+    from stencils_gb300 import _abi as A
+    from stencils_gb300.boundary import Remove
+    if not isinstance(boundary, Remove):
+        return src_code
+    pt = A.padval_type_code(boundary.padval, src_code)
+    return src_code if pt == 0 else promote_code(src_code, pt - 1)
+
+
+def convert_array(a: np.ndarray, frm: int, to: int) -> np.ndarray:
+    """Julia's convert(T, x) elementwise: to a float type round to nearest; to an integer or Bool type the
+    value must be exact (else ValueError, the reference's InexactError)."""
+    from stencils_gb300 import _abi as A
+    if frm == to:
+        return np.asfortranarray(a)
+    x = bf16_bits_to_f32(a).reshape(a.shape) if frm == A.BF16 else np.asarray(a)
+    if to in A.FLOAT_DTYPES:
+        if to == A.BF16:
+            return np.asfortranarray(f32_to_bf16_bits(x.astype(np.float64).astype(np.float32)))
+        return np.asfortranarray(x.astype(A.NP_DTYPE[to]))
+    xf = x.astype(np.float64) if x.dtype.kind == "f" else x
+    lo, hi = {A.U8: (0, 255), A.BOOL: (0, 1), A.I32: (-2**31, 2**31 - 1), A.I64: (-2**63, 2**63 - 1)}[to]
+    if x.dtype.kind == "f" and not np.all(np.isfinite(xf) & (xf == np.trunc(xf))):
+        raise ValueError("InexactError: non-integral value")
+    if np.any(xf < lo) or np.any(xf > hi):
+        raise ValueError("InexactError: value out of range")
+    return np.asfortranarray(x.astype(A.NP_DTYPE[to]))
+
+
 def map(src: np.ndarray, src_code: int, stencil, red, boundary, padding, *,
         dst_code: int | None = None, dst_padded: bool = False, nthreads: int = 1) -> np.ndarray:
-    """dst = mapstencil(f, StencilArray(src parent, ...)); updates src's halo like the reference."""
+    """dst = mapstencil(f, StencilArray(src parent, ...)); updates src's halo like the reference.  A Remove
+    padval of another type promotes the neighbours first (the parent converted to the promoted type)."""
     from stencils_gb300 import _abi as A
+    ndt = neighbor_code(src_code, boundary)
+    if ndt != src_code:
+        src, src_code = convert_array(src, src_code, ndt), ndt
     lst = A.LoweredStencil(stencil)
     op = A.lower_op(red)
-    bc = A.lower_bc(boundary, padding)
+    bc = A.lower_bc(boundary, padding, src_code)
     if dst_code is None:
         dst_code = result_dtype(red, src_code, lst.desc.weight_dtype)
     R = stencil.radius
@@ -121,7 +178,7 @@ def map_into(src: np.ndarray, src_code: int, dst: np.ndarray, dst_code: int, ste
     from stencils_gb300 import _abi as A
     lst = A.LoweredStencil(stencil)
     op = A.lower_op(red)
-    bc = A.lower_bc(boundary, padding)
+    bc = A.lower_bc(boundary, padding, src_code)
     gs, gd = _grid(src, src_code), _grid(dst, dst_code)
     _check(lib().orc_map(C.byref(gs), C.byref(gd), int(dst_padded), C.byref(lst.desc), C.byref(op),
                          C.byref(bc), nthreads), "map")
@@ -129,11 +186,24 @@ def map_into(src: np.ndarray, src_code: int, dst: np.ndarray, dst_code: int, ste
 
 def map_steps(a: np.ndarray, b: np.ndarray, code: int, stencil, red, boundary, padding, nsteps: int,
               *, nthreads: int = 1) -> bool:
-    """nsteps of A = mapstencil!(f, A) on parents (a, b); returns True if b holds the result."""
+    """nsteps of A = mapstencil!(f, A) on parents (a, b); returns True if b holds the result.  With a
+    promoting padval (Conditional padding), every step maps the promoted neighbours and converts the
+    result back into the dest parent's type, as the reference's setindex! does."""
     from stencils_gb300 import _abi as A
+    ndt = neighbor_code(code, boundary)
+    if ndt != code:
+        if padding.code != 0:
+            raise NotImplementedError("the oracle restates promoted multi-step runs on Conditional grids")
+        grids, cur = [a, b], 0
+        for _ in range(nsteps):
+            y = map(grids[cur], code, stencil, red, boundary, padding, nthreads=nthreads)
+            rdt = result_dtype(red, ndt, A.LoweredStencil(stencil).desc.weight_dtype)
+            grids[1 - cur][...] = convert_array(y, rdt, code)
+            cur = 1 - cur
+        return cur == 1
     lst = A.LoweredStencil(stencil)
     op = A.lower_op(red)
-    bc = A.lower_bc(boundary, padding)
+    bc = A.lower_bc(boundary, padding, code)
     ga, gb = _grid(a, code), _grid(b, code)
     out = C.c_int(0)
     _check(lib().orc_map_steps(C.byref(ga), C.byref(gb), C.byref(lst.desc), C.byref(op), C.byref(bc),

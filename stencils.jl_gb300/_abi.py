@@ -19,7 +19,7 @@ STATUS_NAMES = {
     0: "STC_OK", -1: "STC_ERR_SIZE_MISMATCH", -2: "STC_ERR_RADIUS", -3: "STC_ERR_KERNEL_LENGTH",
     -4: "STC_ERR_UNSUPPORTED", -5: "STC_ERR_INVALID", -6: "STC_ERR_CUDA", -7: "STC_ERR_TIMEOUT",
     -8: "STC_ERR_NO_DEVICE", -9: "STC_ERR_BUDGET", -10: "STC_ERR_BUSY", -11: "STC_ERR_CANCELLED",
-    -12: "STC_ERR_TOO_LARGE",
+    -12: "STC_ERR_TOO_LARGE", -13: "STC_ERR_INEXACT",
 }
 STC_ERR_BUSY = -10
 STC_ASYNC = 1
@@ -79,7 +79,7 @@ class OpDesc(C.Structure):
 
 class BcDesc(C.Structure):
     _fields_ = [("boundary", C.c_int32), ("padding", C.c_int32), ("padval", C.c_double),
-                ("padval_int", C.c_int64)]
+                ("padval_int", C.c_int64), ("padval_type", C.c_int32), ("reserved", C.c_int32)]
 
 
 # stc_term_kind
@@ -164,7 +164,47 @@ def lower_op(red) -> OpDesc:
     return o
 
 
-def lower_bc(boundary, padding) -> BcDesc:
+_NP_CODE = {np.dtype(np.float64): F64, np.dtype(np.float32): F32, np.dtype(np.float16): F16,
+            np.dtype(np.uint8): U8, np.dtype(np.bool_): BOOL, np.dtype(np.int32): I32, np.dtype(np.int64): I64}
+
+
+def _fits(pv, code) -> bool:
+    """True if the Python number pv is exactly a value of element type `code`."""
+    if code in (F64, F32, F16):
+        return bool(np.array(pv, dtype=NP_DTYPE[code]).astype(np.float64) == pv) or pv != pv
+    if code == BF16:
+        f = np.float32(pv)
+        return bool(f == pv and (f.view(np.uint32) & 0xFFFF) == 0) or pv != pv
+    if isinstance(pv, float) and not float(pv).is_integer():
+        return False
+    lo, hi = {U8: (0, 255), BOOL: (0, 1), I32: (-2**31, 2**31 - 1), I64: (-2**63, 2**63 - 1)}[code]
+    return lo <= int(pv) <= hi
+
+
+def padval_type_code(pv, grid_code: int | None) -> int:
+    """The padval's element type for stc_bc.padval_type (1 + dtype code; 0 = the grid's own type).
+
+    The reference promotes the neighbours to promote_type(eltype, typeof(padval)) (src/gatherstencil.jl:50).
+    A numpy scalar carries its type (np.float64(0.0) on a Float32 grid promotes to Float64, as Julia's
+    Remove(0.0) does).  A Python bool is Julia's Bool.  A plain Python number has no Julia type: it is
+    taken as the grid's element type when it is exactly a value of that type (the reference's default
+    Remove(zero(eltype))), else as Julia's Int64 (int) or Float64 (float), so Remove(0.5) on a UInt8 grid
+    promotes to Float64 instead of silently becoming 0."""
+    if isinstance(pv, (np.generic,)) and np.dtype(type(pv)) in _NP_CODE:
+        code = _NP_CODE[np.dtype(type(pv))]
+        return 0 if code == grid_code else code + 1
+    if grid_code is None or grid_code == BOOL and isinstance(pv, (bool, np.bool_)):
+        return 0     # no grid type to compare with: a plain number is taken as the grid's own type
+    if isinstance(pv, (bool, np.bool_)):
+        return BOOL + 1
+    if _fits(pv, grid_code):
+        return 0
+    return (I64 if isinstance(pv, (int, np.integer)) else F64) + 1
+
+
+def lower_bc(boundary, padding, grid_code: int | None = None) -> BcDesc:
+    """The stc_bc of (boundary, padding); grid_code (the grid's element type) decides whether a plain
+    Python padval promotes the neighbours (see padval_type_code)."""
     from .boundary import Remove
     b = BcDesc()
     b.boundary = boundary.code
@@ -173,6 +213,7 @@ def lower_bc(boundary, padding) -> BcDesc:
         pv = boundary.padval
         if pv is None:
             raise ValueError("Remove() without a padval cannot feed a numeric reduction; use Remove(0)")
+        b.padval_type = padval_type_code(pv, grid_code)
         if isinstance(pv, (bool, np.bool_)):
             pv = int(pv)
         b.padval = float(pv)

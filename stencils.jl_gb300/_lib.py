@@ -49,6 +49,7 @@ def load(path: str | Path | None = None):
         "stc_last_cuda_error": ([], C.c_int),
         "stc_release_workspace": ([], C.c_int),
         "stc_result_dtype": ([C.c_int32, C.c_int32, C.c_int32], C.c_int),
+        "stc_neighbor_dtype": ([C.c_int32, P(A.BcDesc)], C.c_int),
         "stc_map": ([P(A.Grid), P(A.Grid), C.c_int32, P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc), vp, C.c_uint32],
                     C.c_int),
         "stc_map_steps": ([P(A.Grid), P(A.Grid), P(A.StencilDesc), P(A.OpDesc), P(A.BcDesc), C.c_int64,

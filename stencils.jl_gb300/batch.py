@@ -29,7 +29,7 @@ class Batch:
             raise NotImplementedError("batched jobs use Conditional padding")
         st = A.LoweredStencil(S.stencil)
         op = A.lower_op(red)
-        bc = A.lower_bc(S.boundary, S.padding)
+        bc = A.lower_bc(S.boundary, S.padding, A.torch_dtype_code(S.source.dtype))
         ga, gb = A.grid_from_torch(S.source), A.grid_from_torch(S.dest)
         rc = self._lib.stc_batch_add(self._h, C.byref(ga), C.byref(gb), C.byref(st.desc), C.byref(op),
                                      C.byref(bc), int(steps))

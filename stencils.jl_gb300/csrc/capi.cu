@@ -181,11 +181,37 @@ static int finish_sync(cudaStream_t s, DeviceCtx* ctx) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e);
     volatile int* h = ctx->status_host;
-    if (*h) {
+    const int v = *h;
+    if (v) {
         *h = 0;
-        return STC_ERR_TIMEOUT;
+        return (v & DEV_ERR_TIMEOUT) ? STC_ERR_TIMEOUT : STC_ERR_INEXACT;
     }
     return STC_OK;
+}
+
+// ---------------------------------------------------------------------------- type promotion
+// Julia's promote_type over the element types the library takes: Bool gives way to anything; an
+// integer and a float give the float; integers the wider (UInt8 < Int32 < Int64); floats the wider, with
+// BFloat16 and Float16 meeting at Float32 (BFloat16s.jl's promote_rule).
+int promote_dtype(int a, int b) {
+    if (a == b) return a;
+    if (a == STC_BOOL) return b;
+    if (b == STC_BOOL) return a;
+    const bool fa = is_float_dtype(a), fb = is_float_dtype(b);
+    if (fa != fb) return fa ? a : b;
+    if (!fa) {
+        auto rank = [](int d) { return d == STC_U8 ? 1 : d == STC_I32 ? 2 : 3; };
+        return rank(a) >= rank(b) ? a : b;
+    }
+    if (a == STC_F64 || b == STC_F64) return STC_F64;
+    return STC_F32;   // F32 with a 16-bit type, or BFloat16 with Float16
+}
+
+int neighbor_dtype(int src, const stc_bc* bc) {
+    if (!bc || bc->boundary != STC_REMOVE || bc->padval_type == 0) return src;
+    const int pt = bc->padval_type - 1;
+    if (pt < 0 || dtype_size(pt) == 0) return STC_ERR_INVALID;
+    return promote_dtype(src, pt);
 }
 
 // ---------------------------------------------------------------------------- tensor maps
@@ -290,7 +316,9 @@ int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const
     if (bc->boundary < STC_REMOVE || bc->boundary > STC_USE) return STC_ERR_INVALID;
     if (bc->padding < STC_CONDITIONAL || bc->padding > STC_HALO_OUT) return STC_ERR_INVALID;
     if (bc->boundary == STC_USE && bc->padding == STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
-    const int rdt = result_dtype(op->code, src->dtype, st->weight_dtype);
+    const int ndt = neighbor_dtype(src->dtype, bc);
+    if (ndt < 0) return ndt;
+    const int rdt = result_dtype(op->code, ndt, st->weight_dtype);
     if (rdt < 0) return rdt;
     if (dst->dtype != rdt) return STC_ERR_UNSUPPORTED;
     if (dst->ndims != src->ndims) return STC_ERR_SIZE_MISMATCH;
@@ -554,6 +582,7 @@ const char* stc_strerror(int status) {
     case STC_ERR_BUSY: return "not finished";
     case STC_ERR_CANCELLED: return "cancelled";
     case STC_ERR_TOO_LARGE: return "grid exceeds the fixed no-allocation scratch (4096*4096 cells)";
+    case STC_ERR_INEXACT: return "InexactError: a result does not convert exactly to the destination element type";
     }
     return "unknown status";
 }
@@ -582,6 +611,54 @@ int stc_result_dtype(int32_t opcode, int32_t src_dtype, int32_t weight_dtype) {
     return result_dtype(opcode, src_dtype, weight_dtype);
 }
 
+int stc_neighbor_dtype(int32_t src_dtype, const stc_bc* bc) {
+    if (dtype_size(src_dtype) == 0) return STC_ERR_INVALID;
+    return neighbor_dtype(src_dtype, bc);
+}
+
+}  // extern "C"
+
+namespace stc {
+// A dense device grid of `dt` with g's sizes, in stream-ordered memory (freed with cudaFreeAsync).
+static int dense_like(const stc_grid* g, int dt, stc_grid* out, cudaStream_t s) {
+    *out = *g;
+    out->dtype = dt;
+    int64_t cells = 1;
+    for (int d = 0; d < 3; ++d) {
+        const int64_t n = d < g->ndims ? g->size[d] : 1;
+        out->stride[d] = d < g->ndims ? cells : 0;
+        cells *= n;
+    }
+    out->data = nullptr;
+    cudaError_t e = cudaMallocAsync(&out->data, (size_t)std::max<int64_t>(cells, 1) * dtype_size(dt), s);
+    return cuda_fail(e);
+}
+
+static void sizes3(const stc_grid* g, int64_t n[3]) {
+    for (int d = 0; d < 3; ++d) n[d] = d < g->ndims ? g->size[d] : 1;
+}
+
+// stc_map with a padval of another type: the source parent (ring included) is converted to the
+// neighbour type promote_type(eltype, typeof(padval)) (src/gatherstencil.jl:50) and mapped from there.
+static int map_promoted(const stc_grid* src, const stc_grid* dst, int dst_padded, const stc_stencil* st,
+                        const stc_op* op, const stc_bc* bc, int ndt, cudaStream_t s, DeviceCtx* ctx) {
+    stc_grid t;
+    int rc = dense_like(src, ndt, &t, s);
+    if (rc) return rc;
+    int64_t n[3];
+    sizes3(src, n);
+    stc_bc b2 = *bc;
+    b2.padval_type = 0;
+    rc = launch_grid_convert(src, 0, &t, 0, n, ctx->status, s);
+    if (!rc) rc = launch_halo_fill(&t, st->radius, &b2, s);
+    if (!rc) rc = launch_map(&t, dst, dst_padded, st, op, &b2, s, ctx);
+    cudaFreeAsync(t.data, s);
+    return rc;
+}
+}  // namespace stc
+
+extern "C" {
+
 int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded, const stc_stencil* st, const stc_op* op,
             const stc_bc* bc, void* stream, uint32_t flags) {
     int rc = validate_map(src, dst, dst_padded, st, op, bc);
@@ -590,6 +667,11 @@ int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded, const 
     DeviceCtx* ctx = nullptr;
     if ((rc = device_ctx(&ctx))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
+    const int ndt = neighbor_dtype(src->dtype, bc);
+    if (ndt != src->dtype) {
+        if ((rc = map_promoted(src, dst, dst_padded, st, op, bc, ndt, s, ctx))) return rc;
+        return (flags & STC_ASYNC) ? STC_OK : finish_sync(s, ctx);
+    }
     if ((rc = launch_halo_fill(src, st->radius, bc, s))) return rc;
     if ((rc = launch_map(src, dst, dst_padded, st, op, bc, s, ctx))) return rc;
     if (!(flags & STC_ASYNC)) rc = finish_sync(s, ctx);
@@ -666,6 +748,60 @@ static int padded_steps(const stc_grid* a, const stc_grid* b, const stc_stencil*
     *done = nsteps;
     return STC_OK;
 }
+// stc_map_steps with a padval of another type: every step reads the neighbours in the promoted type
+// (the source parent converted), maps into a result of that type's result type, and converts it back
+// into the dest parent, as the reference's setindex! does (InexactError where it is not exact).
+static int map_steps_promoted(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op,
+                              const stc_bc* bc, int ndt, int64_t nsteps, int32_t* out_src_is_b, void* stream,
+                              uint32_t flags) {
+    if (check_grid(b) || !st || !op) return STC_ERR_INVALID;
+    for (int d = 0; d < a->ndims; ++d)
+        if (a->size[d] != b->size[d] || a->dtype != b->dtype) return STC_ERR_SIZE_MISMATCH;
+    const int rdt = result_dtype(op->code, ndt, st->weight_dtype);
+    if (rdt < 0) return rdt;
+    stc_grid fake = *a;   // the step's result: a parent of the result type
+    fake.dtype = rdt;
+    int rc = validate_map(a, &fake, 1, st, op, bc);
+    if (rc) return rc;
+    if (nsteps > 0 && grids_overlap(a, b)) return STC_ERR_INVALID;
+    DeviceCtx* ctx = nullptr;
+    if ((rc = device_ctx(&ctx))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int src_is_b = 0;
+    if (nsteps > 0) {
+        stc_grid tin, tout;
+        if ((rc = dense_like(a, ndt, &tin, s))) return rc;
+        if ((rc = dense_like(a, rdt, &tout, s))) { cudaFreeAsync(tin.data, s); return rc; }
+        stc_bc b2 = *bc;
+        b2.padval_type = 0;
+        const bool halo = bc->padding != STC_CONDITIONAL;
+        const int R = halo ? st->radius : 0;
+        int64_t whole[3], n[3];
+        sizes3(a, whole);
+        for (int d = 0; d < 3; ++d) n[d] = d < a->ndims ? a->size[d] - 2 * R : 1;
+        auto org = [&](const stc_grid* g) {
+            int64_t o = 0;
+            for (int d = 0; d < g->ndims; ++d) o += (int64_t)R * g->stride[d];
+            return o;
+        };
+        const stc_grid* grids[2] = {a, b};
+        for (int64_t k = 0; k < nsteps && !rc; ++k) {
+            const stc_grid* sg = grids[src_is_b];
+            const stc_grid* dg = grids[1 - src_is_b];
+            rc = launch_grid_convert(sg, 0, &tin, 0, whole, ctx->status, s);
+            if (!rc) rc = launch_halo_fill(&tin, st->radius, &b2, s);
+            if (!rc) rc = launch_map(&tin, &tout, 1, st, op, &b2, s, ctx);
+            if (!rc) rc = launch_grid_convert(&tout, org(&tout), dg, org(dg), n, ctx->status, s);
+            src_is_b = 1 - src_is_b;
+        }
+        cudaFreeAsync(tin.data, s);
+        cudaFreeAsync(tout.data, s);
+        if (rc) return rc;
+    }
+    if (out_src_is_b) *out_src_is_b = src_is_b;
+    return (flags & STC_ASYNC) ? STC_OK : finish_sync(s, ctx);
+}
+
 }  // namespace stc
 
 extern "C" {
@@ -673,6 +809,10 @@ extern "C" {
 int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
                   int64_t nsteps, int32_t* out_src_is_b, void* stream, uint32_t flags) {
     if (nsteps < 0) return STC_ERR_INVALID;
+    if (check_grid(a) || !bc) return STC_ERR_INVALID;
+    const int ndt = neighbor_dtype(a->dtype, bc);
+    if (ndt < 0) return ndt;
+    if (ndt != a->dtype) return map_steps_promoted(a, b, st, op, bc, ndt, nsteps, out_src_is_b, stream, flags);
     int rc = validate_map(a, b, 1, st, op, bc);
     if (rc) return rc;
     for (int d = 0; d < a->ndims; ++d)

@@ -17,7 +17,7 @@ namespace stc {
 
 // ------------------------------------------------------------------ status word
 // Kernels that give up a bounded wait OR a bit into this word; the host reads and clears it.
-enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BOUNDS = 2 };
+enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BOUNDS = 2, DEV_ERR_INEXACT = 4 };
 
 // ------------------------------------------------------------------ element traits
 template <int DT> struct Elem;

@@ -59,6 +59,10 @@ int validate_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const
 // true if the two grids' element byte ranges intersect
 bool grids_overlap(const stc_grid* a, const stc_grid* b);
 int result_dtype(int op, int sdt, int wdt);
+// Julia's promote_type over the library's element types, and the type a grid's neighbours are read as
+// (promote_type(eltype, typeof(padval)) for Remove with a padval_type; a negative status if malformed)
+int promote_dtype(int a, int b);
+int neighbor_dtype(int src, const stc_bc* bc);
 // true if the FMA-corrected Float32 quotient by L is exact for every input (checked once per L)
 bool fastdiv_f_exact(int L);
 // true if `offsets` (len entries of N components) is the table Stencils.jl generates for the shape
@@ -73,5 +77,9 @@ int launch_halo_fill(const stc_grid* parent, int radius, const stc_bc* bc, cudaS
 // copy an n[0] x n[1] x n[2] box from src (element offset sorg) to dst (offset dorg), same dtype
 int launch_grid_copy(const stc_grid* src, int64_t sorg, const stc_grid* dst, int64_t dorg, const int64_t n[3],
                      cudaStream_t stream);
+// the same box converted from src's element type to dst's as Julia's convert does (round to nearest into
+// a float type; into an integer or Bool type only exact values, else DEV_ERR_INEXACT in *status)
+int launch_grid_convert(const stc_grid* src, int64_t sorg, const stc_grid* dst, int64_t dorg, const int64_t n[3],
+                        int* status, cudaStream_t stream);
 
 }  // namespace stc

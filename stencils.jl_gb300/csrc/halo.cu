@@ -6,6 +6,8 @@
 // (Wrap / Reflect, src/array.jl:154-179).  Every halo cell depends only on interior cells, so the
 // slabs are written in one launch; cells shared by two slabs receive the same value from both.
 #include <algorithm>
+#include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 #include "dispatch.h"
@@ -198,6 +200,126 @@ int launch_grid_copy(const stc_grid* src, int64_t sorg, const stc_grid* dst, int
     default: return STC_ERR_UNSUPPORTED;
     }
     return cuda_fail(cudaGetLastError());
+}
+
+// ------------------------------------------------------------------ box conversion between element types
+// Julia's convert(TO, x): into a float type round to nearest; into an integer type only an exactly
+// representable value (else InexactError: the status bit), into Bool only 0 or 1.  Integer sources go
+// through Float64 into a 16-bit float (exact below 2^53).
+template <class TI> __device__ __forceinline__ double cv_f64(TI v) {
+    if constexpr (std::is_same_v<TI, __nv_bfloat16>) return (double)__bfloat162float(v);
+    else if constexpr (std::is_same_v<TI, __half>) return (double)__half2float(v);
+    else return (double)v;
+}
+
+template <class TI, class TO, bool TO_BOOL>
+__device__ __forceinline__ TO cv_convert(TI v, bool& ok) {
+    constexpr bool in_int = std::is_integral_v<TI>;
+    constexpr bool out_int = std::is_integral_v<TO>;
+    ok = true;
+    if constexpr (!out_int) {
+        if constexpr (in_int) {
+            const long long i = (long long)v;
+            if constexpr (std::is_same_v<TO, double>) return __ll2double_rn(i);
+            else if constexpr (std::is_same_v<TO, float>) return __ll2float_rn(i);
+            else if constexpr (std::is_same_v<TO, __nv_bfloat16>) return __double2bfloat16(__ll2double_rn(i));
+            else return __double2half(__ll2double_rn(i));
+        } else {
+            const double d = cv_f64(v);
+            if constexpr (std::is_same_v<TO, double>) return d;
+            else if constexpr (std::is_same_v<TO, float>) return __double2float_rn(d);
+            else if constexpr (std::is_same_v<TO, __nv_bfloat16>) return __double2bfloat16(d);
+            else return __double2half(d);
+        }
+    } else {
+        long long i;
+        if constexpr (in_int) {
+            i = (long long)v;
+        } else {
+            const double d = cv_f64(v);
+            ok = d == trunc(d) && d >= -9223372036854775808.0 && d < 9223372036854775808.0;
+            i = ok ? (long long)d : 0;
+        }
+        if constexpr (TO_BOOL) ok = ok && (i == 0 || i == 1);
+        else if constexpr (std::is_same_v<TO, uint8_t>) ok = ok && i >= 0 && i <= 255;
+        else if constexpr (std::is_same_v<TO, int32_t>) ok = ok && i >= INT32_MIN && i <= INT32_MAX;
+        return (TO)i;
+    }
+}
+
+struct ConvertParams {
+    const void* src;
+    void* dst;
+    int64_t sorg, ss1, ss2, dorg, ds1, ds2;
+    int64_t n0, n1, rows;
+    int* status;
+};
+
+template <class TI, class TO, bool TO_BOOL>
+__global__ void grid_convert_kernel(const ConvertParams p) {
+    const TI* src = (const TI*)p.src;
+    TO* dst = (TO*)p.dst;
+    bool all_ok = true;
+    for (int64_t row = blockIdx.x; row < p.rows; row += gridDim.x) {
+        const int64_t y = row % p.n1, z = row / p.n1;
+        const TI* s = src + p.sorg + y * p.ss1 + z * p.ss2;
+        TO* d = dst + p.dorg + y * p.ds1 + z * p.ds2;
+        for (int64_t x = threadIdx.x; x < p.n0; x += blockDim.x) {
+            bool ok;
+            d[x] = cv_convert<TI, TO, TO_BOOL>(s[x], ok);
+            all_ok = all_ok && ok;
+        }
+    }
+    if (!all_ok && p.status) atomicOr(p.status, DEV_ERR_INEXACT);
+}
+
+template <class TI>
+static int convert_from(const ConvertParams& p, int odt, int blocks, int threads, cudaStream_t s) {
+    switch (odt) {
+    case STC_F64: grid_convert_kernel<TI, double, false><<<blocks, threads, 0, s>>>(p); break;
+    case STC_F32: grid_convert_kernel<TI, float, false><<<blocks, threads, 0, s>>>(p); break;
+    case STC_BF16: grid_convert_kernel<TI, __nv_bfloat16, false><<<blocks, threads, 0, s>>>(p); break;
+    case STC_F16: grid_convert_kernel<TI, __half, false><<<blocks, threads, 0, s>>>(p); break;
+    case STC_U8: grid_convert_kernel<TI, uint8_t, false><<<blocks, threads, 0, s>>>(p); break;
+    case STC_BOOL: grid_convert_kernel<TI, uint8_t, true><<<blocks, threads, 0, s>>>(p); break;
+    case STC_I32: grid_convert_kernel<TI, int32_t, false><<<blocks, threads, 0, s>>>(p); break;
+    case STC_I64: grid_convert_kernel<TI, int64_t, false><<<blocks, threads, 0, s>>>(p); break;
+    default: return STC_ERR_UNSUPPORTED;
+    }
+    return cuda_fail(cudaGetLastError());
+}
+
+int launch_grid_convert(const stc_grid* src, int64_t sorg, const stc_grid* dst, int64_t dorg, const int64_t n[3],
+                        int* status, cudaStream_t stream) {
+    DeviceCtx* ctx = nullptr;
+    int rc = device_ctx(&ctx);
+    if (rc) return rc;
+    ConvertParams p{};
+    p.src = src->data;
+    p.dst = dst->data;
+    p.sorg = sorg;
+    p.dorg = dorg;
+    p.ss1 = src->ndims > 1 ? src->stride[1] : 0;
+    p.ss2 = src->ndims > 2 ? src->stride[2] : 0;
+    p.ds1 = dst->ndims > 1 ? dst->stride[1] : 0;
+    p.ds2 = dst->ndims > 2 ? dst->stride[2] : 0;
+    p.n0 = n[0];
+    p.n1 = n[1];
+    p.rows = n[1] * n[2];
+    p.status = status;
+    if (p.n0 < 1 || p.rows < 1) return STC_OK;
+    const int threads = p.n0 >= 256 ? 256 : 128;
+    const int blocks = (int)std::min<int64_t>(p.rows, (int64_t)ctx->num_sms * 16);
+    switch (src->dtype) {
+    case STC_F64: return convert_from<double>(p, dst->dtype, blocks, threads, stream);
+    case STC_F32: return convert_from<float>(p, dst->dtype, blocks, threads, stream);
+    case STC_BF16: return convert_from<__nv_bfloat16>(p, dst->dtype, blocks, threads, stream);
+    case STC_F16: return convert_from<__half>(p, dst->dtype, blocks, threads, stream);
+    case STC_U8: case STC_BOOL: return convert_from<uint8_t>(p, dst->dtype, blocks, threads, stream);
+    case STC_I32: return convert_from<int32_t>(p, dst->dtype, blocks, threads, stream);
+    case STC_I64: return convert_from<int64_t>(p, dst->dtype, blocks, threads, stream);
+    }
+    return STC_ERR_UNSUPPORTED;
 }
 
 }  // namespace stc

@@ -142,6 +142,7 @@ int stc_scatter(const stc_grid* src, const stc_grid* dst, const stc_stencil* st,
     if (!src || !dst || !st || !op || !bc || !src->data || !dst->data || !st->offsets) return STC_ERR_INVALID;
     if (src->ndims != 2 || dst->ndims != 2 || st->ndims != 2) return STC_ERR_UNSUPPORTED;
     if (src->dtype != dst->dtype || (src->dtype != STC_F64 && src->dtype != STC_F32)) return STC_ERR_UNSUPPORTED;
+    if (neighbor_dtype(src->dtype, bc) != src->dtype) return STC_ERR_UNSUPPORTED;   // padval promotion
     if ((src->size[0] > 1 && src->stride[0] != 1) || (dst->size[0] > 1 && dst->stride[0] != 1)) return STC_ERR_INVALID;
     if (op->value < STC_SCATTER_CONST || op->value > STC_SCATTER_WEIGHTED) return STC_ERR_UNSUPPORTED;
     if (op->combine < STC_COMBINE_ADD || op->combine > STC_COMBINE_MIN) return STC_ERR_UNSUPPORTED;

@@ -131,6 +131,7 @@ int stc_map_terms(const stc_term* terms, int32_t nterms, const stc_grid* dst, in
         for (int d = 0; d < nd; ++d)
             if (g->size[d] < 0 || g->stride[d] < 0) return STC_ERR_INVALID;
         if (g->dtype != dt) return STC_ERR_UNSUPPORTED;
+        if (tm.bc && neighbor_dtype(g->dtype, tm.bc) != g->dtype) return STC_ERR_UNSUPPORTED;   // padval promotion
         if (grids_overlap(g, dst)) return STC_ERR_INVALID;   // dest may not share memory with an argument
         if (tm.kind < STC_TERM_CENTER || tm.kind > STC_TERM_VALUE) return STC_ERR_UNSUPPORTED;
         TermDev& t = p.t[m];

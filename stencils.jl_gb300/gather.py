@@ -19,12 +19,20 @@ from .ops import Terms, as_reduction
 from .stencil import Layered, Stencil, with_radius
 
 
-def result_dtype_code(red, src_code: int, stencil) -> int:
+def result_dtype_code(red, src_code: int, stencil, boundary=None, padding=None) -> int:
+    """The reference's result type (src/gatherstencil.jl:41-56): f over neighbours of type
+    promote_type(eltype, typeof(padval)) for a Remove boundary."""
     lib = _lib.load()
     wdt = A.LoweredStencil(stencil).desc.weight_dtype
-    rc = lib.stc_result_dtype(red.code, src_code, wdt)
+    code = src_code
+    if boundary is not None:
+        bc = A.lower_bc(boundary, padding or Conditional(), src_code)
+        code = lib.stc_neighbor_dtype(src_code, C.byref(bc))
+        if code < 0:
+            _lib.check(code, "mapstencil")
+    rc = lib.stc_result_dtype(red.code, code, wdt)
     if rc < 0:
-        raise NotImplementedError(f"{red} is not registered for element type {A.DTYPE_NAMES[src_code]}")
+        raise NotImplementedError(f"{red} is not registered for element type {A.DTYPE_NAMES[code]}")
     return rc
 
 
@@ -69,11 +77,11 @@ def _run_map(red, dest, src: AbstractStencilArray, dst_padded: bool, sync: bool 
     lib = _lib.load()
     st = A.LoweredStencil(src.stencil)
     op = A.lower_op(red)
-    bc = A.lower_bc(src.boundary, src.padding if not isinstance(src, SwitchingStencilArray) else
-                    (Halo("in") if isinstance(src.padding, Halo) else src.padding))
     halo = isinstance(src.padding, Halo)
     stage = _Staged(src.parent, dest, writeback=(0, 1) if halo else (1,))
     sp, dp = stage.dev
+    bc = A.lower_bc(src.boundary, src.padding if not isinstance(src, SwitchingStencilArray) else
+                    (Halo("in") if isinstance(src.padding, Halo) else src.padding), _code_of(src.parent))
     _require_device(sp)
     gs, gd = _grid(sp), _grid(dp)
     stream = _lib.current_stream_handle()
@@ -152,7 +160,7 @@ def mapstencil(f, *args, boundary=None, padding=None):
             raise TypeError("mapstencil needs a StencilArray or (stencil, array)")
     if rest:
         raise NotImplementedError("extra array arguments are not part of the registered GPU path")
-    code = result_dtype_code(red, _code_of(sa.parent), sa.stencil)
+    code = result_dtype_code(red, _code_of(sa.parent), sa.stencil, sa.boundary, sa.padding)
     dest = _new_dest(sa.parent, sa.shape, code)
     if isinstance(sa, SwitchingStencilArray):
         sa = StencilArray.from_parent(sa.source, sa.stencil, sa.boundary, sa.padding)
@@ -210,7 +218,7 @@ def _run_steps(red, S: SwitchingStencilArray, steps: int, sync: bool = True,
     st = A.LoweredStencil(S.stencil)
     op = A.lower_op(red)
     pad = Halo("in") if isinstance(S.padding, Halo) else Conditional()
-    bc = A.lower_bc(S.boundary, pad)
+    bc = A.lower_bc(S.boundary, pad, _code_of(S.source))
     stage = _Staged(S.source, S.dest, writeback=(0, 1))
     a, b = stage.dev
     _require_device(a)
@@ -231,7 +239,7 @@ def update_boundary_(A_: AbstractStencilArray):
     if not isinstance(A_.padding, Halo):
         return A_
     lib = _lib.load()
-    bc = A.lower_bc(A_.boundary, A_.padding)
+    bc = A.lower_bc(A_.boundary, A_.padding, _code_of(A_.parent))
     stage = _Staged(A_.parent, writeback=(0,))
     g = _grid(stage.dev[0])
     _lib.check(lib.stc_update_boundary(C.byref(g), A_.radius, C.byref(bc), _lib.current_stream_handle(), 0),

@@ -194,7 +194,7 @@ class Terms:
                 parent, stencil, boundary, padding = it
                 g = grid_fn(parent)
                 ls = A.LoweredStencil(stencil)
-                bc = A.lower_bc(boundary, padding)
+                bc = A.lower_bc(boundary, padding, code)
                 d.grid = C.pointer(g)
                 d.stencil = C.pointer(ls.desc)
                 d.bc = C.pointer(bc)

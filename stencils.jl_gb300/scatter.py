@@ -98,7 +98,8 @@ def scatterstencil_(f, op, dest, source=None):
 def _scatter(d, parent, dest, stencil, boundary, padding, _Staged, _grid, _require_device):
     lib = _lib.load()
     lst = A.LoweredStencil(stencil)
-    bc = A.lower_bc(boundary, padding)
+    code = A.torch_dtype_code(parent.dtype) if hasattr(parent, "device") else A.numpy_dtype_code(parent.dtype)
+    bc = A.lower_bc(boundary, padding, code)
     halo = isinstance(padding, Halo)
     stage = _Staged(parent, dest, writeback=(0, 1) if halo else (1,))
     sp, dp = stage.dev

@@ -36,7 +36,7 @@ class Server:
         st = A.LoweredStencil(stencil)
         job.stencil = st.desc
         job.op = A.lower_op(red)
-        job.bc = A.lower_bc(boundary, Conditional())
+        job.bc = A.lower_bc(boundary, Conditional(), code)
         job.nsteps = int(steps)
         out = C.c_int64(0)
         _lib.check(self._lib.stc_server_submit(self._h, C.byref(job), C.byref(out)), "stc_server_submit")

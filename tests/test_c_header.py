@@ -64,6 +64,6 @@ def test_header_compiles_as_c99_and_links(lib, tmp_path):
     subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", str(root / "include"), str(tmp_path / "t.c"),
                     "-o", str(exe), str(so), f"-Wl,-rpath,{so.parent}"], check=True, capture_output=True, text=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split(maxsplit=2)
-    assert out[0] == "1" and out[1] == "-1"
+    assert out[0] == "2" and out[1] == "-1"
     assert "sizes must match" in out[2]
     assert out[2].strip().endswith(" 0")      # mean of UInt8 -> Float64 (code 0)

@@ -25,7 +25,7 @@ def test_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_strerror(lib):
-    assert lib.stc_abi_version() == 1
+    assert lib.stc_abi_version() == 2
     assert b"radius" in lib.stc_strerror(-2)
     assert lib.stc_result_dtype(0, 0, 0) == 0
 
