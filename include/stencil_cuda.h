@@ -152,11 +152,12 @@ typedef struct {
 /* stc_map flags */
 /* stc_map_steps flag, BFloat16 / Float16 state only: the precision mode for long runs of 16-bit state.
  * The state is held in memory in the 16-bit type, but between the rounding points it stays Float32.
- * With s = 1..n the steps of this call and m = 4 * floor((n - 1) / 4), the state after step s <= m is
- * rounded to the storage type only when s is a multiple of 4: BFloat16 stochastically (round up with
- * probability equal to the distance from the value below; the bits come from a hash of the cell's
- * column-major linear index and s, so results are deterministic), Float16 to nearest.  The last n - m
- * steps (1 to 4) run as separate maps, each rounded to nearest.  Results then differ from n maps of
+ * With s = 1..n the steps of this call, P the pass length (8 for BFloat16, 4 for Float16) and
+ * m = P * floor((n - 1) / P), the state after step s <= m is rounded to the storage type only when s
+ * is a multiple of P: BFloat16 stochastically (round up with probability equal to the distance from the
+ * value below; the bits come from a hash of the cell's column-major linear index and s, so results are
+ * deterministic), Float16 to nearest.  The last n - m steps (1 to P) run as separate maps, each rounded
+ * to nearest.  Results then differ from n maps of
  * 16-bit state (each rounded to nearest); their error against an FP64 run is stated by the benchmark.
  * Runs the temporally blocked 3D path only (3D VonNeumann(1,3) diffusion / mean, Cross(1,3) sum, Wrap
  * or Remove); other runs return STC_ERR_UNSUPPORTED.  Ignored for Float32 / Float64 / integer state. */

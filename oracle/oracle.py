@@ -239,18 +239,18 @@ def bf16_stochastic_bits(x: np.ndarray, step: int) -> np.ndarray:
     return r.reshape(x.shape, order="F")
 
 
-def keep_f32_schedule(nsteps: int):
-    """The STC_KEEP_F32 precision mode's rounding schedule: m = 4 * floor((nsteps - 1) / 4) steps in
-    passes of 4 held in Float32 and rounded at the end of each pass, then the last nsteps - m steps as
-    separate maps (each rounded to nearest).  Returns (number of 4-step passes, per-step tail length)."""
-    m = (nsteps - 1) // 4 * 4 if nsteps >= 1 else 0
-    return m // 4, nsteps - m
+def keep_f32_schedule(nsteps: int, period: int = 4):
+    """The STC_KEEP_F32 precision mode's rounding schedule: m = P * floor((nsteps - 1) / P) steps in passes
+    of P (8 for BFloat16, 4 for Float16) held in Float32 and rounded at the end of each pass, then the last
+    nsteps - m steps as separate maps (each rounded to nearest).  Returns (passes, per-step tail length)."""
+    m = (nsteps - 1) // period * period if nsteps >= 1 else 0
+    return m // period, nsteps - m
 
 
 def map_steps_keep_f32(a: np.ndarray, code: int, stencil, red, boundary, padding, nsteps: int,
                        *, nthreads: int = 1):
-    """The STC_KEEP_F32 precision mode restated: 16-bit state `a` (BFloat16 bits or float16).  Each 4-step
-    pass runs as Float32 maps (the oracle's Float32 gather) from the widened state, then rounds (BFloat16
+    """The STC_KEEP_F32 precision mode restated: 16-bit state `a` (BFloat16 bits or float16).  Each pass
+    (8 steps for BFloat16, 4 for Float16) runs as Float32 maps (the oracle's Float32 gather) from the widened state, then rounds (BFloat16
     stochastically with the step number reached, Float16 to nearest); the tail steps are plain 16-bit
     maps.  Returns (state n, state n - 1) as 16-bit arrays of a's type."""
     from stencils_gb300 import _abi as A
@@ -274,15 +274,16 @@ def map_steps_keep_f32(a: np.ndarray, code: int, stencil, red, boundary, padding
         else:
             pv = np.float32(np.float16(boundary.padval))
         bnd = Remove(float(np.asarray(pv).ravel()[0]))
-    passes, tail = keep_f32_schedule(nsteps)
+    period = 8 if code == A.BF16 else 4
+    passes, tail = keep_f32_schedule(nsteps, period)
     cur = np.asfortranarray(a)
     prev = cur
     step = 0
     for _ in range(passes):
         pa = np.asfortranarray(widen(cur))
         pb = pa.copy(order="F")
-        in_b = map_steps(pa, pb, A.F32, stencil, red, bnd, padding, 4, nthreads=nthreads)
-        step += 4
+        in_b = map_steps(pa, pb, A.F32, stencil, red, bnd, padding, period, nthreads=nthreads)
+        step += period
         prev, cur = cur, np.asfortranarray(narrow(pb if in_b else pa, step))
     if tail:
         pa, pb = cur.copy(order="F"), cur.copy(order="F")

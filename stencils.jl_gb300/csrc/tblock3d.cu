@@ -43,7 +43,8 @@
 
 namespace stc {
 
-constexpr int kTbK = 4;              // time levels per pass (the STC_KEEP_F32 rounding period)
+constexpr int kTbK = 4;              // time levels per pass (8 for BFloat16 in the STC_KEEP_F32 mode)
+constexpr int kTbKMax = 8;
 constexpr int kTbRPT = 2;            // rows per thread block (the thread owns 4 x kTbRPT cells of a plane)
 constexpr int kTbRing = 5;           // input planes resident: i-2 .. i (read) and i+1, i+2 (in flight)
 constexpr int kTbMaxThreads = 512;   // 16 warps: four per SM sub-partition, up to 128 registers each
@@ -55,7 +56,7 @@ struct TB6Params {
     int32_t n[3];                    // logical size
     int32_t H;                       // ring width: tensor-map coordinate of logical 0 on every axis
     int32_t BX, BY;                  // plane box
-    int32_t XH;                      // box column of the tile's first column (>= kTbK, multiple of 4)
+    int32_t XH;                      // box column of the tile's first column (>= K, multiple of 4)
     int32_t TX, TY, ZC;              // tile and z chunk (outputs)
     int32_t ntx, nty, nzc, nitems;
     int32_t remove;                  // Remove: cells outside the grid hold padval at every level
@@ -277,13 +278,13 @@ __device__ __forceinline__ void tb_sides(const float (&M)[kTbRPT][4], const floa
     }
 }
 
-template <class T, class Op, class Sh>
+template <class T, class Op, class Sh, int K>
 __global__ void __launch_bounds__(kTbMaxThreads, 1) tb6_kernel(const __grid_constant__ TB6Params p) {
     static_assert(TbTaps<Sh>::only_axis_taps(), "taps must be the centre or one step along one axis");
     using OpF = typename TbF32<Op>::type;
     extern __shared__ __align__(128) unsigned char tsm[];
     const int BX = p.BX, QX = BX >> 2;
-    constexpr int k = kTbK;
+    constexpr int k = K;
     auto ring = [&](uint32_t g) { return (const T*)(tsm + p.ring_off + (size_t)(g % kTbRing) * p.ring_stride); };
     // level buffer (t, parity): plane pointer (one slack row precedes it)
     auto lvl = [&](int t, int par) {
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(kTbMaxThreads, 1) tb6_kernel(const __grid_cons
         const int x0 = txi * p.TX, y0 = tyi * p.TY, z0 = tzi * p.ZC;
         const int z1 = min(z0 + p.ZC, p.n[2]);
         const int NI = (z1 - z0) + 2 * k;       // input planes z0-k .. z1+k-1
-        const int gx0 = x0 - p.XH, gy0 = y0 - kTbK, gz0 = z0 - k;   // global coords of box (0, 0, plane 0)
+        const int gx0 = x0 - p.XH, gy0 = y0 - K, gz0 = z0 - k;   // global coords of box (0, 0, plane 0)
         auto issue = [&](int j) {
             const uint32_t g = gplane + (uint32_t)j;
             uint64_t* bar = &bars[g % kTbRing];
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(kTbMaxThreads, 1) tb6_kernel(const __grid_cons
         for (int c = 0; c < 4; ++c) xout |= (gx0 + cx + c < 0 || gx0 + cx + c >= p.n[0]) ? (1 << c) : 0;
 #pragma unroll
         for (int r = 0; r < kTbRPT; ++r) yout |= (gy0 + cy + r < 0 || gy0 + cy + r >= p.n[1]) ? (1 << r) : 0;
-        const bool own_out = act && cx >= p.XH && cx < p.XH + p.TX && cy >= kTbK && cy < kTbK + p.TY &&
+        const bool own_out = act && cx >= p.XH && cx < p.XH + p.TX && cy >= K && cy < K + p.TY &&
                              gx0 + cx < p.n[0] && gy0 + cy < p.n[1];
         const bool full4 = gx0 + cx + 3 < p.n[0];
 
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(kTbMaxThreads, 1) tb6_kernel(const __grid_cons
         // previous iteration is this iteration's plane below (LO): its shared-memory buffer has been
         // overwritten by then.  Iterations run in pairs, so the set index is a compile-time constant and
         // nothing is copied between registers.  Level 1 reads its three planes from the input ring.
-        float S[kTbK - 1][2][kTbRPT][4];
+        float S[K - 1][2][kTbRPT][4];
         bool failed = false;
         auto iteration = [&](const int i, auto u_c) {
             constexpr int U = decltype(u_c)::value;
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(kTbMaxThreads, 1) tb6_kernel(const __grid_cons
             }
             float prev[kTbRPT][4];   // the plane the level below produced this iteration (this level's HI)
 #pragma unroll
-            for (int t = 1; t <= kTbK; ++t) {
+            for (int t = 1; t <= K; ++t) {
                 if (!(i >= 2 * t - 1)) continue;   // uniform across the CTA
                 const int pz = i - t;              // this level's plane (input-plane numbering)
                 float LO[kTbRPT][4], HI[kTbRPT][4], UP[4], DN[4], EDGE[kTbRPT], LF[kTbRPT], RT[kTbRPT];
@@ -489,7 +490,7 @@ static TbEncodeFn tb_encoder() {
 
 using TbLaunch = cudaError_t (*)(const TB6Params&, int grid, int threads, size_t smem, cudaStream_t);
 
-template <class T, class Op, class Sh>
+template <class T, class Op, class Sh, int K>
 static cudaError_t tb6_launch(const TB6Params& p, int grid, int threads, size_t smem, cudaStream_t s) {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
@@ -497,23 +498,26 @@ static cudaError_t tb6_launch(const TB6Params& p, int grid, int threads, size_t 
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        attr = cudaFuncSetAttribute(tb6_kernel<T, Op, Sh>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        attr = cudaFuncSetAttribute(tb6_kernel<T, Op, Sh, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
     });
     if (attr != cudaSuccess) return attr;
-    tb6_kernel<T, Op, Sh><<<grid, threads, smem, s>>>(p);
+    tb6_kernel<T, Op, Sh, K><<<grid, threads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
-struct TbEntry { int dt, opv, shape; TbLaunch fn; };
+// fn: passes of kTbK levels; fn8: passes of 8 levels (BFloat16 state in the STC_KEEP_F32 mode)
+struct TbEntry { int dt, opv, shape; TbLaunch fn, fn8; };
 
 using VN3 = Shape<STC_SHAPE_VONNEUMANN, 1, 3>;
 using CR3 = Shape<STC_SHAPE_CROSS, 1, 3>;
+using DiffBF = OpDiffuse<__nv_bfloat16, __nv_bfloat16, float>;
 static const TbEntry kTbTable[] = {
-    {STC_F32, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<float, OpDiffuse<float, float, float>, VN3>},
-    {STC_BF16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<__nv_bfloat16, OpDiffuse<__nv_bfloat16, __nv_bfloat16, float>, VN3>},
-    {STC_F16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<__half, OpDiffuse<__half, __half, float>, VN3>},
-    {STC_F32, OPV_MEAN, STC_SHAPE_VONNEUMANN, &tb6_launch<float, OpMean<float, float, float>, VN3>},
-    {STC_F32, OPV_SUM, STC_SHAPE_CROSS, &tb6_launch<float, OpSumF<float, float, float>, CR3>},
+    {STC_F32, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<float, OpDiffuse<float, float, float>, VN3, kTbK>, nullptr},
+    {STC_BF16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<__nv_bfloat16, DiffBF, VN3, kTbK>,
+     &tb6_launch<__nv_bfloat16, DiffBF, VN3, kTbKMax>},
+    {STC_F16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, &tb6_launch<__half, OpDiffuse<__half, __half, float>, VN3, kTbK>, nullptr},
+    {STC_F32, OPV_MEAN, STC_SHAPE_VONNEUMANN, &tb6_launch<float, OpMean<float, float, float>, VN3, kTbK>, nullptr},
+    {STC_F32, OPV_SUM, STC_SHAPE_CROSS, &tb6_launch<float, OpSumF<float, float, float>, CR3, kTbK>, nullptr},
 };
 
 static CUtensorMapDataType tb_dtype(int dt) {
@@ -521,12 +525,18 @@ static CUtensorMapDataType tb_dtype(int dt) {
            : dt == STC_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16;
 }
 
-static TbLaunch tb_find(const stc_grid* a, const stc_stencil* st, const stc_op* op) {
+static const TbEntry* tb_find(const stc_grid* a, const stc_stencil* st, const stc_op* op) {
     const int opv = op->code == STC_OP_DIFFUSE ? OPV_DIFFUSE : op->code == STC_OP_MEAN ? OPV_MEAN
                     : op->code == STC_OP_SUM ? OPV_SUM : -1;
     for (const TbEntry& e : kTbTable)
-        if (e.dt == a->dtype && e.opv == opv && table_matches_shape(e.shape, 1, 3, st->offsets, st->len)) return e.fn;
+        if (e.dt == a->dtype && e.opv == opv && table_matches_shape(e.shape, 1, 3, st->offsets, st->len)) return &e;
     return nullptr;
+}
+
+// Levels per pass: 8 for BFloat16 state in the precision mode (half the stochastic roundings of 4, which
+// measured 1.04e-2 max relative error on 512^3 x 200 diffusion against the 1e-2 target), else kTbK.
+int tb3d_levels(int dtype, uint32_t flags) {
+    return ((flags & STC_KEEP_F32) && dtype == STC_BF16) ? kTbKMax : kTbK;
 }
 
 bool tb3d_applies(const stc_grid* a, const stc_stencil* st, const stc_op* op, const stc_bc* bc) {
@@ -536,9 +546,9 @@ bool tb3d_applies(const stc_grid* a, const stc_stencil* st, const stc_op* op, co
     return true;
 }
 
-// Steps of the run taken by blocked passes: the largest multiple of kTbK below nsteps; the rest (1 to
-// kTbK steps, so that the pair holds states n - 1 and n at the end) run as per-step maps on the pair.
-static int64_t tb_blocked_steps(int64_t nsteps) { return nsteps >= 1 ? (nsteps - 1) / kTbK * kTbK : 0; }
+// Steps of the run taken by blocked passes of K steps: the largest multiple of K below nsteps; the rest
+// (1 to K steps, so that the pair holds states n - 1 and n at the end) run as per-step maps on the pair.
+static int64_t tb_blocked_steps(int64_t nsteps, int K) { return nsteps >= 1 ? (nsteps - 1) / K * K : 0; }
 
 int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op, const stc_bc* bc,
                    int64_t nsteps, int* src_is_b, cudaStream_t stream, DeviceCtx* ctx, uint32_t flags, int64_t* done) {
@@ -553,12 +563,15 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     // 16-bit state rounded every step: the per-step vector map moves half the bytes of Float32 and was
     // measured faster than the blocked kernel (711 against 557 Gcell/s on 512^3 x 200 BFloat16)
     if (!keep && !forced && a->dtype != STC_F32) return STC_OK;
-    TbLaunch fn = tb_find(a, st, op);
+    const int K = tb3d_levels(a->dtype, flags);
+    const TbEntry* ent = tb_find(a, st, op);
+    TbLaunch fn = K == kTbKMax ? ent->fn8 : ent->fn;
+    if (!fn) return keep ? STC_ERR_UNSUPPORTED : STC_OK;
     const int es = dtype_size(a->dtype);
     const bool halo = bc->padding != STC_CONDITIONAL;
     int64_t n[3];
     for (int d = 0; d < 3; ++d) n[d] = a->size[d] - (halo ? 2 : 0);
-    const int XH = std::max(kTbK, 16 / es);   // tile's first column on a 16-byte boundary of the box
+    const int XH = std::max(K, 16 / es);   // tile's first column on a 16-byte boundary of the box
     const int H = XH;
     for (int d = 0; d < 3; ++d)
         if (n[d] < H || n[d] + 2 * H + 256 >= (1ll << 31)) return keep ? STC_ERR_UNSUPPORTED : STC_OK;
@@ -580,19 +593,19 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         *ring_stride = rs;
         *lvl_off = slack + kTbRing * rs;
         *lvl_stride = ls;
-        *bar_off = *lvl_off + 2 * (kTbK - 1) * ls;
+        *bar_off = *lvl_off + 2 * (K - 1) * ls;
         return (size_t)*bar_off + 8 * kTbRing;
     };
     int best_by = 0, best_tx = 0;
     int64_t best_cost = INT64_MAX;
     for (int TX : {64, 128}) {
         const int BX = TX + 2 * XH;
-        for (int BY = 2 * kTbK + 8; BY <= 256; BY += kTbRPT) {
+        for (int BY = 2 * K + 8; BY <= 256; BY += kTbRPT) {
             uint32_t a0, a1, a2, a3, a4;
             if (smem_for(BX, BY, &a0, &a1, &a2, &a3, &a4) > smem_cap) break;
             const int threads = (BX / 4) * (BY / kTbRPT);
             if (threads > kTbMaxThreads) break;
-            const int TY = BY - 2 * kTbK;
+            const int TY = BY - 2 * K;
             const int64_t cost = (n[0] + TX - 1) / TX * BX * ((n[1] + TY - 1) / TY * BY);
             if (cost < best_cost) {
                 best_cost = cost;
@@ -605,7 +618,7 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     p.TX = best_tx;
     p.BX = p.TX + 2 * XH;
     p.BY = best_by;
-    p.TY = p.BY - 2 * kTbK;
+    p.TY = p.BY - 2 * K;
     const size_t smem = smem_for(p.BX, p.BY, &p.ring_off, &p.ring_stride, &p.lvl_off, &p.lvl_stride, &p.bar_off);
     const int threads = ((p.BX / 4) * (p.BY / kTbRPT) + 31) / 32 * 32;
     p.box_bytes = (uint32_t)((size_t)p.BX * p.BY * es);
@@ -620,7 +633,7 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         for (int c = 1; c <= std::max<int64_t>(1, n[2] / 8); ++c) {
             const int64_t zc = (n[2] + c - 1) / c;
             const int64_t waves = (xy * c + ctx->num_sms - 1) / ctx->num_sms;
-            const int64_t cost = waves * (zc + 2 * kTbK);
+            const int64_t cost = waves * (zc + 2 * K);
             if (cost < best) { best = cost; bz = c; }
         }
         p.ZC = (int)((n[2] + bz - 1) / bz);
@@ -679,12 +692,12 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     int rc = launch_grid_copy(par[*src_is_b], org[*src_is_b], &pg[0], inner, n, stream);
     if (!rc && p.remove) rc = launch_halo_fill(&pg[0], H, &hb, stream);
     if (!rc && p.remove) rc = launch_halo_fill(&pg[1], H, &hb, stream);
-    const int64_t blocked = tb_blocked_steps(nsteps);
+    const int64_t blocked = tb_blocked_steps(nsteps, K);
     int cur = 0;
     int64_t step = 0;
     while (step < blocked && !rc) {
         if (!p.remove && (rc = launch_halo_fill(&pg[cur], H, &hb, stream))) break;
-        step += kTbK;
+        step += K;
         p.round_step = (uint32_t)step;
         p.dst = (char*)pg[1 - cur].data + inner * es;
         p.dstr1 = pitch;
@@ -700,7 +713,7 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         }
         void* prof = prof_begin(stream);
         cudaError_t e = fn(p, grid, threads, smem, stream);
-        prof_end(prof, stream, "tblock3d", 2.0 * es * n[0] * n[1] * n[2] * kTbK, (double)n[0] * n[1] * n[2] * kTbK);
+        prof_end(prof, stream, "tblock3d", 2.0 * es * n[0] * n[1] * n[2] * K, (double)n[0] * n[1] * n[2] * K);
         if (e != cudaSuccess) rc = cuda_fail(e);
         cur = 1 - cur;
     }

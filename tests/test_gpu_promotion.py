@@ -47,7 +47,7 @@ def test_promoted_map_matches_oracle(cuda, st, orc, abi, case):
     want = orc.map(parent if isinstance(pad, st.Halo) else host, code, hood, red, bnd, pad)
     got = st.to_host(out)
     assert got.dtype == want.dtype, (got.dtype, want.dtype)
-    assert np.array_equal(got.view(np.uint8), want.view(np.uint8))
+    assert got.tobytes(order="F") == want.tobytes(order="F")
 
 
 def test_promoted_steps_match_oracle(cuda, st, orc, abi):

@@ -84,10 +84,11 @@ def test_other_blocked_shapes_and_halo(cuda, st, orc, abi, shape_name):
 
 @pytest.mark.parametrize("code", ["bf16", "f16"])
 @pytest.mark.parametrize("bname", ["wrap", "remove_half"])
-@pytest.mark.parametrize("steps", [1, 3, 9, 10])
+@pytest.mark.parametrize("steps", [1, 3, 9, 10, 17])
 def test_keep_f32_matches_oracle(cuda, st, orc, abi, code, bname, steps):
-    """The precision mode (STC_KEEP_F32): Float32 inside 4-step passes, BFloat16 rounded stochastically
-    from hashed bits at their ends; both states bit-exact against the oracle's restatement."""
+    """The precision mode (STC_KEEP_F32): Float32 inside passes of 8 (BFloat16) or 4 (Float16) steps,
+    BFloat16 rounded stochastically from hashed bits at their ends; both states bit-exact against the
+    oracle's restatement."""
     import torch
     from oracle.oracle import f32_to_bf16_bits
     rng = np.random.default_rng(steps + 5 * len(bname))

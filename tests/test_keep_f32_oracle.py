@@ -32,3 +32,5 @@ def test_keep_f32_schedule(orc):
     assert orc.keep_f32_schedule(8) == (1, 4)
     assert orc.keep_f32_schedule(9) == (2, 1)
     assert orc.keep_f32_schedule(200) == (49, 4)
+    assert orc.keep_f32_schedule(200, 8) == (24, 8)
+    assert orc.keep_f32_schedule(9, 8) == (1, 1)
