@@ -467,10 +467,8 @@ def cfg_mean_blur(args):
     t = _timed_steps(lambda: st.mapstencil_(st.mean, out, sa, sync=False), steps, args.warmup, flush)
     prof = _lib.profile_report()
     _lib.profile_enable(False)
-    # e2e: the reference's call on a host array (staged to the device and back by the public API)
-    host_out = np.empty((1000, 1000), order="F")
-    host_sa = st.StencilArray(a, st.Window(1))
-    te = _wall_steps(lambda: st.mapstencil_(st.mean, host_out, host_sa), steps, args.warmup)
+    # e2e: host input (pinned) copied in, the map, the result copied back, every call
+    te = _e2e_map(st, a, sa.parent, out, lambda: st.mapstencil_(st.mean, out, sa, sync=False), steps, args.warmup)
     cpu = _cpu_rate(lambda orc, A, thr: orc.map(a, A.F64, st.Window(1), st.mean, st.Remove(0.0), st.Conditional(),
                                                  nthreads=thr), 1e6, 3.0)
     name, k, roof = _hbm_roof(prof, _peaks())
@@ -488,6 +486,29 @@ def cfg_mean_blur(args):
             "reference_published": {"cpu_min_ms": 2.755, "cpu_gcell_s": 0.363, "mx330_min_ms": 0.9168,
                                     "gtx1080_ms": 0.216, "gtx1080_gcell_s": 4.63,
                                     "source": "Stencils.jl README (8-core ThinkPad T14; MX330; GTX 1080)"}}
+
+
+def _pinned(a: np.ndarray):
+    """A pinned host tensor holding a's bytes in column-major order."""
+    import torch
+    t = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory()
+    t.copy_(torch.from_numpy(np.frombuffer(np.asfortranarray(a).tobytes(order="F"), dtype=np.uint8)))
+    return t
+
+
+def _e2e_map(st, host_in, dev_in, dev_out, run, steps, warmup):
+    """Host-clock seconds of `steps` calls of: pinned host -> dev_in (one pitched copy), run(), dev_out ->
+    pinned host, each call waiting for its result on the host."""
+    import torch
+    pin_in = _pinned(host_in)
+    pin_out = torch.empty(dev_out.numel() * dev_out.element_size(), dtype=torch.uint8).pin_memory()
+
+    def call():
+        st.copy_to_device_(dev_in, pin_in, sync=False)
+        run()
+        st.copy_to_host_(pin_out, dev_out, sync=False)
+        torch.cuda.synchronize()
+    return _wall_steps(call, steps, warmup)
 
 
 def _cpu_rate(call, cells, target_s):
@@ -551,10 +572,10 @@ def cfg_gauss(args):
         res[name] = {"value": args.steps * a32.size / t / 1e9, "ms_per_map": 1e3 * t / args.steps,
                      "max_rel_err_vs_fp64": _max_rel(out, ref), "roofline": roof, "kernel_rate": kr}
         del x, sa, out
-    # e2e (Float32): host array in, map, host array out through the public API
-    host_out = np.empty(a32.shape, dtype=np.float32, order="F")
-    host_sa = st.StencilArray(a32, K, st.Remove(0.0))
-    te = _wall_steps(lambda: st.mapstencil_(st.kernelproduct, host_out, host_sa), 3, 1)
+    # e2e (Float32): host grid in, the map, host result out through the public API
+    sa32 = st.StencilArray(d32, K, st.Remove(0.0))
+    out32 = st.mapstencil(st.kernelproduct, sa32)
+    te = _e2e_map(st, a32, d32, out32, lambda: st.mapstencil_(st.kernelproduct, out32, sa32, sync=False), 3, 3)
     clk_hz = 2.07e9
     for r in res.values():
         # binding unit: the FP32 FMA pipe, 49 FMAs per cell (128 per SM per clock)
@@ -624,11 +645,13 @@ def cfg_diffusion(args):
         del x, S
     del ref
     # e2e (Float32): host grid in, 200 steps, host grid out through the public API
-    host = np.asfortranarray(a.copy())
-    t0 = time.perf_counter()
-    Sh = st.SwitchingStencilArray(host, st.VonNeumann(1, 3), st.Wrap())
-    Sh = st.mapstencil_(st.Diffusion(0.1), Sh, steps=steps)
-    te = time.perf_counter() - t0
+    Se = st.SwitchingStencilArray(_cast(d32, torch.float32), st.VonNeumann(1, 3), st.Wrap())
+    holder = {"S": Se}
+
+    def run_e2e():
+        holder["S"] = st.mapstencil_(st.Diffusion(0.1), holder["S"], steps=steps, sync=False)
+    # steps is even, so the result lands in the parent the input went into
+    te = _e2e_map(st, a, Se.source, Se.source, run_e2e, 1, 1)
     cpu = _cpu_rate(lambda orc, A, thr: orc.map_steps(np.asfortranarray(a[:128, :128, :128]),
                                                       np.asfortranarray(a[:128, :128, :128]), A.F32,
                                                       st.VonNeumann(1, 3), st.Diffusion(0.1), st.Wrap(),
