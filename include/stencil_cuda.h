@@ -163,7 +163,8 @@ typedef struct {
  * or Remove); other runs return STC_ERR_UNSUPPORTED.  Ignored for Float32 / Float64 / integer state. */
 #define STC_KEEP_F32 2u
 #define STC_ASYNC 1u          /* do not synchronise the stream before returning (errors from the
-                                 kernel's own checks surface at the next synchronising call) */
+                                 kernel's own checks surface at the next synchronising call on the
+                                 same stream: each stream has its own status slot) */
 
 /* ---- library ---- */
 STC_API int         stc_abi_version(void);

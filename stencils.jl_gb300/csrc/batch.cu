@@ -731,7 +731,8 @@ int batch_build(stc_batch* b, bool autotune, cudaStream_t stream, DeviceCtx* ctx
     d.ticket = d.counters + b->ncounters;
     d.abort_flag = d.ticket + 1;
     d.nitems = (int)b->hitems.size();
-    d.status = ctx->status;
+    b->slot = status_slot(ctx, b);   // each batch (and each serving tick) has its own slot
+    d.status = b->slot.dev;
     if (nj) cudaMemcpyAsync((void*)d.jobs, b->hjobs.data(), sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, stream);
     if (!b->hitems.empty())
         cudaMemcpyAsync((void*)d.items, b->hitems.data(), sizeof(BatchItem) * b->hitems.size(), cudaMemcpyHostToDevice, stream);
@@ -923,8 +924,7 @@ int stc_batch_run(stc_batch* b, void* stream, uint32_t flags) {
     if (e != cudaSuccess) return cuda_fail(e);
     if (!(flags & STC_ASYNC)) {
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e);
-        volatile int* h = ctx->status_host;
-        if (*h) { *h = 0; return STC_ERR_TIMEOUT; }
+        if (b->slot.host && (rc = take_status(b->slot))) return rc;
     }
     return STC_OK;
 }

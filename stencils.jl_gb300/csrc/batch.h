@@ -92,6 +92,7 @@ struct stc_batch {
     void* dmem = nullptr;
     size_t dmem_bytes = 0;
     stc::BatchDev dev{};
+    stc::StatusSlot slot{};   // this batch's timeout word, baked into the planned launch
     size_t smem = 0;
     int grid = 0;
     cudaStream_t cap_stream = nullptr;

@@ -176,17 +176,62 @@ void workspace_release(void* ptr, bool cached, cudaStream_t s) {
     w.busy = false;
 }
 
-// reads and clears the status word after the stream finished
+// ---------------------------------------------------------------------------- status slots
+constexpr int kStatusSlots = 256;
+struct SlotPool {
+    int* host = nullptr;
+    int* dev = nullptr;
+    std::map<const void*, std::pair<int, uint64_t>> bound;   // key -> (slot, last use)
+    uint64_t clock = 0;
+};
+static SlotPool g_slots[64];
+
+StatusSlot status_slot(DeviceCtx* ctx, const void* key) {
+    std::lock_guard<std::mutex> g(g_ctx_mu);
+    SlotPool& P = g_slots[ctx->device];
+    if (!P.host) {
+        int* h = nullptr;
+        int* d = nullptr;
+        if (cudaHostAlloc((void**)&h, sizeof(int) * kStatusSlots, cudaHostAllocMapped) == cudaSuccess &&
+            cudaHostGetDevicePointer((void**)&d, h, 0) == cudaSuccess) {
+            memset(h, 0, sizeof(int) * kStatusSlots);
+            P.host = h;
+            P.dev = d;
+        } else {
+            cudaGetLastError();   // no pool: every key shares the context's own word
+            return StatusSlot{ctx->status, ctx->status_host};
+        }
+    }
+    ++P.clock;
+    auto it = P.bound.find(key);
+    if (it != P.bound.end()) {
+        it->second.second = P.clock;
+        return StatusSlot{P.dev + it->second.first, P.host + it->second.first};
+    }
+    int slot = (int)P.bound.size();
+    if (slot >= kStatusSlots) {
+        auto lru = P.bound.begin();
+        for (auto j = P.bound.begin(); j != P.bound.end(); ++j)
+            if (j->second.second < lru->second.second) lru = j;
+        slot = lru->second.first;
+        P.bound.erase(lru);
+    }
+    P.bound[key] = {slot, P.clock};
+    return StatusSlot{P.dev + slot, P.host + slot};
+}
+
+int take_status(const StatusSlot& sl) {
+    const int v = *sl.host;
+    if (!v) return STC_OK;
+    *sl.host = 0;
+    return (v & DEV_ERR_TIMEOUT) ? STC_ERR_TIMEOUT : STC_ERR_INEXACT;
+}
+
+// waits for the stream, then reads and clears its status slot
 static int finish_sync(cudaStream_t s, DeviceCtx* ctx) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e);
-    volatile int* h = ctx->status_host;
-    const int v = *h;
-    if (v) {
-        *h = 0;
-        return (v & DEV_ERR_TIMEOUT) ? STC_ERR_TIMEOUT : STC_ERR_INEXACT;
-    }
-    return STC_OK;
+    return take_status(status_slot(ctx, s));
 }
 
 // ---------------------------------------------------------------------------- type promotion
@@ -431,7 +476,7 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     p.ndims = nd;
     p.halo = halo;
     p.boundary = bc->boundary;
-    p.status = ctx->status;
+    p.status = status_slot(ctx, stream).dev;
     p.L = st->len;
     p.rcp_f = (float)(1.0 / (double)st->len);
     p.Lf = (float)st->len;
@@ -649,7 +694,7 @@ static int map_promoted(const stc_grid* src, const stc_grid* dst, int dst_padded
     sizes3(src, n);
     stc_bc b2 = *bc;
     b2.padval_type = 0;
-    rc = launch_grid_convert(src, 0, &t, 0, n, ctx->status, s);
+    rc = launch_grid_convert(src, 0, &t, 0, n, status_slot(ctx, s).dev, s);
     if (!rc) rc = launch_halo_fill(&t, st->radius, &b2, s);
     if (!rc) rc = launch_map(&t, dst, dst_padded, st, op, &b2, s, ctx);
     cudaFreeAsync(t.data, s);
@@ -788,10 +833,10 @@ static int map_steps_promoted(const stc_grid* a, const stc_grid* b, const stc_st
         for (int64_t k = 0; k < nsteps && !rc; ++k) {
             const stc_grid* sg = grids[src_is_b];
             const stc_grid* dg = grids[1 - src_is_b];
-            rc = launch_grid_convert(sg, 0, &tin, 0, whole, ctx->status, s);
+            rc = launch_grid_convert(sg, 0, &tin, 0, whole, status_slot(ctx, s).dev, s);
             if (!rc) rc = launch_halo_fill(&tin, st->radius, &b2, s);
             if (!rc) rc = launch_map(&tin, &tout, 1, st, op, &b2, s, ctx);
-            if (!rc) rc = launch_grid_convert(&tout, org(&tout), dg, org(dg), n, ctx->status, s);
+            if (!rc) rc = launch_grid_convert(&tout, org(&tout), dg, org(dg), n, status_slot(ctx, s).dev, s);
             src_is_b = 1 - src_is_b;
         }
         cudaFreeAsync(tin.data, s);

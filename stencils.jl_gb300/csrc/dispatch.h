@@ -46,6 +46,19 @@ struct DeviceCtx {
 };
 int device_ctx(DeviceCtx** out);
 
+// The status word kernels OR an error bit into (a bounded wait gave up, an inexact conversion) is one of
+// a pool of mapped host words, one per stream (or per other key, e.g. a batch whose graph holds the
+// device address), so an error of an asynchronous call is reported by the next synchronising call on
+// the same stream, not by another caller's.  256 keys per device at a time; beyond that the least
+// recently bound key's word is reused.
+struct StatusSlot {
+    int* dev;
+    volatile int* host;
+};
+StatusSlot status_slot(DeviceCtx* ctx, const void* key);
+// reads and clears a slot: STC_OK, or the status its bits stand for
+int take_status(const StatusSlot& s);
+
 // remembers the CUDA error behind an STC_ERR_CUDA
 int cuda_fail(cudaError_t e);
 

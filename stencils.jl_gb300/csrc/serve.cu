@@ -163,10 +163,8 @@ static void serve_loop(stc_server* s) {
         if (!rc) {
             cudaError_t e = cudaStreamSynchronize(s->stream);
             if (e != cudaSuccess) rc = cuda_fail(e);
-            else if (*(volatile int*)s->ctx->status_host) {
-                *(volatile int*)s->ctx->status_host = 0;
-                rc = STC_ERR_TIMEOUT;
-            }
+            else
+                rc = take_status(tick.slot);
         }
         // retire finished jobs
         std::vector<ServeJob*> done;

@@ -651,7 +651,7 @@ int tb3d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     }
     p.keep_f32 = keep;
     p.stochastic = keep && a->dtype == STC_BF16;
-    p.status = ctx->status;
+    p.status = status_slot(ctx, stream).dev;
     p.L = st->len;
     p.alpha = op->alpha;
     p.rcp_f = (float)(1.0 / (double)st->len);

@@ -117,6 +117,8 @@ def _bc(st, name, code, abi):
     if name == "remove0":
         return st.Remove(0)
     if name == "remove_nz":
+        if code == abi.BOOL:
+            return st.Remove(True)     # a Bool padval: Remove(3) would promote the neighbours to Int64
         return st.Remove(0.75 if code in (abi.F64, abi.F32, abi.BF16, abi.F16) else 3)
     return {"wrap": st.Wrap(), "reflect": st.Reflect()}[name]
 

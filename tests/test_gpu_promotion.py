@@ -80,3 +80,24 @@ def test_promoted_steps_inexact(cuda, st):
     assert e.value.status == -13
     # the library's status word is clear again afterwards
     S = st.mapstencil_(st.sum, st.SwitchingStencilArray(st.to_device(a), st.Window(1), st.Remove(0)), steps=1)
+
+
+def test_status_is_per_stream(cuda, st):
+    """An inexact conversion queued without waiting on stream A is reported by the next synchronising
+    call on stream A, not by a call that synchronises stream B in between."""
+    import torch
+    from stencils_gb300._lib import StencilError
+    a = np.ones((40, 30), dtype=np.uint8, order="F")
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    with torch.cuda.stream(sa):
+        S = st.SwitchingStencilArray(st.to_device(a), st.Window(1), st.Remove(0.5))
+        st.mapstencil_(st.sum, S, steps=1, sync=False)          # queued; the error waits in A's slot
+    with torch.cuda.stream(sb):
+        T = st.SwitchingStencilArray(st.to_device(a), st.Window(1), st.Remove(0))
+        st.mapstencil_(st.sum, T, steps=1)                      # B's own slot is clear
+    with torch.cuda.stream(sa):
+        U = st.SwitchingStencilArray(st.to_device(a), st.Window(1), st.Remove(0))
+        with pytest.raises(StencilError) as e:
+            st.mapstencil_(st.sum, U, steps=1)
+        assert e.value.status == -13
+        st.mapstencil_(st.sum, U, steps=1)                      # read once, then clear
