@@ -665,6 +665,63 @@ def cfg_diffusion(args):
             "reference_per_step_gcell_s_before_blocking": 505, "cpu_baseline": cpu}
 
 
+def cfg_blocked2d(args):
+    """2D multi-step maps on Float32 state: Window(1) mean and VonNeumann(1) diffusion, 8192^2 U[0,1), Wrap,
+    100 steps, temporally blocked (4 steps per pass over HBM) against the per-step map (STC_TBLOCK=0)."""
+    import torch
+    st = entry.load_package()
+    from stencils_gb300 import _lib
+    rng = np.random.Generator(np.random.PCG64(6))
+    steps, side = 100, 8192
+    a = np.asfortranarray(rng.random((side, side), dtype=np.float32))
+    d = st.to_device(a)
+    cells = a.size
+    res = {}
+    for name, hood, red in (("window_mean", st.Window(1), st.mean), ("vn_diffusion", st.VonNeumann(1), st.Diffusion(0.1))):
+        for mode in ("blocked", "per_step"):
+            if mode == "per_step":
+                os.environ["STC_TBLOCK"] = "0"
+            try:
+                S = st.SwitchingStencilArray(d.clone(), hood, st.Wrap())
+                st.mapstencil_(red, S, steps=8)      # warm-up: kernel attributes
+                torch.cuda.synchronize()
+                _lib.profile_enable(True)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                S = st.mapstencil_(red, S, steps=steps)
+                e1.record()
+                e1.synchronize()
+                t = e0.elapsed_time(e1) / 1e3
+                prof = _lib.profile_report()
+                _lib.profile_enable(False)
+            finally:
+                os.environ.pop("STC_TBLOCK", None)
+            kname, k, roof = _hbm_roof(prof, _peaks())
+            roof["note"] = ("algorithmic bytes: one Float32 read and one write per cell-step (a blocked pass "
+                            "moves them once per 4 steps, so its effective fraction can exceed 1)")
+            res[f"{name}_{mode}"] = {"value": cells * steps / t / 1e9, "s_total": t, "roofline": roof,
+                                     "kernels": _kernels(prof)}
+            del S
+    for name in ("window_mean", "vn_diffusion"):
+        res[f"{name}_speedup"] = res[f"{name}_blocked"]["value"] / res[f"{name}_per_step"]["value"]
+    # e2e: host grid in, 100 blocked steps, host grid out
+    Se = st.SwitchingStencilArray(d.clone(), st.Window(1), st.Wrap())
+    holder = {"S": Se}
+
+    def run_e2e():
+        holder["S"] = st.mapstencil_(st.mean, holder["S"], steps=steps, sync=False)
+    te = _e2e_map(st, a, Se.source, Se.source, run_e2e, 1, 1)   # steps even: the result is in the input parent
+    cpu = _cpu_rate(lambda orc, A, thr: orc.map_steps(np.asfortranarray(a[:512, :512]), np.asfortranarray(a[:512, :512]),
+                                                      A.F32, st.Window(1), st.mean, st.Wrap(), st.Conditional(), 4,
+                                                      nthreads=thr), 512 * 512 * 4, 2.0)
+    cpu["sample"] = "4 steps of a 512^2 grid per call, " + cpu["sample"]
+    return {"workload": f"Window(1) mean and VonNeumann(1) diffusion, Float32 {side}^2, Wrap, {steps} steps",
+            "unit": UNIT, "value": res["window_mean_blocked"]["value"], "results": res,
+            "e2e": {"value": cells * steps / te / 1e9, "unit": UNIT, "dtype": "f32",
+                    "h2d_bytes_per_step": a.nbytes, "d2h_bytes_per_step": a.nbytes},
+            "cpu_baseline": cpu}
+
+
 def _batched_jobs(st, rng, n=256):
     k5 = rng.standard_normal(25).astype(np.float32)
     sten = [(st.mean, st.Window(1)), (st.mean, st.Circle(3)), (st.sum, st.Cross(2)),
@@ -841,8 +898,8 @@ def cfg_serving(args):
             "e2e": {"note": "every figure of this configuration is end to end: host input to host result"}}
 
 
-CONFIGS = {"mean_blur": cfg_mean_blur, "gauss": cfg_gauss, "diffusion": cfg_diffusion, "batched": cfg_batched,
-           "serving": cfg_serving}
+CONFIGS = {"mean_blur": cfg_mean_blur, "gauss": cfg_gauss, "diffusion": cfg_diffusion, "blocked2d": cfg_blocked2d,
+           "batched": cfg_batched, "serving": cfg_serving}
 
 
 def run_configs(args, local):

@@ -327,7 +327,8 @@ STC_API int stc_batch_run_sequential(stc_batch* b, void* stream);
 typedef struct stc_server stc_server;
 
 typedef struct {
-    stc_grid    grid;         /* host-side description: data points to HOST memory holding the input */
+    stc_grid    grid;         /* host-side description: data points to HOST memory holding the input,
+                                 column-major, rows of size[0] elements stride[1] >= size[0] apart */
     stc_stencil stencil;
     stc_op      op;
     stc_bc      bc;
@@ -338,7 +339,11 @@ typedef struct {
  * steps_per_tick: most steps any job advances per batched launch (continuous-batching tick). */
 STC_API int stc_server_create(stc_server** out, double hbm_fraction, int32_t steps_per_tick);
 STC_API int stc_server_destroy(stc_server* s);
-/* Queue a job (copied, including its host input).  *out_id identifies it. */
+/* Queue a job.  Its description and host input are consumed before the call returns (the input is
+ * copied straight into the job's device state while the HBM budget allows, else into pinned staging
+ * memory), so the caller may reuse the buffer.  Grids of at least 2^21 cells run alone on their own
+ * stream (STC_SERVE_SOLO_CELLS overrides the threshold), the others in batched ticks.  *out_id
+ * identifies the job. */
 STC_API int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id);
 /* Non-blocking: 1 if the job finished (its result can be fetched), 0 if not, or a status. */
 STC_API int stc_server_poll(stc_server* s, int64_t id);

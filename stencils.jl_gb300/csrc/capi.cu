@@ -876,6 +876,11 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
         rc = tb3d_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, flags, &done);
         if (rc) return rc;
     }
+    // 2D radius-1 Float32 maps: blocked passes of 4 steps, the last few steps per step below
+    if (done == 0) {
+        rc = tb2d_try_steps(a, b, st, op, bc, nsteps, &src_is_b, s, ctx, &done);
+        if (rc) return rc;
+    }
     if (done == 0 && (flags & STC_KEEP_F32) && (a->dtype == STC_BF16 || a->dtype == STC_F16) && nsteps > 0)
         return STC_ERR_UNSUPPORTED;
     // other 3D grids whose boundary needs edge patching: steps on an internal Halo-padded pair

@@ -3,18 +3,24 @@
 // Replaces the loop  A = mapstencil!(rule, A::SwitchingStencilArray)  (src/gatherstencil.jl:77-83,
 // src/array.jl:610-611) for 2D Moore(1) rules on UInt8 / Bool / Int32 / Int64 grids.
 //
-// Layout: the logical grid is packed 32 cells per 32-bit word along the contiguous axis (bit j of
-// word w is cell 32w + j), rows stacked along axis 1.  A launch advances every row band by up to k
-// generations: each CTA holds full rows (the x-wrap happens inside shared memory) for its band plus
-// k halo rows above and below (y-wrap or zero rows from global), steps them k times in a shared
-// ping-pong pair — the valid band shrinks by one row per generation — and writes the band back.
-// One HBM/L2 round trip per k generations instead of per generation.
+// Packed layout (column-interleaved): a row of n0 = 32 W cells becomes W 32-bit words, and bit j of
+// word w is cell x = j W + w.  The left and right neighbours of every cell of word w are then the same
+// bit of words w-1 and w+1 — no shifts — except across the row's two ends: the left neighbour word of
+// word 0 is word W-1 rotated left by one bit (cell jW - 1 is bit j-1 of word W-1; cell -1 is cell
+// n0-1 under Wrap), and the right neighbour word of word W-1 is word 0 rotated right by one.  Under
+// Remove(0) the rotations become shifts that bring in a dead cell.  In shared memory each row is kept
+// with those two derived words around it, [left ghost | words 0 .. W-1 | right ghost] (pitch W + 2),
+// written by the two threads that produce words W-1 and 0, so every thread reads its three neighbour
+// words at fixed offsets.
 //
-// Per word, each row's 3-cell sum (2 bits, from funnel shifts of its (w-1, w, w+1) words) is formed
-// once as the row enters a rolling three-row window; a carry-save adder adds the three rows' sums into
-// the 4-bit 3x3 total and the rule is evaluated bitwise on it (neighbours = total - centre).
-// The neighbour count is the count of nonzero neighbours, exactly what the LIFE op counts, so the
-// result is bit-identical to the per-cell gather for any input values.
+// A launch advances every row band by up to k generations: each CTA holds full rows for its band plus
+// k halo rows above and below (y-wrap, zero rows, or the neighbouring bands' rows), steps them k times
+// in a shared ping-pong pair — the valid band shrinks by one row per generation — and writes the band
+// back.  Per word, each row's 3-cell sum (2 bit planes) is formed once as the row enters a rolling
+// three-row window; a carry-save adder adds the three rows' sums into the 3x3 total t, and the rule
+// is evaluated bitwise on it (neighbours = t - centre).  The neighbour count is the count of nonzero
+// neighbours, exactly what the LIFE op counts, so the result is bit-identical to the per-cell gather
+// for any input values.
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
@@ -28,11 +34,22 @@ namespace stc {
 
 constexpr int kLifeMaxThreads = 1024;
 
-// CTA size of the Life kernels: 512 threads (STC_LIFE_THREADS = 1024 overrides, a tuning knob)
-static int life_threads() {
+// CTA size of the Life kernels: 512 threads (16 warps; for 4096^2 the measured best of 128, 256 and 512
+// with the warp-row split: 1.49, 1.10 and 0.96 ms per 1000 generations).  STC_LIFE_THREADS = 128, 256
+// or 1024 overrides for the warp-row split, 1024 for the column split (a tuning knob).
+static int life_threads(int W) {
     const char* e = getenv("STC_LIFE_THREADS");
-    return (e && atoi(e) == 1024) ? 1024 : 512;
+    const int v = e ? atoi(e) : 0;
+    if (W == 128) return (v == 128 || v == 256 || v == 1024) ? v : 512;
+    return v == 1024 ? 1024 : 512;
 }
+
+// Two ways to split a band row among threads.  WPL = 0: one packed column per thread; rows are stored
+// with their two ghost words (pitch W + 2).  WPL > 0 (W = 32 WPL): one warp per row, WPL consecutive
+// words per lane; the words beyond a lane's run come from the neighbouring lanes by shuffle (lanes 0 and
+// 31 wrap around and rotate), so rows are stored bare (pitch W).
+template <int WPL>
+__host__ __device__ __forceinline__ int life_pitch(int W) { return WPL > 0 ? W : W + 2; }
 
 __device__ __forceinline__ void full_add(uint32_t a, uint32_t b, uint32_t c, uint32_t& s, uint32_t& cy) {
     const uint32_t t = a ^ b;
@@ -40,53 +57,295 @@ __device__ __forceinline__ void full_add(uint32_t a, uint32_t b, uint32_t c, uin
     cy = (a & b) | (t & c);
 }
 
-// One source row seen from one column word: its 3-cell sums around every bit (a3 + 2 b3 = L + C + R,
-// used when the row is above or below the output row), its 2-cell sums (a2 + 2 b2 = L + R, used when
-// it is the output's own row) and the centre word itself.
-struct RowV { uint32_t a3, b3, a2, b2, c; };
+// the left neighbour word of word 0 from word W-1, and the right neighbour word of word W-1 from word 0
+template <bool WRAP>
+__device__ __forceinline__ uint32_t ghost_left(uint32_t last) {
+    return WRAP ? __funnelshift_l(last, last, 1) : last << 1;
+}
+template <bool WRAP>
+__device__ __forceinline__ uint32_t ghost_right(uint32_t first) {
+    return WRAP ? __funnelshift_r(first, first, 1) : first >> 1;
+}
 
-__device__ __forceinline__ RowV row_v(uint32_t wl, uint32_t c, uint32_t wr) {
-    const uint32_t L = __funnelshift_l(wl, c, 1), R = __funnelshift_r(c, wr, 1);
+// word w of band row r (pitch P), with the ghost word it determines when rows carry them
+template <int WPL>
+__device__ __forceinline__ uint32_t& band_word(uint32_t* buf, int P, int r, int w) {
+    return buf[(size_t)r * P + (WPL > 0 ? 0 : 1) + w];
+}
+template <bool WRAP, int WPL>
+__device__ __forceinline__ void put_word(uint32_t* buf, int P, int W, int r, int w, uint32_t v) {
+    band_word<WPL>(buf, P, r, w) = v;
+    if (WPL == 0) {
+        uint32_t* row = buf + (size_t)r * P;
+        if (w == W - 1) row[0] = ghost_left<WRAP>(v);
+        if (w == 0) row[W + 1] = ghost_right<WRAP>(v);
+    }
+}
+
+// One source row seen from one column word: its 3-cell sums around every bit (a3 + 2 b3 = L + C + R)
+// and the centre word.
+struct RowV { uint32_t a3, b3, c; };
+
+__device__ __forceinline__ RowV row_v(uint32_t l, uint32_t c, uint32_t r) {
     RowV v;
-    v.a3 = L ^ c ^ R;
-    v.b3 = (L & c) | (R & (L ^ c));
-    v.a2 = L ^ R;
-    v.b2 = L & R;
+    v.a3 = l ^ c ^ r;
+    v.b3 = (l & c) | (r & (l ^ c));
     v.c = c;
     return v;
 }
 
-// next state of the middle row m from the neighbour count n = sum3(u) + sum2(m) + sum3(d), 0..8, held
-// as bit planes n0..n3 (B3/S23 uses the 3x3 total instead)
+// next state of the middle row m from the 3x3 total t = sum3(u) + sum3(m) + sum3(d), 0..9: a dead
+// cell is born when its neighbour count t is in `birth`, a live one survives when t - 1 is in `survive`
 template <bool CONWAY>
 __device__ __forceinline__ uint32_t next_state(const RowV& u, const RowV& m, const RowV& d, uint32_t birth,
                                                uint32_t survive) {
+    uint32_t t0, k0, x1, k1;
+    full_add(u.a3, m.a3, d.a3, t0, k0);   // weight 1 and its carry (weight 2)
+    full_add(u.b3, m.b3, d.b3, x1, k1);   // weight 2 and its carry (weight 4)
+    const uint32_t t1 = x1 ^ k0;
     if constexpr (CONWAY) {
-        // B3/S23 from the 3x3 total t = n + centre (0..9): alive next iff t == 3, or t == 4 and alive.
-        // Only t's low three bits are formed: t in {3, 4} is exactly (t0^t2) & (t1^t2) (8 and 9 fail
-        // it), and t2 tells the two apart.
-        uint32_t t0, k0, x1, k1;
-        full_add(u.a3, m.a3, d.a3, t0, k0);
-        full_add(u.b3, m.b3, d.b3, x1, k1);
-        const uint32_t t1 = x1 ^ k0;
+        // B3/S23: alive next iff t == 3, or t == 4 and alive.  Only t's low three bits are formed:
+        // t in {3, 4} is exactly (t0^t2) & (t1^t2) (8 and 9 fail it), and t2 tells the two apart.
         const uint32_t t2 = k1 ^ (x1 & k0);
         return ((t0 ^ t2) & (t1 ^ t2)) & (~t2 | m.c);
     } else {
-        uint32_t n0, k0, x1, k1;
-        full_add(u.a3, m.a2, d.a3, n0, k0);    // weight 1 and its carry (weight 2)
-        full_add(u.b3, m.b2, d.b3, x1, k1);    // weight 2 and its carry (weight 4)
-        const uint32_t n1 = x1 ^ k0;
-        const uint32_t n2 = k1 ^ (x1 & k0);
-        const uint32_t n3 = k1 & x1 & k0;
+        const uint32_t c2 = x1 & k0;
+        const uint32_t t2 = k1 ^ c2, t3 = k1 & c2;
         uint32_t out = 0;
 #pragma unroll
-        for (int v = 0; v <= 8; ++v) {
-            const uint32_t eq = ((v & 1) ? n0 : ~n0) & ((v & 2) ? n1 : ~n1) & ((v & 4) ? n2 : ~n2) &
-                                ((v & 8) ? n3 : ~n3);
-            if ((birth >> v) & 1u) out |= eq & ~m.c;
-            if ((survive >> v) & 1u) out |= eq & m.c;
+        for (int v = 0; v <= 9; ++v) {
+            const bool b = v <= 8 && ((birth >> v) & 1u);
+            const bool s = v >= 1 && ((survive >> (v - 1)) & 1u);
+            if (!b && !s) continue;
+            const uint32_t eq = ((v & 1) ? t0 : ~t0) & ((v & 2) ? t1 : ~t1) & ((v & 4) ? t2 : ~t2) &
+                                ((v & 8) ? t3 : ~t3);
+            out |= eq & (b ? (s ? ~0u : ~m.c) : m.c);
         }
         return out;
+    }
+}
+
+// A thread's fixed share of a band: packed column w of row strip s (of `strips`).  Columns run
+// W-1, 0, 1, .., W-2 across the threads of a strip, so the two threads that write the row's ghost
+// words (w == W-1 and w == 0) sit in the strip's first warp; only warps holding one of them take the
+// ghost-writing variant of the row loop.
+struct LifeLane {
+    bool active;
+    bool edge_warp;
+    bool gl, gr;   // writes the left ghost (w == W-1) / the right ghost (w == 0)
+    int w;
+    int s, strips;
+    float inv_strips;
+};
+
+template <int WPL>
+__device__ __forceinline__ LifeLane life_lane(int W) {
+    LifeLane L;
+    if constexpr (WPL > 0) {
+        // one row strip per warp
+        L.strips = (int)blockDim.x >> 5;
+        L.inv_strips = 1.0f / (float)L.strips;
+        L.s = threadIdx.x >> 5;
+        L.active = true;
+        L.edge_warp = false;
+        L.gl = L.gr = false;
+        L.w = 0;
+        return L;
+    }
+    L.strips = max(1, (int)blockDim.x / W);
+    L.inv_strips = 1.0f / (float)L.strips;
+    const int item = threadIdx.x;
+    const int c = item % W;
+    L.s = item / W;
+    L.active = item < W * L.strips;
+    L.w = c == 0 ? W - 1 : c - 1;
+    L.gl = L.active && L.w == W - 1;
+    L.gr = L.active && L.w == 0;
+    L.edge_warp = __any_sync(0xffffffffu, L.gl || L.gr);
+    return L;
+}
+
+// Rows [ra, rb) of one strip: source rows ra-1 .. rb, each read as its (left, centre, right) words at
+// fixed offsets and reduced to its 3-cell sums once as it enters a three-row window; the row walk is
+// unrolled by three with the window's roles rotating, so nothing is copied between registers.
+template <bool CONWAY, bool WRAP, int WT, bool EDGE>
+__device__ __forceinline__ void life_strip(const LifeLane& L, const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int Wrt, int ra,
+                                           int rb, uint32_t birth, uint32_t survive) {
+    const int W = WT > 0 ? WT : Wrt;
+    const int P = life_pitch<0>(W);
+    const uint32_t* ps = src + (ra - 1) * P + L.w;   // left word of row ra-1; centre at +1, right at +2
+    uint32_t* pd = dst + ra * P + 1 + L.w;
+    auto load = [&](int q) -> RowV { return row_v(ps[q * P], ps[q * P + 1], ps[q * P + 2]); };
+    auto emit = [&](int q, const RowV& u, const RowV& m, const RowV& d) {
+        const uint32_t nx = next_state<CONWAY>(u, m, d, birth, survive);
+        pd[q * P] = nx;
+        if (EDGE) {
+            if (L.gl) pd[q * P - W] = ghost_left<WRAP>(nx);
+            if (L.gr) pd[q * P + W] = ghost_right<WRAP>(nx);
+        }
+    };
+    RowV v0 = load(0), v1 = load(1), v2;
+    int r = ra;
+    // invariant: v0 = row r-1, v1 = row r; ps at row r-1, pd at row r
+    for (; r + 3 <= rb; r += 3) {
+        v2 = load(2);
+        emit(0, v0, v1, v2);
+        v0 = load(3);
+        emit(1, v1, v2, v0);
+        v1 = load(4);
+        emit(2, v2, v0, v1);
+        ps += 3 * P;
+        pd += 3 * P;
+    }
+    if (r < rb) {
+        v2 = load(2);
+        emit(0, v0, v1, v2);
+        if (r + 1 < rb) {
+            v0 = load(3);
+            emit(1, v1, v2, v0);
+        }
+    }
+}
+
+template <int WPL>
+__device__ __forceinline__ void ld_words(const uint32_t* p, uint32_t (&c)[WPL]) {
+    if constexpr (WPL == 4) {
+        const uint4 v = *(const uint4*)p;
+        c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+    } else if constexpr (WPL == 2) {
+        const uint2 v = *(const uint2*)p;
+        c[0] = v.x; c[1] = v.y;
+    } else {
+#pragma unroll
+        for (int i = 0; i < WPL; ++i) c[i] = p[i];
+    }
+}
+template <int WPL>
+__device__ __forceinline__ void st_words(uint32_t* p, const uint32_t (&c)[WPL]) {
+    if constexpr (WPL == 4) *(uint4*)p = make_uint4(c[0], c[1], c[2], c[3]);
+    else if constexpr (WPL == 2) *(uint2*)p = make_uint2(c[0], c[1]);
+    else {
+#pragma unroll
+        for (int i = 0; i < WPL; ++i) p[i] = c[i];
+    }
+}
+
+// Rows [ra, rb) of a band with W = 32 WPL words per row, computed by one warp: lane l holds words
+// l WPL .. l WPL + WPL - 1 of every row it reads.  Each source row is read once (one vector load per
+// lane), its two outer neighbour words arrive by shuffle, and it is reduced to its 3-cell sums as it
+// enters the rolling three-row window.
+template <bool CONWAY, bool WRAP, int WPL>
+__device__ __forceinline__ void life_warp_rows(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int ra,
+                                               int rb, uint32_t birth, uint32_t survive) {
+    constexpr int W = 32 * WPL;
+    const int lane = threadIdx.x & 31;
+    const int lane_l = (lane + 31) & 31, lane_r = (lane + 1) & 31;
+    const uint32_t* ps = src + (ra - 1) * W + lane * WPL;   // row ra-1
+    uint32_t* pd = dst + ra * W + lane * WPL;
+    struct RowW { RowV v[WPL]; };
+    auto load = [&](int q) -> RowW {
+        uint32_t c[WPL];
+        ld_words<WPL>(ps + q * W, c);
+        uint32_t left = __shfl_sync(0xffffffffu, c[WPL - 1], lane_l);
+        uint32_t right = __shfl_sync(0xffffffffu, c[0], lane_r);
+        if (lane == 0) left = ghost_left<WRAP>(left);      // word W-1 seen from word 0
+        if (lane == 31) right = ghost_right<WRAP>(right);  // word 0 seen from word W-1
+        RowW r;
+#pragma unroll
+        for (int i = 0; i < WPL; ++i) r.v[i] = row_v(i ? c[i - 1] : left, c[i], i < WPL - 1 ? c[i + 1] : right);
+        return r;
+    };
+    auto emit = [&](int q, const RowW& u, const RowW& m, const RowW& d) {
+        uint32_t o[WPL];
+#pragma unroll
+        for (int i = 0; i < WPL; ++i) o[i] = next_state<CONWAY>(u.v[i], m.v[i], d.v[i], birth, survive);
+        st_words<WPL>(pd + q * W, o);
+    };
+    RowW v0 = load(0), v1 = load(1), v2;
+    int r = ra;
+    for (; r + 3 <= rb; r += 3) {
+        v2 = load(2);
+        emit(0, v0, v1, v2);
+        v0 = load(3);
+        emit(1, v1, v2, v0);
+        v1 = load(4);
+        emit(2, v2, v0, v1);
+        ps += 3 * W;
+        pd += 3 * W;
+    }
+    if (r < rb) {
+        v2 = load(2);
+        emit(0, v0, v1, v2);
+        if (r + 1 < rb) {
+            v0 = load(3);
+            emit(1, v1, v2, v0);
+        }
+    }
+}
+
+// Advance a band kk generations in the shared ping-pong pair (cur, oth), pitch life_pitch<WPL>(W).  Generation g
+// computes rows [max(g+1, lo_lim), min(rows-g-1, hi_lim)) — the rows whose three source rows are still
+// valid, and (Remove) only rows inside the grid; rows outside it stay zero in both buffers — split into
+// the lanes' strips.  Returns the buffer holding the result.  Ends with a barrier.
+template <bool CONWAY, bool WRAP, int WT, int WPL>
+__device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
+                                               int kk, int lo_lim, int hi_lim, uint32_t birth, uint32_t survive) {
+    for (int g = 0; g < kk; ++g) {
+        const int lo = max(g + 1, lo_lim), hi = min(rows - g - 1, hi_lim);
+        const int nr = hi - lo;
+        // strip bounds: the same monotone expression for a strip's end and the next strip's start, so
+        // the strips tile [lo, hi) exactly whatever the float rounding
+        const int ra = lo + (int)((float)(nr * L.s) * L.inv_strips);
+        const int rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
+        if (L.active && ra < rb) {
+            if constexpr (WPL > 0) life_warp_rows<CONWAY, WRAP, WPL>(cur, oth, ra, rb, birth, survive);
+            else if (L.edge_warp) life_strip<CONWAY, WRAP, WT, true>(L, cur, oth, W, ra, rb, birth, survive);
+            else life_strip<CONWAY, WRAP, WT, false>(L, cur, oth, W, ra, rb, birth, survive);
+        }
+        __syncthreads();
+        uint32_t* t = cur;
+        cur = oth;
+        oth = t;
+    }
+    return cur;
+}
+
+// band rows [lo_lim, hi_lim) lie inside the grid (Remove); under Wrap every row does
+template <bool WRAP>
+__device__ __forceinline__ void band_limits(int rows, int gy_first, int n1, int* lo_lim, int* hi_lim) {
+    if (WRAP) {
+        *lo_lim = 1;
+        *hi_lim = rows - 1;
+    } else {
+        *lo_lim = max(1, -gy_first);
+        *hi_lim = min(rows - 1, n1 - gy_first);
+    }
+}
+
+// fill band rows [0, rows) of buf from the packed grid (row gy_first + r; wrapped, or zero outside
+// it) and zero the rows of `other` that lie outside the grid
+template <bool WRAP, int WPL>
+__device__ __forceinline__ void load_band(const uint32_t* in, uint32_t* buf, uint32_t* other, int rows, int W,
+                                          int gy_first, int n1) {
+    const int P = life_pitch<WPL>(W);
+    for (int i = threadIdx.x; i < rows * W; i += blockDim.x) {
+        const int r = i / W, w = i - r * W;
+        int gy = gy_first + r;
+        uint32_t v = 0;
+        if (WRAP) {
+            gy %= n1;
+            if (gy < 0) gy += n1;
+            v = in[(size_t)gy * W + w];
+        } else if (gy >= 0 && gy < n1) {
+            v = in[(size_t)gy * W + w];
+        }
+        put_word<WRAP, WPL>(buf, P, W, r, w, v);
+    }
+    if (!WRAP) {
+        for (int i = threadIdx.x; i < rows * P; i += blockDim.x) {
+            const int gy = gy_first + i / P;
+            if (gy < 0 || gy >= n1) other[i] = 0u;
+        }
     }
 }
 
@@ -101,173 +360,29 @@ struct LifeParams {
     uint32_t birth, survive;
 };
 
-// A thread's fixed share of a band: one column w (or two, w and w + W/2, for narrow rows) and strip s
-// of `strips` row strips.  One column per thread means fewer, longer strips, so the two rows each
-// strip reads before its first output are a smaller share of the work; the unrolled row walk gives
-// the thread its independent instructions.  Computed once per kernel.
-struct LifeLane {
-    int cols;            // 0 (idle thread), 1 or 2
-    int w[2], wl[2], wr[2];
-    bool ledge[2], redge[2];
-    int s, strips;
-    float inv_strips;
-};
-
-__device__ __forceinline__ LifeLane life_lane(int W) {
-    LifeLane L;
-    const int cols = (W % 2 == 0 && W < 64) ? 2 : 1;
-    const int Wc = W / cols;
-    L.strips = max(1, (int)blockDim.x / Wc);
-    L.inv_strips = 1.0f / (float)L.strips;
-    const int item = threadIdx.x;
-    L.cols = item < Wc * L.strips ? cols : 0;
-    const int cb = item % Wc;
-    L.s = item / Wc;
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        L.w[j] = cb + j * Wc;
-        L.ledge[j] = L.w[j] == 0;
-        L.redge[j] = L.w[j] == W - 1;
-        L.wl[j] = L.ledge[j] ? W - 1 : L.w[j] - 1;
-        L.wr[j] = L.redge[j] ? 0 : L.w[j] + 1;
-    }
-    return L;
-}
-
-// Rows [ra, rb) of one strip for NC columns: source row q is read through per-column pointers to
-// its (w-1, w, w+1) words, each row's sums are formed once as it enters a three-row window, and the
-// row walk is unrolled by three with the window's roles rotating, so nothing is copied between
-// registers.  Remove(0) (WRAP false): words beyond the x edges read as zero, and rows outside the grid
-// stay dead.
-template <bool CONWAY, bool WRAP, int WT, int NC>
-__device__ __forceinline__ void life_strip(const LifeLane& L, const uint32_t* src, uint32_t* dst, int Wrt, int ra,
-                                           int rb, int gy_first, int n1, uint32_t birth, uint32_t survive) {
-    const int W = WT > 0 ? WT : Wrt;
-    const uint32_t *pl[NC], *pc[NC], *pr[NC];
-    uint32_t* pd[NC];
-#pragma unroll
-    for (int j = 0; j < NC; ++j) {
-        pl[j] = src + (size_t)(ra - 1) * W + L.wl[j];
-        pc[j] = src + (size_t)(ra - 1) * W + L.w[j];
-        pr[j] = src + (size_t)(ra - 1) * W + L.wr[j];
-        pd[j] = dst + (size_t)ra * W + L.w[j];
-    }
-    // row (ra - 1 + q) of column j
-    auto load = [&](int j, int q) -> RowV {
-        const uint32_t c = pc[j][q * W];
-        const uint32_t l = (!WRAP && L.ledge[j]) ? 0u : pl[j][q * W];
-        const uint32_t r = (!WRAP && L.redge[j]) ? 0u : pr[j][q * W];
-        return row_v(l, c, r);
-    };
-    // output row (ra + q) from the window (u, m, d)
-    auto emit = [&](int j, int q, int r, const RowV& u, const RowV& m, const RowV& d) {
-        uint32_t nx = next_state<CONWAY>(u, m, d, birth, survive);
-        if (!WRAP) {
-            const int gy = gy_first + r;
-            if (gy < 0 || gy >= n1) nx = 0u;   // rows outside the grid stay dead
-        }
-        pd[j][q * W] = nx;
-    };
-    RowV v0[NC], v1[NC], v2[NC];
-#pragma unroll
-    for (int j = 0; j < NC; ++j) {
-        v0[j] = load(j, 0);
-        v1[j] = load(j, 1);
-    }
-    int r = ra;
-    // invariant: v0 = row r-1, v1 = row r; pointers at row r-1 (sources) and row r (destination)
-    for (; r + 3 <= rb; r += 3) {
-#pragma unroll
-        for (int j = 0; j < NC; ++j) v2[j] = load(j, 2);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) emit(j, 0, r, v0[j], v1[j], v2[j]);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) v0[j] = load(j, 3);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) emit(j, 1, r + 1, v1[j], v2[j], v0[j]);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) v1[j] = load(j, 4);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) emit(j, 2, r + 2, v2[j], v0[j], v1[j]);
-#pragma unroll
-        for (int j = 0; j < NC; ++j) {
-            pl[j] += 3 * W;
-            pc[j] += 3 * W;
-            pr[j] += 3 * W;
-            pd[j] += 3 * W;
-        }
-    }
-    if (r < rb) {
-#pragma unroll
-        for (int j = 0; j < NC; ++j) {
-            v2[j] = load(j, 2);
-            emit(j, 0, r, v0[j], v1[j], v2[j]);
-        }
-        if (r + 1 < rb) {
-#pragma unroll
-            for (int j = 0; j < NC; ++j) {
-                v0[j] = load(j, 3);
-                emit(j, 1, r + 1, v1[j], v2[j], v0[j]);
-            }
-        }
-    }
-}
-
-// Advance a band kk generations in the shared ping-pong pair (cur, oth).  cur holds `rows` valid rows
-// of W words; row r is global row gy_first + r.  Generation g computes rows [g+1, rows-g-1) (the
-// rows whose three source rows are still valid) into the other buffer, split into the lanes' strips.
-// Returns the buffer holding the result.  Ends with a barrier.
-template <bool CONWAY, bool WRAP, int WT>
-__device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
-                                               int kk, int gy_first, int n1, uint32_t birth, uint32_t survive) {
-    for (int g = 0; g < kk; ++g) {
-        const int lo = g + 1, hi = rows - g - 1;   // rows computable from the valid rows of cur
-        const int nr = hi - lo;
-        // strip bounds: the same monotone expression for a strip's end and the next strip's start, so
-        // the strips tile [lo, hi) exactly whatever the float rounding
-        const int ra = lo + (int)((float)(nr * L.s) * L.inv_strips);
-        const int rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
-        if (ra < rb) {
-            if (L.cols == 2) life_strip<CONWAY, WRAP, WT, 2>(L, cur, oth, W, ra, rb, gy_first, n1, birth, survive);
-            else if (L.cols == 1) life_strip<CONWAY, WRAP, WT, 1>(L, cur, oth, W, ra, rb, gy_first, n1, birth, survive);
-        }
-        __syncthreads();
-        uint32_t* t = cur;
-        cur = oth;
-        oth = t;
-    }
-    return cur;
-}
+// warp-row split for the compile-time widths it suits (32, 64, 128 words), else one column per thread
+template <int WT>
+__host__ __device__ constexpr int life_wpl() { return (WT > 0 && WT % 32 == 0 && WT / 32 <= 4 && WT / 32 != 3) ? WT / 32 : 0; }
 
 template <bool CONWAY, bool WRAP, int WT>
 __global__ void __launch_bounds__(kLifeMaxThreads) life_block_kernel(const LifeParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
-    const int W = WT > 0 ? WT : p.W, k = p.k;
+    constexpr int WPL = life_wpl<WT>();
+    const int W = WT > 0 ? WT : p.W, P = life_pitch<WPL>(W), k = p.k;
     const int rows = p.TB + 2 * k;
     uint32_t* buf0 = lsm;
-    uint32_t* buf1 = lsm + (size_t)rows * W;
+    uint32_t* buf1 = lsm + (size_t)rows * P;
     const int y0 = blockIdx.x * p.TB;
-    // load the band plus k halo rows
-    for (int i = threadIdx.x; i < rows * W; i += blockDim.x) {
-        const int r = i / W, w = i - r * W;
-        int gy = y0 - k + r;
-        uint32_t v = 0;
-        if (WRAP) {
-            gy %= p.n1;
-            if (gy < 0) gy += p.n1;
-            v = p.in[(size_t)gy * W + w];
-        } else if (gy >= 0 && gy < p.n1) {
-            v = p.in[(size_t)gy * W + w];
-        }
-        buf0[i] = v;
-    }
+    load_band<WRAP, WPL>(p.in, buf0, buf1, rows, W, y0 - k, p.n1);
     __syncthreads();
-    const LifeLane lane = life_lane(W);
-    const uint32_t* fin = life_gens<CONWAY, WRAP, WT>(lane, buf0, buf1, rows, W, k, y0 - k, p.n1, p.birth, p.survive);
+    int lo_lim, hi_lim;
+    band_limits<WRAP>(rows, y0 - k, p.n1, &lo_lim, &hi_lim);
+    const LifeLane lane = life_lane<WPL>(W);
+    uint32_t* fin = life_gens<CONWAY, WRAP, WT, WPL>(lane, buf0, buf1, rows, W, k, lo_lim, hi_lim, p.birth, p.survive);
     for (int i = threadIdx.x; i < p.TB * W; i += blockDim.x) {
         const int r = i / W, w = i - r * W;
         const int gy = y0 + r;
-        if (gy < p.n1) p.out[(size_t)gy * W + w] = fin[(size_t)(r + k) * W + w];
+        if (gy < p.n1) p.out[(size_t)gy * W + w] = band_word<WPL>(fin, P, r + k, w);
     }
 }
 
@@ -303,10 +418,10 @@ __device__ __forceinline__ void st_relaxed_gpu(uint64_t* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// the word of a tagged pair once its tag equals `tag`; false after ~limit SM clocks
-__device__ __forceinline__ bool take_tagged(const uint64_t* p, uint32_t tag, uint32_t* out,
+// the word of a tagged pair once its tag equals `tag`, starting from v, a value already read from p;
+// false after ~limit SM clocks
+__device__ __forceinline__ bool take_tagged(uint64_t v, const uint64_t* p, uint32_t tag, uint32_t* out,
                                             long long limit = 4000000000ll) {
-    uint64_t v = ld_relaxed_gpu(p);
     if ((uint32_t)(v >> 32) != tag) {
         const long long t0 = clock64();
         do {
@@ -321,30 +436,23 @@ __device__ __forceinline__ bool take_tagged(const uint64_t* p, uint32_t tag, uin
 template <bool CONWAY, bool WRAP, int WT>
 __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCoopParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
-    const int W = WT > 0 ? WT : p.W, k = p.k, G = gridDim.x, b = blockIdx.x;
+    constexpr int WPL = life_wpl<WT>();
+    const int W = WT > 0 ? WT : p.W, P = life_pitch<WPL>(W), k = p.k, G = gridDim.x, b = blockIdx.x;
     const int y0 = (int)(((int64_t)b * p.n1) / G), y1 = (int)(((int64_t)(b + 1) * p.n1) / G);
     const int TB = y1 - y0, rows = TB + 2 * k;
     const int TBmax = (p.n1 + G - 1) / G;
+    uint32_t* const buf1 = lsm + (size_t)(TBmax + 2 * k) * P;
     uint32_t* cur = lsm;
-    uint32_t* oth = lsm + (size_t)(TBmax + 2 * k) * W;
-    for (int i = threadIdx.x; i < rows * W; i += blockDim.x) {
-        const int r = i / W, w = i - r * W;
-        int gy = y0 - k + r;
-        uint32_t v = 0;
-        if (WRAP) {
-            gy = gy < 0 ? gy + p.n1 : (gy >= p.n1 ? gy - p.n1 : gy);
-            v = p.in[(size_t)gy * W + w];
-        } else if (gy >= 0 && gy < p.n1) {
-            v = p.in[(size_t)gy * W + w];
-        }
-        cur[i] = v;
-    }
+    uint32_t* oth = buf1;
+    load_band<WRAP, WPL>(p.in, cur, oth, rows, W, y0 - k, p.n1);
     __syncthreads();
+    int lo_lim, hi_lim;
+    band_limits<WRAP>(rows, y0 - k, p.n1, &lo_lim, &hi_lim);
     const int up = b == 0 ? G - 1 : b - 1, dn = b == G - 1 ? 0 : b + 1;
     const bool has_up = WRAP || b > 0, has_dn = WRAP || b < G - 1;
-    const size_t slab = (size_t)k * W;                 // one published row block
+    const int slab = k * W;                            // one published row block
     const int64_t nmain = p.nsteps - 1;                // generations before the last one
-    const LifeLane lane = life_lane(W);
+    const LifeLane lane = life_lane<WPL>(W);
     int64_t gen = 0;
     for (int step = 0;; ++step) {
         const bool final = gen >= nmain;
@@ -355,12 +463,29 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCo
             const uint64_t* from_up = xs + ((size_t)up * 2 + 1) * slab;   // neighbour's last k rows
             const uint64_t* from_dn = xs + ((size_t)dn * 2 + 0) * slab;   // neighbour's first k rows
             bool ok = true;
-            for (int i = threadIdx.x; i < (int)slab; i += blockDim.x) {
-                uint32_t u = 0u, d = 0u;
-                if (has_up && ok) ok = take_tagged(from_up + i, (uint32_t)step, &u);
-                if (has_dn && ok) ok = take_tagged(from_dn + i, (uint32_t)step, &d);
-                cur[i] = u;
-                cur[(size_t)(k + TB) * W + i] = d;
+            // kB elements per thread at a time: all their first reads are in flight together, so a
+            // super-step's exchange costs about one L2 round trip when the neighbours are ready
+            constexpr int kB = 4;
+            for (int i0 = threadIdx.x; i0 < slab; i0 += kB * blockDim.x) {
+                uint64_t vu[kB], vd[kB];
+#pragma unroll
+                for (int j = 0; j < kB; ++j) {
+                    const int i = i0 + j * (int)blockDim.x;
+                    vu[j] = (has_up && i < slab) ? ld_relaxed_gpu(from_up + i) : 0ull;
+                    vd[j] = (has_dn && i < slab) ? ld_relaxed_gpu(from_dn + i) : 0ull;
+                }
+#pragma unroll
+                for (int j = 0; j < kB; ++j) {
+                    const int i = i0 + j * (int)blockDim.x;
+                    if (i < slab) {
+                        uint32_t u = 0u, d = 0u;
+                        if (has_up && ok) ok = take_tagged(vu[j], from_up + i, (uint32_t)step, &u);
+                        if (has_dn && ok) ok = take_tagged(vd[j], from_dn + i, (uint32_t)step, &d);
+                        const int r = i / W, w = i - r * W;
+                        put_word<WRAP, WPL>(cur, P, W, r, w, u);
+                        put_word<WRAP, WPL>(cur, P, W, k + TB + r, w, d);
+                    }
+                }
             }
             if (!__syncthreads_and(ok)) {
                 if (threadIdx.x == 0 && p.status) atomicOr(p.status, DEV_ERR_TIMEOUT);
@@ -369,21 +494,28 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCo
             if (final && p.nsteps > 1) {
                 // generation n-1: every thread has seen both neighbours' publications (so they are past
                 // their initial load), and nobody reads `in` any more
-                for (int i = threadIdx.x; i < TB * W; i += blockDim.x) p.prev[(size_t)y0 * W + i] = cur[(size_t)k * W + i];
+                for (int i = threadIdx.x; i < TB * W; i += blockDim.x) {
+                    const int r = i / W, w = i - r * W;
+                    p.prev[(size_t)y0 * W + i] = band_word<WPL>(cur, P, k + r, w);
+                }
             }
         }
-        cur = life_gens<CONWAY, WRAP, WT>(lane, cur, oth, rows, W, kk, y0 - k, p.n1, p.birth, p.survive);
-        oth = (cur == lsm) ? lsm + (size_t)(TBmax + 2 * k) * W : lsm;
+        cur = life_gens<CONWAY, WRAP, WT, WPL>(lane, cur, oth, rows, W, kk, lo_lim, hi_lim, p.birth, p.survive);
+        oth = (cur == lsm) ? buf1 : lsm;
         gen += kk;
         if (final) {
-            for (int i = threadIdx.x; i < TB * W; i += blockDim.x) p.last[(size_t)y0 * W + i] = cur[(size_t)k * W + i];
+            for (int i = threadIdx.x; i < TB * W; i += blockDim.x) {
+                const int r = i / W, w = i - r * W;
+                p.last[(size_t)y0 * W + i] = band_word<WPL>(cur, P, k + r, w);
+            }
             return;
         }
         uint64_t* xd = p.xbuf + (size_t)(step & 1) * G * 2 * slab + (size_t)b * 2 * slab;
         const uint64_t tag = (uint64_t)(uint32_t)(step + 1) << 32;
-        for (int i = threadIdx.x; i < (int)slab; i += blockDim.x) {
-            st_relaxed_gpu(xd + i, tag | cur[(size_t)k * W + i]);            // band rows y0 .. y0+k-1
-            st_relaxed_gpu(xd + slab + i, tag | cur[(size_t)TB * W + i]);    // band rows y1-k .. y1-1
+        for (int i = threadIdx.x; i < slab; i += blockDim.x) {
+            const int r = i / W, w = i - r * W;
+            st_relaxed_gpu(xd + i, tag | band_word<WPL>(cur, P, k + r, w));           // band rows y0 .. y0+k-1
+            st_relaxed_gpu(xd + slab + i, tag | band_word<WPL>(cur, P, TB + r, w));   // band rows y1-k .. y1-1
         }
     }
 }
@@ -397,7 +529,7 @@ static cudaError_t life_launch_t(const LifeParams& lp, int grid, size_t smem, cu
     cudaError_t e = cudaFuncSetAttribute(life_block_kernel<C, WR, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    life_block_kernel<C, WR, WT><<<grid, life_threads(), smem, s>>>(lp);
+    life_block_kernel<C, WR, WT><<<grid, life_threads(lp.W), smem, s>>>(lp);
     return cudaGetLastError();
 }
 
@@ -413,6 +545,12 @@ static cudaError_t life_launch(const LifeParams& lp, bool conway, int grid, size
     return lp.W == kLifeWT ? life_launch_w<kLifeWT>(lp, conway, grid, smem, s) : life_launch_w<0>(lp, conway, grid, smem, s);
 }
 
+// bytes of shared memory for a band pair of `rows` rows of W words (the split the kernels use for W)
+static size_t life_band_smem(int rows, int W) {
+    const int P = W == kLifeWT ? life_pitch<life_wpl<kLifeWT>()>(W) : life_pitch<0>(W);
+    return (size_t)2 * rows * P * sizeof(uint32_t);
+}
+
 // ------------------------------------------------------------------ pack / unpack
 struct PackParams {
     const void* base;   // parent base
@@ -423,64 +561,35 @@ struct PackParams {
     uint32_t* P;
 };
 
+// one thread per packed word: bit j of word (y, w) is cell (j W + w, y), so the 32 reads of a warp's
+// threads for one j are consecutive cells
 template <class T>
 __global__ void life_pack_kernel(const PackParams p) {
     const T* base = (const T*)p.base;
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t groups = (int64_t)p.n1 * ((p.W + 31) / 32);
-    for (int64_t gi = warp; gi < groups; gi += nwarps) {
-        const int gpr = (p.W + 31) / 32;
-        const int y = (int)(gi / gpr), w0 = (int)(gi % gpr) * 32;
-        const T* row = base + p.org + (int64_t)y * p.sy;
-        uint32_t mine = 0;
-        const int nw = min(32, p.W - w0);
-        if (nw == 32) {
-            // all 32 loads issued before the first ballot, so the group costs one memory latency
-            bool nz[32];
+    const int64_t nwords = (int64_t)p.n1 * p.W;
+    for (int64_t gi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gi < nwords; gi += (int64_t)gridDim.x * blockDim.x) {
+        const int y = (int)(gi / p.W), w = (int)(gi - (int64_t)y * p.W);
+        const T* cell = base + p.org + (int64_t)y * p.sy + w;
+        bool nz[32];
 #pragma unroll
-            for (int i = 0; i < 32; ++i) nz[i] = row[(int64_t)(w0 + i) * 32 + lane] != (T)0;
+        for (int j = 0; j < 32; ++j) nz[j] = cell[(int64_t)j * p.W] != (T)0;   // all loads before use
+        uint32_t v = 0;
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const uint32_t b = __ballot_sync(0xffffffffu, nz[i]);
-                if (lane == i) mine = b;
-            }
-        } else {
-            for (int i = 0; i < nw; ++i) {
-                const uint32_t b = __ballot_sync(0xffffffffu, row[(int64_t)(w0 + i) * 32 + lane] != (T)0);
-                if (lane == i) mine = b;
-            }
-        }
-        if (lane < nw) p.P[(size_t)y * p.W + w0 + lane] = mine;
+        for (int j = 0; j < 32; ++j) v |= (uint32_t)nz[j] << j;
+        p.P[gi] = v;
     }
 }
 
 template <class T>
 __global__ void life_unpack_kernel(const PackParams p) {
     T* base = (T*)p.base;
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t groups = (int64_t)p.n1 * ((p.W + 31) / 32);
-    for (int64_t gi = warp; gi < groups; gi += nwarps) {
-        const int gpr = (p.W + 31) / 32;
-        const int y = (int)(gi / gpr), w0 = (int)(gi % gpr) * 32;
-        T* row = base + p.org + (int64_t)y * p.sy;
-        const int nw = min(32, p.W - w0);
-        const uint32_t mine = lane < nw ? p.P[(size_t)y * p.W + w0 + lane] : 0u;
-        if (nw == 32) {
+    const int64_t nwords = (int64_t)p.n1 * p.W;
+    for (int64_t gi = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; gi < nwords; gi += (int64_t)gridDim.x * blockDim.x) {
+        const int y = (int)(gi / p.W), w = (int)(gi - (int64_t)y * p.W);
+        T* cell = base + p.org + (int64_t)y * p.sy + w;
+        const uint32_t v = p.P[gi];
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-                row[(int64_t)(w0 + i) * 32 + lane] = (T)((word >> lane) & 1u);
-            }
-        } else {
-            for (int i = 0; i < nw; ++i) {
-                const uint32_t word = __shfl_sync(0xffffffffu, mine, i);
-                row[(int64_t)(w0 + i) * 32 + lane] = (T)((word >> lane) & 1u);
-            }
-        }
+        for (int j = 0; j < 32; ++j) cell[(int64_t)j * p.W] = (T)((v >> j) & 1u);
     }
 }
 
@@ -530,8 +639,8 @@ static bool is_moore1_2d(const stc_stencil* st) {
 void life_plan(int W, int n1, int64_t steps_left, int smem_cap, int num_sms, int* TB, int* k) {
     int kk = (int)std::min<int64_t>(steps_left, 16);
     int tb = std::max(8, (n1 + num_sms - 1) / num_sms);
-    while (kk > 1 && (int64_t)2 * (tb + 2 * kk) * W * 4 > smem_cap) --kk;
-    while (tb > 1 && (int64_t)2 * (tb + 2 * kk) * W * 4 > smem_cap) --tb;
+    while (kk > 1 && (int64_t)life_band_smem(tb + 2 * kk, W) > smem_cap) --kk;
+    while (tb > 1 && (int64_t)life_band_smem(tb + 2 * kk, W) > smem_cap) --tb;
     *TB = tb;
     *k = kk;
 }
@@ -553,12 +662,12 @@ static bool life_coop_enabled() {
 }
 
 template <bool C, bool WR, int WT>
-static cudaError_t coop_fits_t(int grid, size_t smem, int num_sms, bool* fits) {
+static cudaError_t coop_fits_t(int W, int grid, size_t smem, int num_sms, bool* fits) {
     auto fn = life_coop_kernel<C, WR, WT>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, life_threads(), smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, life_threads(W), smem);
     *fits = e == cudaSuccess && (int64_t)nb * num_sms >= grid;
     return e;
 }
@@ -567,7 +676,7 @@ template <bool C, bool WR, int WT>
 static cudaError_t coop_launch_t(const LifeCoopParams& cp, int grid, size_t smem, cudaStream_t s) {
     LifeCoopParams arg = cp;
     void* args[] = {&arg};
-    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR, WT>, dim3(grid), dim3(life_threads()), args,
+    return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR, WT>, dim3(grid), dim3(life_threads(cp.W)), args,
                                        smem, s);
 }
 
@@ -575,10 +684,10 @@ static cudaError_t coop_launch_t(const LifeCoopParams& cp, int grid, size_t smem
 template <int WT>
 static cudaError_t coop_dispatch_w(bool query, bool conway, bool wrap, const LifeCoopParams& cp, int grid, size_t smem,
                                    cudaStream_t s, int num_sms, bool* fits) {
-    if (conway && wrap) return query ? coop_fits_t<true, true, WT>(grid, smem, num_sms, fits) : coop_launch_t<true, true, WT>(cp, grid, smem, s);
-    if (conway) return query ? coop_fits_t<true, false, WT>(grid, smem, num_sms, fits) : coop_launch_t<true, false, WT>(cp, grid, smem, s);
-    if (wrap) return query ? coop_fits_t<false, true, WT>(grid, smem, num_sms, fits) : coop_launch_t<false, true, WT>(cp, grid, smem, s);
-    return query ? coop_fits_t<false, false, WT>(grid, smem, num_sms, fits) : coop_launch_t<false, false, WT>(cp, grid, smem, s);
+    if (conway && wrap) return query ? coop_fits_t<true, true, WT>(cp.W, grid, smem, num_sms, fits) : coop_launch_t<true, true, WT>(cp, grid, smem, s);
+    if (conway) return query ? coop_fits_t<true, false, WT>(cp.W, grid, smem, num_sms, fits) : coop_launch_t<true, false, WT>(cp, grid, smem, s);
+    if (wrap) return query ? coop_fits_t<false, true, WT>(cp.W, grid, smem, num_sms, fits) : coop_launch_t<false, true, WT>(cp, grid, smem, s);
+    return query ? coop_fits_t<false, false, WT>(cp.W, grid, smem, num_sms, fits) : coop_launch_t<false, false, WT>(cp, grid, smem, s);
 }
 
 static cudaError_t coop_dispatch(bool query, bool conway, bool wrap, const LifeCoopParams& cp, int grid, size_t smem,
@@ -607,7 +716,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
         k = (int)n1;
     }
     const int TBmax = (int)((n1 + G - 1) / G);
-    const size_t smem = (size_t)2 * (TBmax + 2 * k) * W * 4;
+    const size_t smem = life_band_smem(TBmax + 2 * k, W);
     if ((int64_t)smem > ctx->max_smem_optin - 1024) return STC_OK;
 
     const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
@@ -636,7 +745,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
     cp.prev = P0;
     cp.last = P1;
     cp.xbuf = X;
-    cp.status = ctx->status;
+    cp.status = status_slot(ctx, stream).dev;
     cp.W = W;
     cp.n1 = (int)n1;
     cp.k = k;
@@ -682,7 +791,7 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     const int smem_cap = ctx->max_smem_optin - 1024;
     int TB, k;
     life_plan(W, (int)n1, nsteps, smem_cap, ctx->num_sms, &TB, &k);
-    if ((int64_t)2 * (TB + 2 * k) * W * 4 > smem_cap) return STC_OK;
+    if ((int64_t)life_band_smem(TB + 2 * k, W) > smem_cap) return STC_OK;
 
     const size_t words = (size_t)W * n1;
     uint32_t* P = nullptr;
@@ -710,7 +819,7 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
         lp.out = Pbuf[1 - cur];
         lp.TB = TB;
         lp.k = k;
-        const size_t smem = (size_t)2 * (TB + 2 * k) * W * 4;
+        const size_t smem = life_band_smem(TB + 2 * k, W);
         const int grid = (int)((n1 + TB - 1) / TB);
         void* prof = prof_begin(stream);
         e = life_launch(lp, conway, grid, smem, stream);
@@ -812,9 +921,9 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     if (!wrap && !remove0) return STC_ERR_UNSUPPORTED;
     const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
     if (n0 < 32 || n0 % 32 != 0 || n1 < 1) return STC_ERR_UNSUPPORTED;
-    // life_block_kernel gives each thread at most one packed column once rows are 64 words or wider, so
-    // rows wider than the CTA (kNoAllocMaxWords words) would leave columns uncomputed
-    if (n0 / 32 > kNoAllocMaxWords || n0 / 32 > life_threads()) return STC_ERR_UNSUPPORTED;
+    // life_block_kernel gives each thread one packed column of a strip, so rows wider than the CTA
+    // (kNoAllocMaxWords words) would leave columns uncomputed
+    if (n0 / 32 > kNoAllocMaxWords || n0 / 32 > life_threads((int)(n0 / 32))) return STC_ERR_UNSUPPORTED;
     if (n0 * n1 > kNoAllocMaxCells) return STC_ERR_TOO_LARGE;
     if (nsteps > 0 && a->data == b->data) return STC_ERR_INVALID;
     if (nsteps == 0) {
@@ -835,7 +944,7 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     const int smem_cap = smem_optin - 1024;
     int TB, k;
     life_plan(W, (int)n1, nsteps, smem_cap, num_sms, &TB, &k);
-    if ((int64_t)2 * (TB + 2 * k) * W * 4 > smem_cap) return STC_ERR_UNSUPPORTED;
+    if ((int64_t)life_band_smem(TB + 2 * k, W) > smem_cap) return STC_ERR_UNSUPPORTED;
     uint32_t* Pbuf[2] = {P, P + kNoAllocWords};
     const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
     if ((rc = noalloc_pack_launch(true, a, org_a, W, (int)n1, Pbuf[0], s, num_sms))) return rc;
@@ -855,7 +964,7 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
         lp.out = Pbuf[1 - cur];
         lp.TB = TB;
         lp.k = k;
-        const size_t smem = (size_t)2 * (TB + 2 * k) * W * 4;
+        const size_t smem = life_band_smem(TB + 2 * k, W);
         const int grid = (int)((n1 + TB - 1) / TB);
         if ((e = life_launch(lp, conway, grid, smem, s)) != cudaSuccess) return cuda_fail(e);
         cur = 1 - cur;

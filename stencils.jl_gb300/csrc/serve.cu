@@ -1,18 +1,30 @@
 // serve.cu — continuous batching of stencil jobs with device-resident state.
 //
 // No counterpart in the reference (a caller there runs each job as its own mapstencil! loop).
-// Clients submit jobs (a host grid, stencil, reduction, boundary, step count).  A scheduler thread:
-//   1. admits queued jobs in arrival order while their two device parents fit in the HBM budget
-//      (a fraction of the free device memory at creation), copying the input to the device once;
-//   2. runs a tick: one batched launch (batch.cu) that advances every admitted job by up to
-//      steps_per_tick steps, whatever its grid size, stencil or element type;
-//   3. retires jobs that reached their step count: their result is copied to pinned host memory, their
-//      device memory returns to the budget, and their latency (submit to result on host) is recorded.
-// Jobs that arrive while a tick runs join the next tick as soon as memory allows: the batch is
-// re-formed every tick (continuous batching), and state never leaves the device between ticks.
-// Each job's result equals running it alone with stc_map_steps (the batch is bit-identical per job).
+// Clients submit jobs (a host grid, stencil, reduction, boundary, step count); results stay on the device
+// until the client fetches them.
+//
+// Data path (GB300: the copy engines read and write pageable host memory through the host's page tables at
+// 90-200 GB/s, while a host memcpy runs at 15-20 GB/s): when the HBM budget allows, submit reserves the job's
+// two device parents and copies the caller's grid (dense or pitched) straight into the first one on the
+// server's upload stream; the call returns once the copy engine has consumed the host buffer, so the caller
+// may reuse it.  Only when the budget is exhausted is the input staged in pinned host memory, and the
+// scheduler uploads it once memory frees (jobs are admitted in arrival order).  fetch copies the result
+// straight into the caller's buffer and releases the last device parent.
+//
+// A scheduler thread runs two lanes:
+//   * solo lane (large grids, at least 2^21 cells): each job runs alone through stc_map_steps on the solo
+//     stream (so it gets the specialised paths: temporal blocking, packed Life, vector kernels), queued
+//     without waiting;
+//   * tick lane (smaller grids): every tick is one batched launch (batch.cu) that advances every active job by
+//     up to steps_per_tick steps, whatever its size, stencil or element type; the batch is re-formed every
+//     tick (continuous batching), and state never leaves the device between ticks.
+// The two lanes run concurrently on the GPU.  Each job's result equals running it alone with stc_map_steps
+// (the batch is bit-identical per job).
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -34,7 +46,7 @@ enum JobState { JOB_QUEUED = 0, JOB_ACTIVE = 1, JOB_DONE = 2, JOB_CANCELLED = 3,
 
 struct ServeJob {
     int64_t id = 0;
-    stc_grid grid{};            // logical grid description (dense column-major)
+    stc_grid grid{};            // device-side description (dense column-major; data unset)
     std::vector<int32_t> offs;
     std::vector<double> wts;
     stc_stencil st{};
@@ -42,13 +54,16 @@ struct ServeJob {
     stc_bc bc{};
     int64_t nsteps = 0, remaining = 0;
     size_t bytes = 0;           // one grid
-    void* h_in = nullptr;       // pinned copies
-    void* h_out = nullptr;
+    void* h_in = nullptr;       // pinned staging copy (only when the budget was exhausted at submit)
     void* d[2] = {nullptr, nullptr};
+    cudaEvent_t ev = nullptr;   // upload finished (stream order), then: solo run finished
     int cur = 0;                // parent holding the current state
+    bool solo = false;
+    bool uploaded = false;      // device parents hold the input (submitted straight, or staged and uploaded)
+    bool waited = false;        // the tick stream already waits on the upload
     int state = JOB_QUEUED;
     int status = STC_OK;
-    double t_submit = 0, t_done = 0;
+    double t_submit = 0;
 };
 
 }  // namespace stc
@@ -56,103 +71,218 @@ struct ServeJob {
 struct stc_server {
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<stc::ServeJob*> queue;
-    std::vector<stc::ServeJob*> active;
+    std::deque<stc::ServeJob*> queue;          // submitted, not yet activated (arrival order)
+    std::vector<stc::ServeJob*> active;        // tick lane
+    std::vector<stc::ServeJob*> solo_running;  // solo lane, queued on the solo stream
     std::map<int64_t, stc::ServeJob*> jobs;
     int64_t next_id = 1;
     size_t budget = 0, used = 0, peak = 0;
     int steps_per_tick = 16;
-    int64_t admitted = 0, finished = 0, ticks = 0;
+    int64_t solo_cells = 1ll << 21;
+    int64_t admitted = 0, finished = 0, ticks = 0, staged_waiting = 0;
     bool stop = false;
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // ticks
+    cudaStream_t solo = nullptr;     // solo runs
+    cudaStream_t up = nullptr;       // uploads
+    cudaStream_t down = nullptr;     // result downloads
     std::thread worker;
     stc::DeviceCtx* ctx = nullptr;
 };
 
 namespace stc {
 
-static void free_device(stc_server* s, ServeJob* j) {
-    for (int k = 0; k < 2; ++k)
-        if (j->d[k]) {
-            cudaFreeAsync(j->d[k], s->stream);
-            j->d[k] = nullptr;
-        }
+static void free_parent(cudaStream_t s, ServeJob* j, int k) {
+    if (j->d[k]) {
+        cudaFreeAsync(j->d[k], s);
+        j->d[k] = nullptr;
+    }
+}
+
+// Device parents for j, its input uploaded from `host` (rows of grid.size[0] elements at `pitch` bytes) on
+// the upload stream, and the event the lanes wait on.  The caller holds the reservation.
+static int upload_job(stc_server* s, ServeJob* j, const void* host, size_t pitch) {
+    const size_t row = (size_t)j->grid.size[0] * dtype_size(j->grid.dtype);
+    cudaError_t e = cudaMallocAsync(&j->d[0], j->bytes, s->up);
+    if (e == cudaSuccess) e = cudaMallocAsync(&j->d[1], j->bytes, s->up);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(j->d[0], row, host, pitch, row, (size_t)j->grid.size[1], cudaMemcpyHostToDevice, s->up);
+    if (e == cudaSuccess && !j->ev) e = cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(j->ev, s->up);
+    if (e != cudaSuccess) {
+        cuda_fail(e);
+        free_parent(s->up, j, 0);
+        free_parent(s->up, j, 1);
+        return STC_ERR_CUDA;
+    }
+    j->uploaded = true;
+    return STC_OK;
+}
+
+static void fail_job(stc_server* s, ServeJob* j, int status) {
+    j->state = JOB_FAILED;
+    j->status = status;
+    s->cv_done.notify_all();
+}
+
+// Queue a solo job's whole run on the solo stream (after its upload).
+static int start_solo(stc_server* s, ServeJob* j) {
+    cudaError_t e = cudaStreamWaitEvent(s->solo, j->ev, 0);
+    if (e != cudaSuccess) return cuda_fail(e);
+    stc_grid a = j->grid, b = j->grid;
+    a.data = j->d[0];
+    b.data = j->d[1];
+    int32_t src_is_b = 0;
+    void* prof = prof_begin(s->solo);
+    int rc = stc_map_steps(&a, &b, &j->st, &j->op, &j->bc, j->nsteps, &src_is_b, s->solo, STC_ASYNC);
+    prof_end(prof, s->solo, "serve_solo", 0.0, (double)j->grid.size[0] * j->grid.size[1] * j->nsteps);
+    if (rc) return rc;
+    j->cur = src_is_b ? 1 : 0;
+    if ((e = cudaEventRecord(j->ev, s->solo)) != cudaSuccess) return cuda_fail(e);
+    return STC_OK;
+}
+
+// A job's run ended: keep only the parent holding the result (released by fetch).
+static void finish_job(stc_server* s, ServeJob* j, cudaStream_t st) {
+    free_parent(st, j, 1 - j->cur);
+    s->used -= j->bytes;
+    if (j->state == JOB_ACTIVE) {
+        j->state = JOB_DONE;
+        ++s->finished;
+    } else {
+        free_parent(st, j, j->cur);   // cancelled: nothing to fetch
+        s->used -= j->bytes;
+    }
 }
 
 static void serve_loop(stc_server* s) {
     cudaSetDevice(s->device);
     stc_batch tick;
     while (true) {
-        std::vector<ServeJob*> to_copy;
+        std::vector<ServeJob*> to_upload, to_start;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv_work.wait_for(lk, std::chrono::milliseconds(2),
-                                [&] { return s->stop || !s->queue.empty() || !s->active.empty(); });
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(1), [&] {
+                return s->stop || !s->queue.empty() || !s->active.empty() || !s->solo_running.empty();
+            });
             if (s->stop) break;
-            // admission in arrival order while the budget allows
+            // activation in arrival order; staged inputs wait for the budget
             while (!s->queue.empty()) {
                 ServeJob* j = s->queue.front();
-                if (j->state == JOB_CANCELLED) { s->queue.pop_front(); continue; }
-                const size_t need = 2 * j->bytes;
-                if (need > s->budget) {
+                if (j->state == JOB_CANCELLED) {
                     s->queue.pop_front();
-                    j->state = JOB_FAILED;
-                    j->status = STC_ERR_BUDGET;
+                    if (j->uploaded) {
+                        free_parent(s->up, j, 0);
+                        free_parent(s->up, j, 1);
+                        s->used -= 2 * j->bytes;
+                    } else {
+                        --s->staged_waiting;
+                    }
                     s->cv_done.notify_all();
                     continue;
                 }
-                if (s->used + need > s->budget) break;
+                if (!j->uploaded) {
+                    const size_t need = 2 * j->bytes;
+                    if (s->used + need > s->budget) break;
+                    s->used += need;
+                    s->peak = std::max(s->peak, s->used);
+                    --s->staged_waiting;
+                    to_upload.push_back(j);
+                }
                 s->queue.pop_front();
-                s->used += need;
-                s->peak = std::max(s->peak, s->used);
                 ++s->admitted;
-                to_copy.push_back(j);
+                to_start.push_back(j);
             }
         }
-        // device state for newly admitted jobs (outside the lock)
-        for (ServeJob* j : to_copy) {
-            cudaError_t e = cudaMallocAsync(&j->d[0], j->bytes, s->stream);
-            if (e == cudaSuccess) e = cudaMallocAsync(&j->d[1], j->bytes, s->stream);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(j->d[0], j->h_in, j->bytes, cudaMemcpyHostToDevice, s->stream);
-            std::lock_guard<std::mutex> lk(s->mu);
-            if (e != cudaSuccess) {
-                cuda_fail(e);
-                free_device(s, j);
+        for (ServeJob* j : to_upload) {
+            const int rc = upload_job(s, j, j->h_in, (size_t)j->grid.size[0] * dtype_size(j->grid.dtype));
+            if (rc) {
+                std::lock_guard<std::mutex> lk(s->mu);
                 s->used -= 2 * j->bytes;
-                j->state = JOB_FAILED;
-                j->status = STC_ERR_CUDA;
-                s->cv_done.notify_all();
-                continue;
+                fail_job(s, j, rc);
             }
-            if (j->state == JOB_CANCELLED) {   // cancelled while its memory was being set up
-                free_device(s, j);
-                s->used -= 2 * j->bytes;
-                s->cv_done.notify_all();
-                continue;
-            }
+        }
+        for (ServeJob* j : to_start) {
+            if (j->state == JOB_FAILED) continue;
             j->state = JOB_ACTIVE;
-            j->cur = 0;
-            s->active.push_back(j);
+            if (j->solo) {
+                const int rc = start_solo(s, j);
+                std::lock_guard<std::mutex> lk(s->mu);
+                if (rc) {
+                    // the run may be partly queued: release the memory after the stream drains it
+                    free_parent(s->solo, j, 0);
+                    free_parent(s->solo, j, 1);
+                    s->used -= 2 * j->bytes;
+                    fail_job(s, j, rc);
+                } else {
+                    s->solo_running.push_back(j);
+                }
+            } else {
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->active.push_back(j);
+            }
         }
+        // solo lane: retire finished runs
+        {
+            std::vector<ServeJob*> running;
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                running = s->solo_running;
+            }
+            std::vector<ServeJob*> done;
+            for (ServeJob* j : running) {
+                const cudaError_t q = cudaEventQuery(j->ev);
+                if (q == cudaErrorNotReady) continue;
+                done.push_back(j);
+                if (q != cudaSuccess) j->status = cuda_fail(q);
+            }
+            if (!done.empty()) {
+                // a kernel's bounded wait or inexact conversion is reported on the solo stream's slot
+                const int st = take_status(status_slot(s->ctx, s->solo));
+                std::lock_guard<std::mutex> lk(s->mu);
+                for (ServeJob* j : done) {
+                    s->solo_running.erase(std::find(s->solo_running.begin(), s->solo_running.end(), j));
+                    if (j->status == STC_OK && st != STC_OK) j->status = st;
+                    if (j->status != STC_OK) {
+                        free_parent(s->solo, j, 0);
+                        free_parent(s->solo, j, 1);
+                        s->used -= 2 * j->bytes;
+                        fail_job(s, j, j->status);
+                    } else {
+                        finish_job(s, j, s->solo);
+                    }
+                }
+                s->cv_done.notify_all();
+            }
+        }
+        // tick lane
         std::vector<ServeJob*> act;
+        bool solo_busy = false;
         {
             std::lock_guard<std::mutex> lk(s->mu);
             act = s->active;
+            solo_busy = !s->solo_running.empty();
         }
-        if (act.empty()) continue;
-        // one tick: every active job advances by up to steps_per_tick steps
+        if (act.empty()) {
+            if (solo_busy) std::this_thread::sleep_for(std::chrono::microseconds(50));   // poll, not spin
+            continue;
+        }
         tick.specs.clear();
         std::vector<int64_t> chunk(act.size());
         int rc = STC_OK;
-        for (size_t i = 0; i < act.size(); ++i) {
+        for (size_t i = 0; i < act.size() && !rc; ++i) {
             ServeJob* j = act[i];
+            if (!j->waited) {
+                cudaError_t e = cudaStreamWaitEvent(s->stream, j->ev, 0);
+                if (e != cudaSuccess) rc = cuda_fail(e);
+                j->waited = true;
+            }
             chunk[i] = std::min<int64_t>(j->remaining, s->steps_per_tick);
             stc_grid a = j->grid, b = j->grid;
             a.data = j->d[j->cur];
             b.data = j->d[1 - j->cur];
             const int r = stc_batch_add(&tick, &a, &b, &j->st, &j->op, &j->bc, chunk[i]);
-            if (r < 0) { rc = r; break; }
+            if (r < 0) rc = r;
         }
         if (!rc) rc = batch_build(&tick, false, s->stream, s->ctx, false);
         if (!rc) {
@@ -163,11 +293,8 @@ static void serve_loop(stc_server* s) {
         if (!rc) {
             cudaError_t e = cudaStreamSynchronize(s->stream);
             if (e != cudaSuccess) rc = cuda_fail(e);
-            else
-                rc = take_status(tick.slot);
+            else rc = take_status(tick.slot);
         }
-        // retire finished jobs
-        std::vector<ServeJob*> done;
         {
             std::lock_guard<std::mutex> lk(s->mu);
             ++s->ticks;
@@ -175,39 +302,27 @@ static void serve_loop(stc_server* s) {
             for (size_t i = 0; i < act.size(); ++i) {
                 ServeJob* j = act[i];
                 if (rc) {
-                    j->state = JOB_FAILED;
-                    j->status = rc;
-                    done.push_back(j);
+                    free_parent(s->stream, j, 0);
+                    free_parent(s->stream, j, 1);
+                    s->used -= 2 * j->bytes;
+                    fail_job(s, j, rc);
                     continue;
                 }
                 if (tick.result_in_b[i]) j->cur = 1 - j->cur;
                 j->remaining -= chunk[i];
-                if (j->remaining <= 0 || j->state == JOB_CANCELLED) done.push_back(j);
+                if (j->remaining <= 0 || j->state == JOB_CANCELLED) finish_job(s, j, s->stream);
                 else keep.push_back(j);
             }
             s->active = keep;
-        }
-        for (ServeJob* j : done) {
-            if (j->state != JOB_FAILED && j->state != JOB_CANCELLED)
-                cudaMemcpyAsync(j->h_out, j->d[j->cur], j->bytes, cudaMemcpyDeviceToHost, s->stream);
-            free_device(s, j);
-        }
-        if (!done.empty()) cudaStreamSynchronize(s->stream);
-        {
-            std::lock_guard<std::mutex> lk(s->mu);
-            const double t = now_s();
-            for (ServeJob* j : done) {
-                s->used -= 2 * j->bytes;
-                if (j->state == JOB_ACTIVE) {
-                    j->state = JOB_DONE;
-                    ++s->finished;
-                }
-                j->t_done = t;
-            }
-            if (!done.empty()) s->cv_done.notify_all();
+            s->cv_done.notify_all();
         }
     }
     batch_free(&tick);
+}
+
+static int64_t solo_threshold() {
+    const char* e = getenv("STC_SERVE_SOLO_CELLS");
+    return e ? atoll(e) : (1ll << 21);
 }
 
 }  // namespace stc
@@ -229,9 +344,15 @@ int stc_server_create(stc_server** out, double hbm_fraction, int32_t steps_per_t
     s->device = ctx->device;
     s->budget = (size_t)(hbm_fraction * (double)free_b);
     s->steps_per_tick = steps_per_tick;
-    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
-        delete s;
-        return cuda_fail(e);
+    s->solo_cells = solo_threshold();
+    cudaStream_t* st[4] = {&s->stream, &s->solo, &s->up, &s->down};
+    for (cudaStream_t* p : st) {
+        if ((e = cudaStreamCreateWithFlags(p, cudaStreamNonBlocking)) != cudaSuccess) {
+            for (cudaStream_t* q : st)
+                if (*q) cudaStreamDestroy(*q);
+            delete s;
+            return cuda_fail(e);
+        }
     }
     s->worker = std::thread(serve_loop, s);
     *out = s;
@@ -246,16 +367,20 @@ int stc_server_destroy(stc_server* s) {
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
-    cudaStreamSynchronize(s->stream);
+    cudaStream_t st[4] = {s->stream, s->solo, s->up, s->down};
+    for (cudaStream_t q : st) cudaStreamSynchronize(q);
     for (auto& kv : s->jobs) {
         ServeJob* j = kv.second;
-        free_device(s, j);
+        free_parent(s->up, j, 0);
+        free_parent(s->up, j, 1);
         if (j->h_in) cudaFreeHost(j->h_in);
-        if (j->h_out) cudaFreeHost(j->h_out);
+        if (j->ev) cudaEventDestroy(j->ev);
         delete j;
     }
-    cudaStreamSynchronize(s->stream);
-    cudaStreamDestroy(s->stream);
+    for (cudaStream_t q : st) {
+        cudaStreamSynchronize(q);
+        cudaStreamDestroy(q);
+    }
     delete s;
     return STC_OK;
 }
@@ -263,20 +388,25 @@ int stc_server_destroy(stc_server* s) {
 int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
     if (!s || !job || !out_id || job->nsteps < 0) return STC_ERR_INVALID;
     const stc_grid& g = job->grid;
-    if (g.ndims != 2 || !g.data || g.size[0] < 1 || g.size[1] < 1 || g.stride[0] != 1 || g.stride[1] != g.size[0])
+    // the host grid: column-major, rows of size[0] elements at a pitch of stride[1] elements
+    if (g.ndims != 2 || !g.data || g.size[0] < 1 || g.size[1] < 1 || g.stride[0] != 1 || g.stride[1] < g.size[0])
         return STC_ERR_INVALID;
     if (job->bc.padding != STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
+    const size_t es = (size_t)dtype_size(g.dtype);
     // validate with the batch rules on placeholder device pointers
     stc_batch probe;
     stc_grid a = g, b = g;
+    a.stride[1] = b.stride[1] = g.size[0];
     // (disjoint placeholders: the batch rules reject a dest that shares memory with its source)
-    const uintptr_t span = (uintptr_t)(g.size[0] * g.size[1]) * (uintptr_t)dtype_size(g.dtype);
+    const uintptr_t span = (uintptr_t)(g.size[0] * g.size[1]) * (uintptr_t)es;
     a.data = (void*)(uintptr_t)0x100;
     b.data = (void*)((uintptr_t)0x200 + span);
     int rc = stc_batch_add(&probe, &a, &b, &job->stencil, &job->op, &job->bc, job->nsteps);
     if (rc < 0) return rc;
     ServeJob* j = new ServeJob();
     j->grid = g;
+    j->grid.stride[1] = g.size[0];
+    j->grid.data = nullptr;
     j->offs.assign(job->stencil.offsets, job->stencil.offsets + job->stencil.len * job->stencil.ndims);
     if (job->stencil.weights) j->wts.assign(job->stencil.weights, job->stencil.weights + job->stencil.len);
     j->st = job->stencil;
@@ -285,26 +415,58 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
     j->op = job->op;
     j->bc = job->bc;
     j->nsteps = j->remaining = job->nsteps;
-    j->bytes = (size_t)g.size[0] * g.size[1] * dtype_size(g.dtype);
-    cudaError_t e = cudaMallocHost(&j->h_in, j->bytes);
-    if (e == cudaSuccess) e = cudaMallocHost(&j->h_out, j->bytes);
-    if (e != cudaSuccess) {
-        if (j->h_in) cudaFreeHost(j->h_in);
-        delete j;
-        return cuda_fail(e);
-    }
-    std::memcpy(j->h_in, g.data, j->bytes);
-    j->grid.data = nullptr;
+    j->bytes = (size_t)g.size[0] * g.size[1] * es;
+    // Large grids run alone (specialised paths), except cellular automata whose rows pack into words: their
+    // persistent kernel needs every SM to itself, so they stay in the tick lane.
+    const bool packs = job->op.code == STC_OP_LIFE && g.size[0] % 32 == 0;
+    j->solo = (int64_t)g.size[0] * g.size[1] >= s->solo_cells && !packs;
     j->t_submit = now_s();
+    const size_t pitch = (size_t)g.stride[1] * es;
+    bool direct = false;
+    if (j->nsteps > 0) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (2 * j->bytes > s->budget) {
+            // can never be admitted: registered as failed, so poll and fetch report STC_ERR_BUDGET
+            j->state = JOB_FAILED;
+            j->status = STC_ERR_BUDGET;
+            j->id = s->next_id++;
+            s->jobs[j->id] = j;
+            *out_id = j->id;
+            return STC_OK;
+        }
+        // straight to the device while the budget allows and no staged job waits ahead of this one
+        if (s->staged_waiting == 0 && s->used + 2 * j->bytes <= s->budget) {
+            s->used += 2 * j->bytes;
+            s->peak = std::max(s->peak, s->used);
+            direct = true;
+        }
+    }
+    if (direct) {
+        if ((rc = upload_job(s, j, g.data, pitch))) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->used -= 2 * j->bytes;
+            direct = false;
+        }
+    }
+    if (!direct) {
+        // staged: a pinned copy, uploaded when the budget allows (also the nsteps == 0 result)
+        cudaError_t e = cudaMallocHost(&j->h_in, j->bytes);
+        if (e != cudaSuccess) {
+            delete j;
+            return cuda_fail(e);
+        }
+        const size_t row = (size_t)g.size[0] * es;
+        for (int64_t y = 0; y < g.size[1]; ++y)
+            std::memcpy((char*)j->h_in + y * row, (const char*)g.data + y * pitch, row);
+    }
     {
         std::lock_guard<std::mutex> lk(s->mu);
         j->id = s->next_id++;
         if (j->nsteps == 0) {
-            std::memcpy(j->h_out, j->h_in, j->bytes);
             j->state = JOB_DONE;
-            j->t_done = j->t_submit;
             ++s->finished;
         } else {
+            if (!direct) ++s->staged_waiting;
             s->queue.push_back(j);
         }
         s->jobs[j->id] = j;
@@ -340,12 +502,30 @@ int stc_server_fetch(stc_server* s, int64_t id, void* out, size_t out_bytes, dou
         if (out && out_bytes < j->bytes) return STC_ERR_SIZE_MISMATCH;
         s->jobs.erase(it);
     }
-    if (out) std::memcpy(out, j->h_out, j->bytes);
-    if (out_latency_s) *out_latency_s = j->t_done - j->t_submit;
-    cudaFreeHost(j->h_in);
-    cudaFreeHost(j->h_out);
+    int rc = STC_OK;
+    const void* src = j->d[j->cur];
+    if (out) {
+        if (src) {
+            // the result parent, straight into the caller's buffer
+            // (a finished job's lane has completed: ticks synchronise before retiring, solo runs are
+            // retired once their event completed)
+            cudaError_t e = cudaMemcpyAsync(out, src, j->bytes, cudaMemcpyDeviceToHost, s->down);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->down);
+            if (e != cudaSuccess) rc = cuda_fail(e);
+        } else if (j->h_in) {
+            std::memcpy(out, j->h_in, j->bytes);   // nsteps == 0: the input
+        }
+    }
+    if (out_latency_s) *out_latency_s = now_s() - j->t_submit;
+    if (src) {
+        free_parent(s->down, j, j->cur);
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->used -= j->bytes;
+    }
+    if (j->h_in) cudaFreeHost(j->h_in);
+    if (j->ev) cudaEventDestroy(j->ev);
     delete j;
-    return STC_OK;
+    return rc;
 }
 
 int stc_server_cancel(stc_server* s, int64_t id) {
@@ -362,10 +542,9 @@ int stc_server_drain(stc_server* s, double timeout_s) {
     if (!s) return STC_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
-    while (!(s->queue.empty() && s->active.empty())) {
-        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout &&
-            !(s->queue.empty() && s->active.empty()))
-            return STC_ERR_TIMEOUT;
+    auto idle = [&] { return s->queue.empty() && s->active.empty() && s->solo_running.empty(); };
+    while (!idle()) {
+        if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !idle()) return STC_ERR_TIMEOUT;
     }
     return STC_OK;
 }

@@ -29,7 +29,11 @@ class Server:
         """Queue `steps` iterations of mapstencil_(f, ·) on a copy of `grid` (2D, Julia axis order).
         `code` overrides the element type (A.BF16 for bfloat16 bit patterns held as uint16)."""
         red = as_reduction(f)
-        a = np.asfortranarray(grid)
+        a = np.asarray(grid)
+        # a column-major view (axis 0 contiguous, e.g. a corner of a larger Fortran array) is sent as is:
+        # the server copies its rows straight from this memory; anything else is made column-major first
+        if a.ndim != 2 or a.strides[0] != a.itemsize or a.strides[1] % a.itemsize or a.strides[1] < a.shape[0] * a.itemsize:
+            a = np.asfortranarray(a)
         code = A.numpy_dtype_code(a.dtype) if code is None else code
         job = A.JobDesc()
         job.grid = A.grid_from_numpy(a, code)

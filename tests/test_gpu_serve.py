@@ -104,3 +104,21 @@ def test_invalid_job_rejected_at_submit(cuda, st):
             srv.submit(np.zeros((2, 40), np.float32), st.Window(3), st.mean, st.Wrap(), 3)   # radius >= axis
         with pytest.raises(NotImplementedError):
             srv.submit(np.zeros((40, 40), np.float64), st.Window(1), st.mean, st.Wrap(), 3)  # f64 not batched
+
+
+def test_solo_lane_and_pitched_inputs(cuda, st, abi):
+    """Grids of at least 2^21 cells run alone on the solo stream beside the ticks; inputs given as corners of a
+    larger column-major array are copied from their pitched rows; every result equals the job run alone."""
+    rng = np.random.default_rng(5)
+    pool = np.asfortranarray(rng.random((1600, 1500), dtype=np.float32))
+    jobs = [(pool[:1500, :1450], st.Window(1), st.mean, st.Wrap(), 9),        # solo, pitched
+            (pool[:1450, :1500], st.VonNeumann(1), st.Diffusion(0.1), st.Remove(0.0), 13),   # solo, pitched
+            (pool[:300, :200], st.Circle(3), st.mean, st.Wrap(), 20),         # tick lane, pitched
+            (np.asfortranarray(pool[:257, :129]), st.Cross(2), st.sum, st.Remove(0.0), 7)]
+    with st.Server(hbm_fraction=0.5, steps_per_tick=4) as srv:
+        ids = [srv.submit(a, hood, red, bnd, steps) for a, hood, red, bnd, steps in jobs]
+        srv.drain(120.0)
+        for i, (a, hood, red, bnd, steps) in zip(ids, jobs):
+            got, _ = srv.fetch(i)
+            want = _alone(st, abi, np.asfortranarray(a), None, hood, red, bnd, steps)
+            assert np.array_equal(got, want)
