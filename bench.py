@@ -672,7 +672,7 @@ def cfg_blocked2d(args):
     st = entry.load_package()
     from stencils_gb300 import _lib
     rng = np.random.Generator(np.random.PCG64(6))
-    steps, side = 100, 8192
+    steps, side = 100, (args.side or 8192)
     a = np.asfortranarray(rng.random((side, side), dtype=np.float32))
     d = st.to_device(a)
     cells = a.size
@@ -1016,7 +1016,7 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="the headline line only")
     ap.add_argument("--workload", default="life", choices=["life"] + sorted(WORKLOADS),
                     help="life (the headline line, with every configuration under `configs`) or one configuration")
-    ap.add_argument("--side", type=int, default=0, help="diffusion: grid side (default 512)")
+    ap.add_argument("--side", type=int, default=0, help="diffusion: grid side (default 512); blocked2d: grid side (default 8192)")
     ap.add_argument("--serve-jobs", type=int, default=1000)
     ap.add_argument("--serve-rates", default="100,300,1000,3000,5000")
     ap.add_argument("--serve-tick", type=int, default=32)

@@ -284,8 +284,8 @@ STC_API int stc_mass(const stc_grid* g, int32_t radius, const stc_bc* bc, double
  * keeps the packed copies in a fixed device array that is part of the library image (4 MiB, held on
  * every GPU that loads the library until the process exits) instead of allocating them.  The caller
  * still owns and passes both parents.  Accepts only what that path runs: a 2D Moore(1) LIFE rule,
- * UInt8/Bool/Int32/Int64 grids whose width is a multiple of 32 cells and at most 16384 cells,
- * Wrap or Remove(0), at most 4096*4096 logical cells (larger grids return STC_ERR_TOO_LARGE, other
+ * UInt8/Bool/Int32/Int64 grids whose width is 32 to 16382 cells (rows pack into at most 512 words),
+ * Wrap or Remove(0), at most 4096*4096 packed cells (larger grids return STC_ERR_TOO_LARGE, other
  * inputs STC_ERR_UNSUPPORTED).  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) and keeps it for the life of the process, so make that first call before
  * any stream capture; a device reset (cudaDeviceReset) after it is not supported.  All calls share
@@ -347,10 +347,18 @@ STC_API int stc_server_destroy(stc_server* s);
 STC_API int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id);
 /* Non-blocking: 1 if the job finished (its result can be fetched), 0 if not, or a status. */
 STC_API int stc_server_poll(stc_server* s, int64_t id);
-/* Copy a finished job's result into host memory `out` (logical size, the job's dtype, column-major)
- * and release its device state.  Returns STC_ERR_BUSY if it has not finished. */
+/* A job counts as finished once its result is in pinned host memory (copied from the device as its run
+ * ends).  stc_server_fetch copies that result into host memory `out` (logical size, the job's dtype,
+ * column-major, dense) and forgets the job; *out_latency_s = submit to result in host memory.  Returns
+ * STC_ERR_BUSY if it has not finished. */
 STC_API int stc_server_fetch(stc_server* s, int64_t id, void* out, size_t out_bytes,
                      double* out_latency_s);
+/* The same without a copy: *out_host receives the pinned buffer holding the result (*out_bytes bytes,
+ * column-major, dense); the caller owns it until stc_server_release_buffer returns it to the library's
+ * process-wide pool (it may outlive the server). */
+STC_API int stc_server_fetch_buffer(stc_server* s, int64_t id, void** out_host, size_t* out_bytes,
+                     double* out_latency_s);
+STC_API int stc_server_release_buffer(void* host);
 STC_API int stc_server_cancel(stc_server* s, int64_t id);
 /* Block until every submitted job finished or timeout_s passed (STC_ERR_TIMEOUT). */
 STC_API int stc_server_drain(stc_server* s, double timeout_s);

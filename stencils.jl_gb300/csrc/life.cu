@@ -133,13 +133,21 @@ struct LifeLane {
     bool active;
     bool edge_warp;
     bool gl, gr;   // writes the left ghost (w == W-1) / the right ghost (w == 0)
+    bool rl, rr;   // ragged rows: replaces the left neighbour of cell 0 / the right neighbour of cell n0-1
     int w;
+    int w1, j1;    // ragged rows: cell n0-1 is bit j1 of word w1
     int s, strips;
     float inv_strips;
 };
 
+// Rows of n0 cells with 32 W > n0 (column-interleaved, so cells n0 .. 32W-1 are spare bits): W is
+// chosen so at least two bits are spare, and the two layout neighbours that fall on spare bits are
+// replaced when read: the right neighbour of cell n0-1 (bit j1 of its right word) by cell 0, and the
+// left neighbour of cell 0 (bit 0 of its left word) by cell n0-1 — under Remove(0) by a dead cell.
+__host__ __device__ __forceinline__ int life_words(int64_t n0) { return n0 % 32 == 0 ? (int)(n0 / 32) : (int)((n0 + 2 + 31) / 32); }
+
 template <int WPL>
-__device__ __forceinline__ LifeLane life_lane(int W) {
+__device__ __forceinline__ LifeLane life_lane(int W, int n0) {
     LifeLane L;
     if constexpr (WPL > 0) {
         // one row strip per warp
@@ -148,8 +156,8 @@ __device__ __forceinline__ LifeLane life_lane(int W) {
         L.s = threadIdx.x >> 5;
         L.active = true;
         L.edge_warp = false;
-        L.gl = L.gr = false;
-        L.w = 0;
+        L.gl = L.gr = L.rl = L.rr = false;
+        L.w = L.w1 = L.j1 = 0;
         return L;
     }
     L.strips = max(1, (int)blockDim.x / W);
@@ -161,7 +169,12 @@ __device__ __forceinline__ LifeLane life_lane(int W) {
     L.w = c == 0 ? W - 1 : c - 1;
     L.gl = L.active && L.w == W - 1;
     L.gr = L.active && L.w == 0;
-    L.edge_warp = __any_sync(0xffffffffu, L.gl || L.gr);
+    const bool ragged = n0 != 32 * W;
+    L.w1 = (n0 - 1) % W;
+    L.j1 = (n0 - 1) / W;
+    L.rl = ragged && L.gr;
+    L.rr = ragged && L.active && L.w == L.w1;
+    L.edge_warp = __any_sync(0xffffffffu, L.gl || L.gr || L.rr);
     return L;
 }
 
@@ -175,7 +188,15 @@ __device__ __forceinline__ void life_strip(const LifeLane& L, const uint32_t* __
     const int P = life_pitch<0>(W);
     const uint32_t* ps = src + (ra - 1) * P + L.w;   // left word of row ra-1; centre at +1, right at +2
     uint32_t* pd = dst + ra * P + 1 + L.w;
-    auto load = [&](int q) -> RowV { return row_v(ps[q * P], ps[q * P + 1], ps[q * P + 2]); };
+    auto load = [&](int q) -> RowV {
+        uint32_t l = ps[q * P], c = ps[q * P + 1], r = ps[q * P + 2];
+        if (EDGE) {
+            const uint32_t* row = ps + q * P - L.w + 1;   // word 0 of this row
+            if (L.rr) r = (r & ~(1u << L.j1)) | (WRAP ? (row[0] & 1u) << L.j1 : 0u);
+            if (L.rl) l = (l & ~1u) | (WRAP ? (row[L.w1] >> L.j1) & 1u : 0u);
+        }
+        return row_v(l, c, r);
+    };
     auto emit = [&](int q, const RowV& u, const RowV& m, const RowV& d) {
         const uint32_t nx = next_state<CONWAY>(u, m, d, birth, survive);
         pd[q * P] = nx;
@@ -352,6 +373,7 @@ __device__ __forceinline__ void load_band(const uint32_t* in, uint32_t* buf, uin
 struct LifeParams {
     const uint32_t* in;
     uint32_t* out;
+    int n0;         // cells per row
     int W;          // words per row
     int n1;         // rows
     int TB;         // band rows written back per CTA
@@ -377,7 +399,7 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_block_kernel(const LifeP
     __syncthreads();
     int lo_lim, hi_lim;
     band_limits<WRAP>(rows, y0 - k, p.n1, &lo_lim, &hi_lim);
-    const LifeLane lane = life_lane<WPL>(W);
+    const LifeLane lane = life_lane<WPL>(W, p.n0);
     uint32_t* fin = life_gens<CONWAY, WRAP, WT, WPL>(lane, buf0, buf1, rows, W, k, lo_lim, hi_lim, p.birth, p.survive);
     for (int i = threadIdx.x; i < p.TB * W; i += blockDim.x) {
         const int r = i / W, w = i - r * W;
@@ -404,7 +426,7 @@ struct LifeCoopParams {
     uint32_t* last;       // generation n
     uint64_t* xbuf;       // [2 slots][grid][2 (first, last rows)][k][W] tagged words, zero before launch
     int* status;
-    int W, n1, k;
+    int n0, W, n1, k;   // cells per row, words per row, rows, ghost depth
     int64_t nsteps;
     uint32_t birth, survive;
 };
@@ -452,7 +474,7 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCo
     const bool has_up = WRAP || b > 0, has_dn = WRAP || b < G - 1;
     const int slab = k * W;                            // one published row block
     const int64_t nmain = p.nsteps - 1;                // generations before the last one
-    const LifeLane lane = life_lane<WPL>(W);
+    const LifeLane lane = life_lane<WPL>(W, p.n0);
     int64_t gen = 0;
     for (int step = 0;; ++step) {
         const bool final = gen >= nmain;
@@ -522,6 +544,8 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCo
 
 // Row width specialised at compile time (128 words = 4096 cells); other widths use the run-time path.
 constexpr int kLifeWT = 128;
+// The warp-row split runs rows of exactly kLifeWT words with no spare bits; everything else the column split.
+static bool life_split_rows(int64_t n0, int W) { return W == kLifeWT && n0 == 32ll * W; }
 
 // launch one k-generation pass (both entry points use this)
 template <bool C, bool WR, int WT>
@@ -542,12 +566,12 @@ static cudaError_t life_launch_w(const LifeParams& lp, bool conway, int grid, si
 }
 
 static cudaError_t life_launch(const LifeParams& lp, bool conway, int grid, size_t smem, cudaStream_t s) {
-    return lp.W == kLifeWT ? life_launch_w<kLifeWT>(lp, conway, grid, smem, s) : life_launch_w<0>(lp, conway, grid, smem, s);
+    return life_split_rows(lp.n0, lp.W) ? life_launch_w<kLifeWT>(lp, conway, grid, smem, s) : life_launch_w<0>(lp, conway, grid, smem, s);
 }
 
 // bytes of shared memory for a band pair of `rows` rows of W words (the split the kernels use for W)
-static size_t life_band_smem(int rows, int W) {
-    const int P = W == kLifeWT ? life_pitch<life_wpl<kLifeWT>()>(W) : life_pitch<0>(W);
+static size_t life_band_smem(int rows, int W, int64_t n0) {
+    const int P = life_split_rows(n0, W) ? life_pitch<life_wpl<kLifeWT>()>(W) : life_pitch<0>(W);
     return (size_t)2 * rows * P * sizeof(uint32_t);
 }
 
@@ -557,7 +581,7 @@ struct PackParams {
     int64_t org;        // parent offset of logical (0, 0)
     int64_t sy;         // parent row stride (elements)
     int dt;
-    int W, n1;
+    int n0, W, n1;      // cells per row, words per row, rows
     uint32_t* P;
 };
 
@@ -572,7 +596,7 @@ __global__ void life_pack_kernel(const PackParams p) {
         const T* cell = base + p.org + (int64_t)y * p.sy + w;
         bool nz[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) nz[j] = cell[(int64_t)j * p.W] != (T)0;   // all loads before use
+        for (int j = 0; j < 32; ++j) nz[j] = j * p.W + w < p.n0 && cell[(int64_t)j * p.W] != (T)0;   // spare bits 0
         uint32_t v = 0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) v |= (uint32_t)nz[j] << j;
@@ -589,17 +613,19 @@ __global__ void life_unpack_kernel(const PackParams p) {
         T* cell = base + p.org + (int64_t)y * p.sy + w;
         const uint32_t v = p.P[gi];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) cell[(int64_t)j * p.W] = (T)((v >> j) & 1u);
+        for (int j = 0; j < 32; ++j)
+            if (j * p.W + w < p.n0) cell[(int64_t)j * p.W] = (T)((v >> j) & 1u);
     }
 }
 
-static int launch_pack(bool pack, const stc_grid* g, int64_t org, int W, int n1, uint32_t* P, cudaStream_t s,
-                       int num_sms) {
+static int launch_pack(bool pack, const stc_grid* g, int64_t org, int64_t n0, int W, int n1, uint32_t* P,
+                       cudaStream_t s, int num_sms) {
     PackParams p{};
     p.base = g->data;
     p.org = org;
     p.sy = g->stride[1];
     p.dt = g->dtype;
+    p.n0 = (int)n0;
     p.W = W;
     p.n1 = n1;
     p.P = P;
@@ -636,11 +662,11 @@ static bool is_moore1_2d(const stc_stencil* st) {
 // Band rows and generations per launch for a grid of W words x n1 rows: one band per SM when the
 // grid is tall enough (the kernel is ALU-bound, so every SM should hold one band), at most 16
 // generations per launch, and whatever fits in shared memory.
-void life_plan(int W, int n1, int64_t steps_left, int smem_cap, int num_sms, int* TB, int* k) {
+void life_plan(int W, int64_t n0, int n1, int64_t steps_left, int smem_cap, int num_sms, int* TB, int* k) {
     int kk = (int)std::min<int64_t>(steps_left, 16);
     int tb = std::max(8, (n1 + num_sms - 1) / num_sms);
-    while (kk > 1 && (int64_t)life_band_smem(tb + 2 * kk, W) > smem_cap) --kk;
-    while (tb > 1 && (int64_t)life_band_smem(tb + 2 * kk, W) > smem_cap) --tb;
+    while (kk > 1 && (int64_t)life_band_smem(tb + 2 * kk, W, n0) > smem_cap) --kk;
+    while (tb > 1 && (int64_t)life_band_smem(tb + 2 * kk, W, n0) > smem_cap) --tb;
     *TB = tb;
     *k = kk;
 }
@@ -692,7 +718,7 @@ static cudaError_t coop_dispatch_w(bool query, bool conway, bool wrap, const Lif
 
 static cudaError_t coop_dispatch(bool query, bool conway, bool wrap, const LifeCoopParams& cp, int grid, size_t smem,
                                  cudaStream_t s, int num_sms, bool* fits) {
-    return cp.W == kLifeWT ? coop_dispatch_w<kLifeWT>(query, conway, wrap, cp, grid, smem, s, num_sms, fits)
+    return life_split_rows(cp.n0, cp.W) ? coop_dispatch_w<kLifeWT>(query, conway, wrap, cp, grid, smem, s, num_sms, fits)
                            : coop_dispatch_w<0>(query, conway, wrap, cp, grid, smem, s, num_sms, fits);
 }
 
@@ -708,7 +734,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
         cudaGetLastError();
         return STC_OK;
     }
-    const int W = (int)(n0 / 32);
+    const int W = life_words(n0);
     int k = (int)std::min<int64_t>(life_coop_depth(n1, ctx->num_sms), std::max<int64_t>(1, nsteps - 1));
     int G = (int)std::min<int64_t>(ctx->num_sms, n1 / k);
     if (G < 1) {
@@ -716,12 +742,13 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
         k = (int)n1;
     }
     const int TBmax = (int)((n1 + G - 1) / G);
-    const size_t smem = life_band_smem(TBmax + 2 * k, W);
+    const size_t smem = life_band_smem(TBmax + 2 * k, W, n0);
     if ((int64_t)smem > ctx->max_smem_optin - 1024) return STC_OK;
 
     const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
     bool fits = false;
     LifeCoopParams q{};
+    q.n0 = (int)n0;
     q.W = W;
     cudaError_t e = coop_dispatch(true, conway, wrap, q, G, smem, stream, ctx->num_sms, &fits);
     if (e != cudaSuccess) return cuda_fail(e);
@@ -737,7 +764,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
     uint32_t* P0 = (uint32_t*)(X + xwords);
     uint32_t* P1 = P0 + words;
     const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
-    int rc = launch_pack(true, a, org_a, W, (int)n1, P0, stream, ctx->num_sms);
+    int rc = launch_pack(true, a, org_a, n0, W, (int)n1, P0, stream, ctx->num_sms);
     if (!rc) rc = cuda_fail(cudaMemsetAsync(X, 0, xwords * sizeof(uint64_t), stream));   // no stale tags
     if (rc) { cudaFreeAsync(mem, stream); return rc; }
     LifeCoopParams cp{};
@@ -746,6 +773,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
     cp.last = P1;
     cp.xbuf = X;
     cp.status = status_slot(ctx, stream).dev;
+    cp.n0 = (int)n0;
     cp.W = W;
     cp.n1 = (int)n1;
     cp.k = k;
@@ -765,8 +793,8 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
     const bool res_in_b = (nsteps & 1) != 0;
     const stc_grid* res = res_in_b ? b : a;
     const stc_grid* prev = res_in_b ? a : b;
-    rc = launch_pack(false, res, res_in_b ? org_b : org_a, W, (int)n1, P1, stream, ctx->num_sms);
-    if (!rc && nsteps > 1) rc = launch_pack(false, prev, res_in_b ? org_a : org_b, W, (int)n1, P0, stream, ctx->num_sms);
+    rc = launch_pack(false, res, res_in_b ? org_b : org_a, n0, W, (int)n1, P1, stream, ctx->num_sms);
+    if (!rc && nsteps > 1) rc = launch_pack(false, prev, res_in_b ? org_a : org_b, n0, W, (int)n1, P0, stream, ctx->num_sms);
     cudaFreeAsync(mem, stream);
     if (rc) return rc;
     *src_is_b = res_in_b ? 1 : 0;
@@ -784,14 +812,14 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     const bool remove0 = bc->boundary == STC_REMOVE && bc->padval_int == 0;
     if (!wrap && !remove0) return STC_OK;   // Reflect / Use / nonzero padval take the per-step kernel
     const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
-    if (n0 < 32 || n0 % 32 != 0 || n1 < 1 || n0 / 32 > 512 || n1 > (1 << 30)) return STC_OK;
+    if (n0 < 32 || n1 < 1 || life_words(n0) > 512 || n1 > (1 << 30)) return STC_OK;
     int rc = life_coop_steps(a, b, op, halo, wrap, n0, n1, nsteps, src_is_b, stream, ctx, done);
     if (rc || *done) return rc;
-    const int W = (int)(n0 / 32);
+    const int W = life_words(n0);
     const int smem_cap = ctx->max_smem_optin - 1024;
     int TB, k;
-    life_plan(W, (int)n1, nsteps, smem_cap, ctx->num_sms, &TB, &k);
-    if ((int64_t)life_band_smem(TB + 2 * k, W) > smem_cap) return STC_OK;
+    life_plan(W, n0, (int)n1, nsteps, smem_cap, ctx->num_sms, &TB, &k);
+    if ((int64_t)life_band_smem(TB + 2 * k, W, n0) > smem_cap) return STC_OK;
 
     const size_t words = (size_t)W * n1;
     uint32_t* P = nullptr;
@@ -799,10 +827,11 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     if (e != cudaSuccess) return cuda_fail(e);
     uint32_t* Pbuf[2] = {P, P + words};
     const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
-    rc = launch_pack(true, a, org_a, W, (int)n1, Pbuf[0], stream, ctx->num_sms);
+    rc = launch_pack(true, a, org_a, n0, W, (int)n1, Pbuf[0], stream, ctx->num_sms);
     if (rc) { cudaFreeAsync(P, stream); return rc; }
 
     LifeParams lp{};
+    lp.n0 = (int)n0;
     lp.W = W;
     lp.n1 = (int)n1;
     lp.wrap = wrap;
@@ -814,12 +843,12 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     while (left > 0) {
         // the last generation runs alone so both packed buffers hold the last two states
         const int64_t budget = left > 1 ? left - 1 : 1;
-        life_plan(W, (int)n1, budget, smem_cap, ctx->num_sms, &TB, &k);
+        life_plan(W, n0, (int)n1, budget, smem_cap, ctx->num_sms, &TB, &k);
         lp.in = Pbuf[cur];
         lp.out = Pbuf[1 - cur];
         lp.TB = TB;
         lp.k = k;
-        const size_t smem = life_band_smem(TB + 2 * k, W);
+        const size_t smem = life_band_smem(TB + 2 * k, W, n0);
         const int grid = (int)((n1 + TB - 1) / TB);
         void* prof = prof_begin(stream);
         e = life_launch(lp, conway, grid, smem, stream);
@@ -833,8 +862,8 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     const bool res_in_b = (nsteps & 1) != 0;
     const stc_grid* res = res_in_b ? b : a;
     const stc_grid* prev = res_in_b ? a : b;
-    rc = launch_pack(false, res, res_in_b ? org_b : org_a, W, (int)n1, Pbuf[cur], stream, ctx->num_sms);
-    if (!rc && nsteps > 1) rc = launch_pack(false, prev, res_in_b ? org_a : org_b, W, (int)n1, Pbuf[1 - cur], stream, ctx->num_sms);
+    rc = launch_pack(false, res, res_in_b ? org_b : org_a, n0, W, (int)n1, Pbuf[cur], stream, ctx->num_sms);
+    if (!rc && nsteps > 1) rc = launch_pack(false, prev, res_in_b ? org_a : org_b, n0, W, (int)n1, Pbuf[1 - cur], stream, ctx->num_sms);
     cudaFreeAsync(P, stream);
     if (rc) return rc;
     *src_is_b = res_in_b ? 1 : 0;
@@ -879,13 +908,14 @@ static void noalloc_pack(bool pack, const PackParams& p, int blocks, cudaStream_
     else life_unpack_kernel<T><<<blocks, 256, 0, s>>>(p);
 }
 
-static int noalloc_pack_launch(bool pack, const stc_grid* g, int64_t org, int W, int n1, uint32_t* P,
+static int noalloc_pack_launch(bool pack, const stc_grid* g, int64_t org, int64_t n0, int W, int n1, uint32_t* P,
                                cudaStream_t s, int num_sms) {
     PackParams p{};
     p.base = g->data;
     p.org = org;
     p.sy = g->stride[1];
     p.dt = g->dtype;
+    p.n0 = (int)n0;
     p.W = W;
     p.n1 = n1;
     p.P = P;
@@ -920,11 +950,11 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     const bool remove0 = bc->boundary == STC_REMOVE && bc->padval_int == 0;
     if (!wrap && !remove0) return STC_ERR_UNSUPPORTED;
     const int64_t n0 = a->size[0] - (halo ? 2 : 0), n1 = a->size[1] - (halo ? 2 : 0);
-    if (n0 < 32 || n0 % 32 != 0 || n1 < 1) return STC_ERR_UNSUPPORTED;
+    if (n0 < 32 || n1 < 1) return STC_ERR_UNSUPPORTED;
     // life_block_kernel gives each thread one packed column of a strip, so rows wider than the CTA
     // (kNoAllocMaxWords words) would leave columns uncomputed
-    if (n0 / 32 > kNoAllocMaxWords || n0 / 32 > life_threads((int)(n0 / 32))) return STC_ERR_UNSUPPORTED;
-    if (n0 * n1 > kNoAllocMaxCells) return STC_ERR_TOO_LARGE;
+    if (life_words(n0) > kNoAllocMaxWords || life_words(n0) > life_threads(life_words(n0))) return STC_ERR_UNSUPPORTED;
+    if ((int64_t)life_words(n0) * 32 * n1 > kNoAllocMaxCells) return STC_ERR_TOO_LARGE;   // packed words fit
     if (nsteps > 0 && a->data == b->data) return STC_ERR_INVALID;
     if (nsteps == 0) {
         if (out_src_is_b) *out_src_is_b = 0;
@@ -940,15 +970,16 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     uint32_t* P = nullptr;
     if ((rc = noalloc_scratch(dev, &P))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
-    const int W = (int)(n0 / 32);
+    const int W = life_words(n0);
     const int smem_cap = smem_optin - 1024;
     int TB, k;
-    life_plan(W, (int)n1, nsteps, smem_cap, num_sms, &TB, &k);
-    if ((int64_t)life_band_smem(TB + 2 * k, W) > smem_cap) return STC_ERR_UNSUPPORTED;
+    life_plan(W, n0, (int)n1, nsteps, smem_cap, num_sms, &TB, &k);
+    if ((int64_t)life_band_smem(TB + 2 * k, W, n0) > smem_cap) return STC_ERR_UNSUPPORTED;
     uint32_t* Pbuf[2] = {P, P + kNoAllocWords};
     const int64_t org_a = halo ? 1 + a->stride[1] : 0, org_b = halo ? 1 + b->stride[1] : 0;
-    if ((rc = noalloc_pack_launch(true, a, org_a, W, (int)n1, Pbuf[0], s, num_sms))) return rc;
+    if ((rc = noalloc_pack_launch(true, a, org_a, n0, W, (int)n1, Pbuf[0], s, num_sms))) return rc;
     LifeParams lp{};
+    lp.n0 = (int)n0;
     lp.W = W;
     lp.n1 = (int)n1;
     lp.wrap = wrap;
@@ -959,12 +990,12 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     int64_t left = nsteps;
     while (left > 0) {
         const int64_t budget = left > 1 ? left - 1 : 1;
-        life_plan(W, (int)n1, budget, smem_cap, num_sms, &TB, &k);
+        life_plan(W, n0, (int)n1, budget, smem_cap, num_sms, &TB, &k);
         lp.in = Pbuf[cur];
         lp.out = Pbuf[1 - cur];
         lp.TB = TB;
         lp.k = k;
-        const size_t smem = life_band_smem(TB + 2 * k, W);
+        const size_t smem = life_band_smem(TB + 2 * k, W, n0);
         const int grid = (int)((n1 + TB - 1) / TB);
         if ((e = life_launch(lp, conway, grid, smem, s)) != cudaSuccess) return cuda_fail(e);
         cur = 1 - cur;
@@ -973,9 +1004,9 @@ extern "C" int stc_life_steps_noalloc(const stc_grid* a, const stc_grid* b, cons
     const bool res_in_b = (nsteps & 1) != 0;
     const stc_grid* res = res_in_b ? b : a;
     const stc_grid* prev = res_in_b ? a : b;
-    if ((rc = noalloc_pack_launch(false, res, res_in_b ? org_b : org_a, W, (int)n1, Pbuf[cur], s, num_sms))) return rc;
+    if ((rc = noalloc_pack_launch(false, res, res_in_b ? org_b : org_a, n0, W, (int)n1, Pbuf[cur], s, num_sms))) return rc;
     if (nsteps > 1 &&
-        (rc = noalloc_pack_launch(false, prev, res_in_b ? org_a : org_b, W, (int)n1, Pbuf[1 - cur], s, num_sms)))
+        (rc = noalloc_pack_launch(false, prev, res_in_b ? org_a : org_b, n0, W, (int)n1, Pbuf[1 - cur], s, num_sms)))
         return rc;
     if (out_src_is_b) *out_src_is_b = res_in_b ? 1 : 0;
     return cuda_fail(cudaStreamSynchronize(s));

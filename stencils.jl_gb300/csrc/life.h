@@ -5,8 +5,8 @@
 
 namespace stc {
 
-// If (stencil, op, boundary, grid) is a 2D Moore(1) outer-totalistic rule on a byte grid whose
-// width packs into 32-bit words, run as many of `nsteps` as possible on a packed copy and unpack
+// If (stencil, op, boundary, grid) is a 2D Moore(1) outer-totalistic rule on a UInt8/Bool/Int32/Int64
+// grid at least 32 cells wide, run as many of `nsteps` as possible on a packed copy and unpack
 // the result into the parent the reference's switch() would leave it in.  *done reports how many
 // steps ran (0 when the fast path does not apply); *src_is_b is updated accordingly.
 int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, const stc_op* op,

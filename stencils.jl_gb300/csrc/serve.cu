@@ -9,8 +9,11 @@
 // two device parents and copies the caller's grid (dense or pitched) straight into the first one on the
 // server's upload stream; the call returns once the copy engine has consumed the host buffer, so the caller
 // may reuse it.  Only when the budget is exhausted is the input staged in pinned host memory, and the
-// scheduler uploads it once memory frees (jobs are admitted in arrival order).  fetch copies the result
-// straight into the caller's buffer and releases the last device parent.
+// scheduler uploads it once memory frees (jobs are admitted in arrival order).  When a job's run ends its
+// result is copied on the download stream into a pinned buffer from a process-wide pool (copy engines
+// write pinned memory at ~180 GB/s, a freshly allocated pageable buffer at ~17 GB/s), overlapped with the
+// work still running; the job is finished once that copy has landed.  stc_server_fetch_buffer hands the
+// pinned buffer itself to the caller (no copy), stc_server_fetch copies it into the caller's memory.
 //
 // A scheduler thread runs two lanes:
 //   * solo lane (large grids, at least 2^21 cells): each job runs alone through stc_map_steps on the solo
@@ -46,15 +49,17 @@ enum JobState { JOB_QUEUED = 0, JOB_ACTIVE = 1, JOB_DONE = 2, JOB_CANCELLED = 3,
 
 struct ServeJob {
     int64_t id = 0;
-    stc_grid grid{};            // device-side description (dense column-major; data unset)
+    stc_grid grid{};            // device-side description (column-major, rows at `pitch` bytes; data unset)
     std::vector<int32_t> offs;
     std::vector<double> wts;
     stc_stencil st{};
     stc_op op{};
     stc_bc bc{};
     int64_t nsteps = 0, remaining = 0;
-    size_t bytes = 0;           // one grid
+    size_t bytes = 0;           // one device parent (pitched)
+    size_t row = 0, pitch = 0;  // bytes of a row's cells; bytes between device rows (a multiple of 128)
     void* h_in = nullptr;       // pinned staging copy (only when the budget was exhausted at submit)
+    void* h_out = nullptr;      // pinned result (from the pool)
     void* d[2] = {nullptr, nullptr};
     cudaEvent_t ev = nullptr;   // upload finished (stream order), then: solo run finished
     int cur = 0;                // parent holding the current state
@@ -63,7 +68,7 @@ struct ServeJob {
     bool waited = false;        // the tick stream already waits on the upload
     int state = JOB_QUEUED;
     int status = STC_OK;
-    double t_submit = 0;
+    double t_submit = 0, t_done = 0;
 };
 
 }  // namespace stc
@@ -74,6 +79,7 @@ struct stc_server {
     std::deque<stc::ServeJob*> queue;          // submitted, not yet activated (arrival order)
     std::vector<stc::ServeJob*> active;        // tick lane
     std::vector<stc::ServeJob*> solo_running;  // solo lane, queued on the solo stream
+    std::vector<stc::ServeJob*> copying;       // runs ended, results being copied to pinned host memory
     std::map<int64_t, stc::ServeJob*> jobs;
     int64_t next_id = 1;
     size_t budget = 0, used = 0, peak = 0;
@@ -92,6 +98,68 @@ struct stc_server {
 
 namespace stc {
 
+// ---------------------------------------------------------------------------- pinned host buffers
+// Process-wide pool (buffers handed to callers may outlive the server that filled them), by power-of-two
+// size class from 64 KiB; at most kPoolKeep bytes stay pooled, the rest is freed on release.
+constexpr size_t kPoolKeep = 16ull << 30;
+static std::mutex g_pin_mu;
+static std::map<size_t, std::vector<void*>> g_pin_free;
+static std::map<void*, size_t> g_pin_size;
+static size_t g_pin_pooled = 0;
+
+static size_t pin_class(size_t bytes) {
+    size_t c = 64 << 10;
+    while (c < bytes) c <<= 1;
+    return c;
+}
+
+static void* pinned_get(size_t bytes) {
+    const size_t c = pin_class(bytes);
+    {
+        std::lock_guard<std::mutex> g(g_pin_mu);
+        auto it = g_pin_free.find(c);
+        if (it != g_pin_free.end() && !it->second.empty()) {
+            void* p = it->second.back();
+            it->second.pop_back();
+            g_pin_pooled -= c;
+            return p;
+        }
+    }
+    void* p = nullptr;
+    if (cudaMallocHost(&p, c) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> g(g_pin_mu);
+    g_pin_size[p] = c;
+    return p;
+}
+
+static bool pinned_put(void* p) {
+    size_t c = 0;
+    {
+        std::lock_guard<std::mutex> g(g_pin_mu);
+        auto it = g_pin_size.find(p);
+        if (it == g_pin_size.end()) return false;
+        c = it->second;
+        if (g_pin_pooled + c <= kPoolKeep) {
+            g_pin_free[c].push_back(p);
+            g_pin_pooled += c;
+            return true;
+        }
+        g_pin_size.erase(it);
+    }
+    cudaFreeHost(p);
+    return true;
+}
+
+static void drop_job(ServeJob* j) {
+    if (j->h_in) pinned_put(j->h_in);
+    if (j->h_out) pinned_put(j->h_out);
+    if (j->ev) cudaEventDestroy(j->ev);
+    delete j;
+}
+
 static void free_parent(cudaStream_t s, ServeJob* j, int k) {
     if (j->d[k]) {
         cudaFreeAsync(j->d[k], s);
@@ -102,11 +170,11 @@ static void free_parent(cudaStream_t s, ServeJob* j, int k) {
 // Device parents for j, its input uploaded from `host` (rows of grid.size[0] elements at `pitch` bytes) on
 // the upload stream, and the event the lanes wait on.  The caller holds the reservation.
 static int upload_job(stc_server* s, ServeJob* j, const void* host, size_t pitch) {
-    const size_t row = (size_t)j->grid.size[0] * dtype_size(j->grid.dtype);
     cudaError_t e = cudaMallocAsync(&j->d[0], j->bytes, s->up);
     if (e == cudaSuccess) e = cudaMallocAsync(&j->d[1], j->bytes, s->up);
     if (e == cudaSuccess)
-        e = cudaMemcpy2DAsync(j->d[0], row, host, pitch, row, (size_t)j->grid.size[1], cudaMemcpyHostToDevice, s->up);
+        e = cudaMemcpy2DAsync(j->d[0], j->pitch, host, pitch, j->row, (size_t)j->grid.size[1], cudaMemcpyHostToDevice,
+                              s->up);
     if (e == cudaSuccess && !j->ev) e = cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventRecord(j->ev, s->up);
     if (e != cudaSuccess) {
@@ -142,17 +210,28 @@ static int start_solo(stc_server* s, ServeJob* j) {
     return STC_OK;
 }
 
-// A job's run ended: keep only the parent holding the result (released by fetch).
+// A job's run ended on lane stream `st`: copy its result into a pinned buffer on the download stream (after
+// `st`), release both device parents behind the copy, and wait for the copy in the `copying` list.  Holds mu.
 static void finish_job(stc_server* s, ServeJob* j, cudaStream_t st) {
-    free_parent(st, j, 1 - j->cur);
-    s->used -= j->bytes;
     if (j->state == JOB_ACTIVE) {
-        j->state = JOB_DONE;
-        ++s->finished;
-    } else {
-        free_parent(st, j, j->cur);   // cancelled: nothing to fetch
-        s->used -= j->bytes;
+        const size_t host_bytes = j->row * (size_t)j->grid.size[1];
+        j->h_out = pinned_get(host_bytes);
+        cudaError_t e = j->h_out ? cudaEventRecord(j->ev, st) : cudaErrorMemoryAllocation;
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->down, j->ev, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(j->h_out, j->row, j->d[j->cur], j->pitch, j->row, (size_t)j->grid.size[1],
+                                  cudaMemcpyDeviceToHost, s->down);
+        if (e == cudaSuccess) e = cudaEventRecord(j->ev, s->down);
+        if (e == cudaSuccess) {
+            s->copying.push_back(j);
+        } else {
+            cuda_fail(e);
+            fail_job(s, j, STC_ERR_CUDA);
+        }
     }
+    free_parent(s->down, j, 0);
+    free_parent(s->down, j, 1);
+    s->used -= 2 * j->bytes;
 }
 
 static void serve_loop(stc_server* s) {
@@ -163,7 +242,8 @@ static void serve_loop(stc_server* s) {
         {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_work.wait_for(lk, std::chrono::milliseconds(1), [&] {
-                return s->stop || !s->queue.empty() || !s->active.empty() || !s->solo_running.empty();
+                return s->stop || !s->queue.empty() || !s->active.empty() || !s->solo_running.empty() ||
+                       !s->copying.empty();
             });
             if (s->stop) break;
             // activation in arrival order; staged inputs wait for the budget
@@ -195,7 +275,7 @@ static void serve_loop(stc_server* s) {
             }
         }
         for (ServeJob* j : to_upload) {
-            const int rc = upload_job(s, j, j->h_in, (size_t)j->grid.size[0] * dtype_size(j->grid.dtype));
+            const int rc = upload_job(s, j, j->h_in, j->row);
             if (rc) {
                 std::lock_guard<std::mutex> lk(s->mu);
                 s->used -= 2 * j->bytes;
@@ -255,16 +335,41 @@ static void serve_loop(stc_server* s) {
                 s->cv_done.notify_all();
             }
         }
+        // results that reached host memory
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (!s->copying.empty()) {
+                std::vector<ServeJob*> still;
+                bool any = false;
+                for (ServeJob* j : s->copying) {
+                    const cudaError_t q = cudaEventQuery(j->ev);
+                    if (q == cudaErrorNotReady) {
+                        still.push_back(j);
+                        continue;
+                    }
+                    any = true;
+                    if (q != cudaSuccess) {
+                        fail_job(s, j, cuda_fail(q));
+                    } else if (j->state == JOB_ACTIVE) {
+                        j->state = JOB_DONE;
+                        j->t_done = now_s();
+                        ++s->finished;
+                    }
+                }
+                s->copying = still;
+                if (any) s->cv_done.notify_all();
+            }
+        }
         // tick lane
         std::vector<ServeJob*> act;
-        bool solo_busy = false;
+        bool busy = false;
         {
             std::lock_guard<std::mutex> lk(s->mu);
             act = s->active;
-            solo_busy = !s->solo_running.empty();
+            busy = !s->solo_running.empty() || !s->copying.empty();
         }
         if (act.empty()) {
-            if (solo_busy) std::this_thread::sleep_for(std::chrono::microseconds(50));   // poll, not spin
+            if (busy) std::this_thread::sleep_for(std::chrono::microseconds(50));   // poll, not spin
             continue;
         }
         tick.specs.clear();
@@ -373,9 +478,7 @@ int stc_server_destroy(stc_server* s) {
         ServeJob* j = kv.second;
         free_parent(s->up, j, 0);
         free_parent(s->up, j, 1);
-        if (j->h_in) cudaFreeHost(j->h_in);
-        if (j->ev) cudaEventDestroy(j->ev);
-        delete j;
+        drop_job(j);
     }
     for (cudaStream_t q : st) {
         cudaStreamSynchronize(q);
@@ -393,20 +496,24 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
         return STC_ERR_INVALID;
     if (job->bc.padding != STC_CONDITIONAL) return STC_ERR_UNSUPPORTED;
     const size_t es = (size_t)dtype_size(g.dtype);
+    // device rows on 128-byte boundaries, so every grid can be staged by TMA
+    const size_t row = (size_t)g.size[0] * es, dpitch = (row + 127) / 128 * 128;
     // validate with the batch rules on placeholder device pointers
     stc_batch probe;
     stc_grid a = g, b = g;
-    a.stride[1] = b.stride[1] = g.size[0];
+    a.stride[1] = b.stride[1] = (int64_t)(dpitch / es);
     // (disjoint placeholders: the batch rules reject a dest that shares memory with its source)
-    const uintptr_t span = (uintptr_t)(g.size[0] * g.size[1]) * (uintptr_t)es;
+    const uintptr_t span = (uintptr_t)(dpitch * g.size[1]);
     a.data = (void*)(uintptr_t)0x100;
     b.data = (void*)((uintptr_t)0x200 + span);
     int rc = stc_batch_add(&probe, &a, &b, &job->stencil, &job->op, &job->bc, job->nsteps);
     if (rc < 0) return rc;
     ServeJob* j = new ServeJob();
     j->grid = g;
-    j->grid.stride[1] = g.size[0];
+    j->grid.stride[1] = (int64_t)(dpitch / es);
     j->grid.data = nullptr;
+    j->row = row;
+    j->pitch = dpitch;
     j->offs.assign(job->stencil.offsets, job->stencil.offsets + job->stencil.len * job->stencil.ndims);
     if (job->stencil.weights) j->wts.assign(job->stencil.weights, job->stencil.weights + job->stencil.len);
     j->st = job->stencil;
@@ -415,7 +522,7 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
     j->op = job->op;
     j->bc = job->bc;
     j->nsteps = j->remaining = job->nsteps;
-    j->bytes = (size_t)g.size[0] * g.size[1] * es;
+    j->bytes = dpitch * (size_t)g.size[1];
     // Large grids run alone (specialised paths), except cellular automata whose rows pack into words: their
     // persistent kernel needs every SM to itself, so they stay in the tick lane.
     const bool packs = job->op.code == STC_OP_LIFE && g.size[0] % 32 == 0;
@@ -450,12 +557,11 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
     }
     if (!direct) {
         // staged: a pinned copy, uploaded when the budget allows (also the nsteps == 0 result)
-        cudaError_t e = cudaMallocHost(&j->h_in, j->bytes);
-        if (e != cudaSuccess) {
+        j->h_in = pinned_get(row * (size_t)g.size[1]);
+        if (!j->h_in) {
             delete j;
-            return cuda_fail(e);
+            return STC_ERR_CUDA;
         }
-        const size_t row = (size_t)g.size[0] * es;
         for (int64_t y = 0; y < g.size[1]; ++y)
             std::memcpy((char*)j->h_in + y * row, (const char*)g.data + y * pitch, row);
     }
@@ -464,6 +570,7 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
         j->id = s->next_id++;
         if (j->nsteps == 0) {
             j->state = JOB_DONE;
+            j->t_done = j->t_submit;
             ++s->finished;
         } else {
             if (!direct) ++s->staged_waiting;
@@ -488,44 +595,52 @@ int stc_server_poll(stc_server* s, int64_t id) {
     return 0;
 }
 
+// Take a finished job out of the server: its pinned result (the staged input when nsteps == 0).
+static int take_result(stc_server* s, int64_t id, size_t out_bytes, bool check_size, ServeJob** out_job) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(id);
+    if (it == s->jobs.end()) return STC_ERR_INVALID;
+    ServeJob* j = it->second;
+    if (j->state == JOB_FAILED) return j->status;
+    if (j->state == JOB_CANCELLED) return STC_ERR_CANCELLED;
+    if (j->state != JOB_DONE) return STC_ERR_BUSY;
+    if (check_size && out_bytes < j->row * (size_t)j->grid.size[1]) return STC_ERR_SIZE_MISMATCH;
+    s->jobs.erase(it);
+    if (!j->h_out) {   // nsteps == 0
+        j->h_out = j->h_in;
+        j->h_in = nullptr;
+    }
+    *out_job = j;
+    return STC_OK;
+}
+
 int stc_server_fetch(stc_server* s, int64_t id, void* out, size_t out_bytes, double* out_latency_s) {
     if (!s) return STC_ERR_INVALID;
     ServeJob* j = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        auto it = s->jobs.find(id);
-        if (it == s->jobs.end()) return STC_ERR_INVALID;
-        j = it->second;
-        if (j->state == JOB_FAILED) return j->status;
-        if (j->state == JOB_CANCELLED) return STC_ERR_CANCELLED;
-        if (j->state != JOB_DONE) return STC_ERR_BUSY;
-        if (out && out_bytes < j->bytes) return STC_ERR_SIZE_MISMATCH;
-        s->jobs.erase(it);
-    }
-    int rc = STC_OK;
-    const void* src = j->d[j->cur];
-    if (out) {
-        if (src) {
-            // the result parent, straight into the caller's buffer
-            // (a finished job's lane has completed: ticks synchronise before retiring, solo runs are
-            // retired once their event completed)
-            cudaError_t e = cudaMemcpyAsync(out, src, j->bytes, cudaMemcpyDeviceToHost, s->down);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(s->down);
-            if (e != cudaSuccess) rc = cuda_fail(e);
-        } else if (j->h_in) {
-            std::memcpy(out, j->h_in, j->bytes);   // nsteps == 0: the input
-        }
-    }
-    if (out_latency_s) *out_latency_s = now_s() - j->t_submit;
-    if (src) {
-        free_parent(s->down, j, j->cur);
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->used -= j->bytes;
-    }
-    if (j->h_in) cudaFreeHost(j->h_in);
-    if (j->ev) cudaEventDestroy(j->ev);
-    delete j;
-    return rc;
+    int rc = take_result(s, id, out_bytes, out != nullptr, &j);
+    if (rc) return rc;
+    if (out) std::memcpy(out, j->h_out, j->row * (size_t)j->grid.size[1]);
+    if (out_latency_s) *out_latency_s = j->t_done - j->t_submit;
+    drop_job(j);
+    return STC_OK;
+}
+
+int stc_server_fetch_buffer(stc_server* s, int64_t id, void** out_host, size_t* out_bytes, double* out_latency_s) {
+    if (!s || !out_host) return STC_ERR_INVALID;
+    ServeJob* j = nullptr;
+    int rc = take_result(s, id, 0, false, &j);
+    if (rc) return rc;
+    *out_host = j->h_out;
+    if (out_bytes) *out_bytes = j->row * (size_t)j->grid.size[1];
+    if (out_latency_s) *out_latency_s = j->t_done - j->t_submit;
+    j->h_out = nullptr;   // the caller's until stc_server_release_buffer
+    drop_job(j);
+    return STC_OK;
+}
+
+int stc_server_release_buffer(void* host) {
+    if (!host) return STC_ERR_INVALID;
+    return pinned_put(host) ? STC_OK : STC_ERR_INVALID;
 }
 
 int stc_server_cancel(stc_server* s, int64_t id) {
@@ -542,7 +657,7 @@ int stc_server_drain(stc_server* s, double timeout_s) {
     if (!s) return STC_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
-    auto idle = [&] { return s->queue.empty() && s->active.empty() && s->solo_running.empty(); };
+    auto idle = [&] { return s->queue.empty() && s->active.empty() && s->solo_running.empty() && s->copying.empty(); };
     while (!idle()) {
         if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !idle()) return STC_ERR_TIMEOUT;
     }

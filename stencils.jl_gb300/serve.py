@@ -7,6 +7,7 @@ with its latency from submission.  Each result equals running the job alone.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -54,13 +55,18 @@ class Server:
         return rc == 1
 
     def fetch(self, job_id: int):
-        """(result array, latency in seconds); raises StencilError(BUSY) if not finished."""
+        """(result array, latency in seconds); raises StencilError(BUSY) if not finished.
+
+        The array is a view of the pinned host buffer the server copied the result into (no further copy);
+        the buffer returns to the library's pool when the array and its views are gone."""
         shape, dtype, code = self._meta[job_id]
-        out = np.empty(shape, dtype=dtype, order="F")
-        lat = C.c_double(0.0)
-        _lib.check(self._lib.stc_server_fetch(self._h, job_id, out.ctypes.data_as(C.c_void_p), out.nbytes,
-                                              C.byref(lat)), "stc_server_fetch")
+        ptr, nbytes, lat = C.c_void_p(), C.c_size_t(0), C.c_double(0.0)
+        _lib.check(self._lib.stc_server_fetch_buffer(self._h, job_id, C.byref(ptr), C.byref(nbytes), C.byref(lat)),
+                   "stc_server_fetch")
         del self._meta[job_id]
+        raw = (C.c_char * nbytes.value).from_address(ptr.value)
+        weakref.finalize(raw, self._lib.stc_server_release_buffer, C.c_void_p(ptr.value))
+        out = np.frombuffer(raw, dtype=dtype).reshape(shape, order="F")
         return out, lat.value
 
     def cancel(self, job_id: int):

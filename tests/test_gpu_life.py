@@ -103,12 +103,12 @@ def test_life_other_rule_and_small_grids(cuda, st, orc, abi):
 
 
 def test_life_fallback_shapes_still_exact(cuda, st, orc, abi):
-    """Widths that do not pack into words, Reflect and nonzero Remove take the per-generation kernel."""
+    """Rows shorter than 32 cells, Reflect and nonzero Remove take the per-generation kernel."""
     rng = np.random.default_rng(4)
-    for shape, bnd in (((100, 64), st.Wrap()), ((128, 64), st.Reflect()), ((128, 64), st.Remove(1))):
+    for shape, bnd in (((20, 64), st.Wrap()), ((128, 64), st.Reflect()), ((128, 64), st.Remove(1))):
         a = np.asfortranarray((rng.random(shape) < 0.4).astype(np.uint8))
         S2, kern = _gpu_run(st, st.to_device(a), st.life, bnd, st.Conditional(), 9)
-        assert "life_block" not in kern
+        assert "life_block" not in kern and "life_coop" not in kern
         res, _, _ = _oracle_steps(orc, abi, st, a, abi.U8, st.life, bnd, st.Conditional(), 9)
         assert np.array_equal(_logical(S2.source, st.Conditional(), st), res)
 
@@ -150,3 +150,23 @@ def test_queued_calls_equal_waiting_calls(cuda, st):
     a = st.to_host(S1.source)[1:-1, 1:-1]
     b = st.to_host(S2.source)[1:-1, 1:-1]
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("n0", [33, 62, 63, 100, 1000, 4094])
+@pytest.mark.parametrize("bname", ["wrap", "remove0"])
+def test_life_ragged_rows(cuda, st, orc, abi, n0, bname):
+    """Row lengths that are not a multiple of 32 take the packed path too (spare bits at the end of the
+    column-interleaved rows, the two neighbours that fall on them replaced when read), persistent and
+    multi-launch; both states bit-exact against the oracle, for B3/S23 and HighLife."""
+    rng = np.random.default_rng(n0 + len(bname))
+    n1 = 300 if n0 < 4000 else 160
+    a = np.asfortranarray((rng.random((n0, n1)) < 0.35).astype(np.uint8))
+    bnd = st.Wrap() if bname == "wrap" else st.Remove(0)
+    for rule in (st.life, st.LifeRule((3, 6), (2, 3))):
+        for steps in (1, 9, 40):
+            S2, kern = _gpu_run(st, st.to_device(a), rule, bnd, st.Conditional(), steps)
+            assert "life_coop" in kern or "life_block" in kern, kern
+            res, prev, _ = _oracle_steps(orc, abi, st, a, abi.U8, rule, bnd, st.Conditional(), steps)
+            assert np.array_equal(_logical(S2.source, st.Conditional(), st), res), (rule, steps)
+            if steps > 1:
+                assert np.array_equal(_logical(S2.dest, st.Conditional(), st), prev), (rule, steps)

@@ -63,7 +63,8 @@ def test_noalloc_matches_allocating_path_twice(cuda, lib, st, abi):
     import torch
     rng = np.random.default_rng(2024)
     cases = [((4096, 4096), st.Wrap(), st.Halo("out"), 100),
-             ((1024, 700), st.Remove(0), st.Conditional(), 37)]
+             ((1024, 700), st.Remove(0), st.Conditional(), 37),
+             ((1001, 300), st.Wrap(), st.Conditional(), 29)]      # rows with spare bits
     for shape, bnd, pad, steps in cases:            # two calls in a row, different grids
         a = np.asfortranarray((rng.random(shape) < 0.3).astype(np.uint8))
         _compare_pair(lib, abi, st, a, bnd, pad, steps, torch.uint8)
@@ -94,10 +95,10 @@ def test_noalloc_rejects_grids_beyond_its_scratch(cuda, lib, st, abi):
     b = st.colmajor_zeros((8192, 4096), torch.uint8)
     rc, _ = _run(lib, abi, st, "noalloc", a, b, st.Wrap(), st.Conditional(), 3)
     assert rc == -12   # STC_ERR_TOO_LARGE
-    odd = st.colmajor_zeros((100, 64), torch.uint8)
-    odd2 = st.colmajor_zeros((100, 64), torch.uint8)
-    rc, _ = _run(lib, abi, st, "noalloc", odd, odd2, st.Wrap(), st.Conditional(), 3)
-    assert rc == -4    # width not a multiple of 32: not this path
+    narrow = st.colmajor_zeros((20, 64), torch.uint8)
+    narrow2 = st.colmajor_zeros((20, 64), torch.uint8)
+    rc, _ = _run(lib, abi, st, "noalloc", narrow, narrow2, st.Wrap(), st.Conditional(), 3)
+    assert rc == -4    # rows shorter than 32 cells: not this path
     # 32768 x 512 holds exactly 4096^2 cells but its rows (1024 words) are wider than the CTA
     wide = st.colmajor_zeros((32768, 512), torch.uint8)
     wide2 = st.colmajor_zeros((32768, 512), torch.uint8)
