@@ -698,7 +698,13 @@ def cfg_blocked2d(args):
                 os.environ.pop("STC_TBLOCK", None)
             kname, k, roof = _hbm_roof(prof, _peaks())
             roof["note"] = ("algorithmic bytes: one Float32 read and one write per cell-step (a blocked pass "
-                            "moves them once per 4 steps, so its effective fraction can exceed 1)")
+                            "moves them once per 8 steps, so its effective fraction can exceed 1)")
+            e = _traffic().get(f"{kname}:{name}")
+            if e:
+                # the binding unit: instruction issue, from an ncu capture of this kernel
+                roof.update(_issue_frac(k["updates"] / (k["ms"] / 1e3), e["warp_inst_per_update"], {}))
+                roof["traffic_bytes_per_update"] = e["dram_bytes_per_update"]
+                roof["counters_source"] = e["source"]
             res[f"{name}_{mode}"] = {"value": cells * steps / t / 1e9, "s_total": t, "roofline": roof,
                                      "kernels": _kernels(prof)}
             del S
@@ -842,22 +848,21 @@ def cfg_serving(args):
         with st.Server(hbm_fraction=0.8, steps_per_tick=args.serve_tick) as srv:
             pending = {}
             t0 = time.perf_counter()
+            def collect(wait_s):
+                # the server's completion queue: only finished jobs are touched
+                for i in srv.ready(timeout_s=wait_s):
+                    srv.fetch(i)
+                    lat[i] = time.perf_counter() - t0 - pending.pop(i)
             for j, at in zip(jobs, arrivals):
                 while True:
                     now = time.perf_counter() - t0
-                    for i in [i for i in pending if srv.poll(i)]:
-                        srv.fetch(i)
-                        lat[i] = time.perf_counter() - t0 - pending.pop(i)
                     if now >= at:
                         break
-                    time.sleep(min(0.0005, at - now))
+                    collect(min(0.0005, at - now))
                 g, code, hood, red, bnd, steps = j
                 pending[srv.submit(g, hood, red, bnd, steps, code=code)] = at
             while pending:
-                for i in [i for i in pending if srv.poll(i)]:
-                    srv.fetch(i)
-                    lat[i] = time.perf_counter() - t0 - pending.pop(i)
-                time.sleep(0.0002)
+                collect(0.002)
             makespan = time.perf_counter() - t0
         served = np.array(list(lat.values()))
         # plain: one worker serves the arrivals in order, concurrently with their arrival

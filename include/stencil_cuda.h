@@ -284,11 +284,11 @@ STC_API int stc_mass(const stc_grid* g, int32_t radius, const stc_bc* bc, double
  * keeps the packed copies in a fixed device array that is part of the library image (4 MiB, held on
  * every GPU that loads the library until the process exits) instead of allocating them.  The caller
  * still owns and passes both parents.  Accepts only what that path runs: a 2D Moore(1) LIFE rule,
- * UInt8/Bool/Int32/Int64 grids whose width is 32 to 16382 cells (rows pack into at most 512 words),
+ * UInt8/Bool/Int32/Int64 grids whose rows are at least 32 cells and pack into at most 512 words (16384 cells),
  * Wrap or Remove(0), at most 4096*4096 packed cells (larger grids return STC_ERR_TOO_LARGE, other
  * inputs STC_ERR_UNSUPPORTED).  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and keeps it for the life of the process, so make that first call before
- * any stream capture; a device reset (cudaDeviceReset) after it is not supported.  All calls share
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; a device reset (cudaDeviceReset)
+ * after it is not supported.  All calls share
  * the one array and each call overwrites it: calls whose work overlaps on the GPU (other streams,
  * other host threads) race and must be serialised by the caller.  The call waits for its stream
  * before returning.  Same results and parent switching as stc_map_steps. */
@@ -359,6 +359,9 @@ STC_API int stc_server_fetch(stc_server* s, int64_t id, void* out, size_t out_by
 STC_API int stc_server_fetch_buffer(stc_server* s, int64_t id, void** out_host, size_t* out_bytes,
                      double* out_latency_s);
 STC_API int stc_server_release_buffer(void* host);
+/* Completion queue: up to max_ids ids of jobs that finished, failed or were cancelled since the last call
+ * (each reported once), waiting up to timeout_s for the first; *n_out = how many were written. */
+STC_API int stc_server_ready(stc_server* s, int64_t* ids, int32_t max_ids, double timeout_s, int32_t* n_out);
 STC_API int stc_server_cancel(stc_server* s, int64_t id);
 /* Block until every submitted job finished or timeout_s passed (STC_ERR_TIMEOUT). */
 STC_API int stc_server_drain(stc_server* s, double timeout_s);

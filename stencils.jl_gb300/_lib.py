@@ -79,6 +79,7 @@ def load(path: str | Path | None = None):
         "stc_server_fetch": ([vp, C.c_int64, vp, C.c_size_t, P(C.c_double)], C.c_int),
         "stc_server_fetch_buffer": ([vp, C.c_int64, P(vp), P(C.c_size_t), P(C.c_double)], C.c_int),
         "stc_server_release_buffer": ([vp], C.c_int),
+        "stc_server_ready": ([vp, P(C.c_int64), C.c_int32, C.c_double, P(C.c_int32)], C.c_int),
         "stc_server_cancel": ([vp, C.c_int64], C.c_int),
         "stc_server_drain": ([vp, C.c_double], C.c_int),
         "stc_server_stats": ([vp, P(C.c_int64), P(C.c_int64), P(C.c_int64), P(C.c_int64)], C.c_int),

@@ -17,8 +17,8 @@
 //
 // A scheduler thread runs two lanes:
 //   * solo lane (large grids, at least 2^21 cells): each job runs alone through stc_map_steps on the solo
-//     stream (so it gets the specialised paths: temporal blocking, packed Life, vector kernels), queued
-//     without waiting;
+//     stream (so it gets the specialised paths: temporal blocking, packed Life, vector kernels), at most
+//     three runs queued on the stream at a time;
 //   * tick lane (smaller grids): every tick is one batched launch (batch.cu) that advances every active job by
 //     up to steps_per_tick steps, whatever its size, stencil or element type; the batch is re-formed every
 //     tick (continuous batching), and state never leaves the device between ticks.
@@ -79,8 +79,10 @@ struct stc_server {
     std::deque<stc::ServeJob*> queue;          // submitted, not yet activated (arrival order)
     std::vector<stc::ServeJob*> active;        // tick lane
     std::vector<stc::ServeJob*> solo_running;  // solo lane, queued on the solo stream
+    std::deque<stc::ServeJob*> solo_waiting;   // solo lane, uploaded, not yet queued
     std::vector<stc::ServeJob*> copying;       // runs ended, results being copied to pinned host memory
     std::map<int64_t, stc::ServeJob*> jobs;
+    std::deque<int64_t> completed;             // ids that finished (or failed) and were not yet reported
     int64_t next_id = 1;
     size_t budget = 0, used = 0, peak = 0;
     int steps_per_tick = 16;
@@ -160,6 +162,8 @@ static void drop_job(ServeJob* j) {
     delete j;
 }
 
+constexpr int kSoloInFlight = 3;
+
 static void free_parent(cudaStream_t s, ServeJob* j, int k) {
     if (j->d[k]) {
         cudaFreeAsync(j->d[k], s);
@@ -190,6 +194,7 @@ static int upload_job(stc_server* s, ServeJob* j, const void* host, size_t pitch
 static void fail_job(stc_server* s, ServeJob* j, int status) {
     j->state = JOB_FAILED;
     j->status = status;
+    s->completed.push_back(j->id);
     s->cv_done.notify_all();
 }
 
@@ -228,6 +233,8 @@ static void finish_job(stc_server* s, ServeJob* j, cudaStream_t st) {
             cuda_fail(e);
             fail_job(s, j, STC_ERR_CUDA);
         }
+    } else {
+        s->completed.push_back(j->id);   // cancelled while running
     }
     free_parent(s->down, j, 0);
     free_parent(s->down, j, 1);
@@ -243,6 +250,7 @@ static void serve_loop(stc_server* s) {
             std::unique_lock<std::mutex> lk(s->mu);
             s->cv_work.wait_for(lk, std::chrono::milliseconds(1), [&] {
                 return s->stop || !s->queue.empty() || !s->active.empty() || !s->solo_running.empty() ||
+                       !s->solo_waiting.empty() ||
                        !s->copying.empty();
             });
             if (s->stop) break;
@@ -251,6 +259,7 @@ static void serve_loop(stc_server* s) {
                 ServeJob* j = s->queue.front();
                 if (j->state == JOB_CANCELLED) {
                     s->queue.pop_front();
+                    s->completed.push_back(j->id);
                     if (j->uploaded) {
                         free_parent(s->up, j, 0);
                         free_parent(s->up, j, 1);
@@ -286,20 +295,42 @@ static void serve_loop(stc_server* s) {
             if (j->state == JOB_FAILED) continue;
             j->state = JOB_ACTIVE;
             if (j->solo) {
-                const int rc = start_solo(s, j);
                 std::lock_guard<std::mutex> lk(s->mu);
-                if (rc) {
-                    // the run may be partly queued: release the memory after the stream drains it
-                    free_parent(s->solo, j, 0);
-                    free_parent(s->solo, j, 1);
-                    s->used -= 2 * j->bytes;
-                    fail_job(s, j, rc);
-                } else {
-                    s->solo_running.push_back(j);
-                }
+                s->solo_waiting.push_back(j);
             } else {
                 std::lock_guard<std::mutex> lk(s->mu);
                 s->active.push_back(j);
+            }
+        }
+        // solo lane: at most kSoloInFlight runs queued on the solo stream at a time, so that its launches
+        // never fill the stream's launch queue (a full queue blocks the launching thread, and with it the
+        // ticks and the retirements)
+        while (true) {
+            ServeJob* j = nullptr;
+            {
+                std::lock_guard<std::mutex> lk(s->mu);
+                if (s->solo_waiting.empty() || (int)s->solo_running.size() >= kSoloInFlight) break;
+                j = s->solo_waiting.front();
+                s->solo_waiting.pop_front();
+                if (j->state == JOB_CANCELLED) {
+                    free_parent(s->solo, j, 0);
+                    free_parent(s->solo, j, 1);
+                    s->used -= 2 * j->bytes;
+                    s->completed.push_back(j->id);
+                    s->cv_done.notify_all();
+                    continue;
+                }
+            }
+            const int rc = start_solo(s, j);
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (rc) {
+                // the run may be partly queued: release the memory after the stream drains it
+                free_parent(s->solo, j, 0);
+                free_parent(s->solo, j, 1);
+                s->used -= 2 * j->bytes;
+                fail_job(s, j, rc);
+            } else {
+                s->solo_running.push_back(j);
             }
         }
         // solo lane: retire finished runs
@@ -354,6 +385,7 @@ static void serve_loop(stc_server* s) {
                         j->state = JOB_DONE;
                         j->t_done = now_s();
                         ++s->finished;
+                        s->completed.push_back(j->id);
                     }
                 }
                 s->copying = still;
@@ -366,7 +398,7 @@ static void serve_loop(stc_server* s) {
         {
             std::lock_guard<std::mutex> lk(s->mu);
             act = s->active;
-            busy = !s->solo_running.empty() || !s->copying.empty();
+            busy = !s->solo_running.empty() || !s->solo_waiting.empty() || !s->copying.empty();
         }
         if (act.empty()) {
             if (busy) std::this_thread::sleep_for(std::chrono::microseconds(50));   // poll, not spin
@@ -538,6 +570,7 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
             j->status = STC_ERR_BUDGET;
             j->id = s->next_id++;
             s->jobs[j->id] = j;
+            s->completed.push_back(j->id);
             *out_id = j->id;
             return STC_OK;
         }
@@ -572,6 +605,7 @@ int stc_server_submit(stc_server* s, const stc_job* job, int64_t* out_id) {
             j->state = JOB_DONE;
             j->t_done = j->t_submit;
             ++s->finished;
+            s->completed.push_back(j->id);
         } else {
             if (!direct) ++s->staged_waiting;
             s->queue.push_back(j);
@@ -643,6 +677,20 @@ int stc_server_release_buffer(void* host) {
     return pinned_put(host) ? STC_OK : STC_ERR_INVALID;
 }
 
+int stc_server_ready(stc_server* s, int64_t* ids, int32_t max_ids, double timeout_s, int32_t* n_out) {
+    if (!s || !n_out || max_ids < 0 || (max_ids > 0 && !ids)) return STC_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (s->completed.empty() && timeout_s > 0)
+        s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] { return !s->completed.empty(); });
+    int32_t n = 0;
+    while (n < max_ids && !s->completed.empty()) {
+        ids[n++] = s->completed.front();
+        s->completed.pop_front();
+    }
+    *n_out = n;
+    return STC_OK;
+}
+
 int stc_server_cancel(stc_server* s, int64_t id) {
     if (!s) return STC_ERR_INVALID;
     std::lock_guard<std::mutex> lk(s->mu);
@@ -657,7 +705,10 @@ int stc_server_drain(stc_server* s, double timeout_s) {
     if (!s) return STC_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
     const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
-    auto idle = [&] { return s->queue.empty() && s->active.empty() && s->solo_running.empty() && s->copying.empty(); };
+    auto idle = [&] {
+        return s->queue.empty() && s->active.empty() && s->solo_running.empty() && s->solo_waiting.empty() &&
+               s->copying.empty();
+    };
     while (!idle()) {
         if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && !idle()) return STC_ERR_TIMEOUT;
     }

@@ -54,6 +54,14 @@ class Server:
             _lib.check(rc, "stc_server_poll")
         return rc == 1
 
+    def ready(self, timeout_s: float = 0.0, max_ids: int = 4096) -> list:
+        """Ids of jobs that finished, failed or were cancelled since the last call (a completion queue:
+        each id once), waiting up to timeout_s for the first."""
+        ids = (C.c_int64 * max_ids)()
+        n = C.c_int32(0)
+        _lib.check(self._lib.stc_server_ready(self._h, ids, max_ids, float(timeout_s), C.byref(n)), "stc_server_ready")
+        return list(ids[:n.value])
+
     def fetch(self, job_id: int):
         """(result array, latency in seconds); raises StencilError(BUSY) if not finished.
 

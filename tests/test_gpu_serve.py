@@ -118,6 +118,8 @@ def test_solo_lane_and_pitched_inputs(cuda, st, abi):
     with st.Server(hbm_fraction=0.5, steps_per_tick=4) as srv:
         ids = [srv.submit(a, hood, red, bnd, steps) for a, hood, red, bnd, steps in jobs]
         srv.drain(120.0)
+        assert sorted(srv.ready()) == sorted(ids)   # the completion queue reports each job once
+        assert srv.ready() == []
         for i, (a, hood, red, bnd, steps) in zip(ids, jobs):
             got, _ = srv.fetch(i)
             want = _alone(st, abi, np.asfortranarray(a), None, hood, red, bnd, steps)
