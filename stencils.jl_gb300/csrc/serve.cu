@@ -291,15 +291,13 @@ static void serve_loop(stc_server* s) {
                 fail_job(s, j, rc);
             }
         }
-        for (ServeJob* j : to_start) {
-            if (j->state == JOB_FAILED) continue;
-            j->state = JOB_ACTIVE;
-            if (j->solo) {
-                std::lock_guard<std::mutex> lk(s->mu);
-                s->solo_waiting.push_back(j);
-            } else {
-                std::lock_guard<std::mutex> lk(s->mu);
-                s->active.push_back(j);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);   // cancel() may run concurrently
+            for (ServeJob* j : to_start) {
+                if (j->state == JOB_FAILED) continue;
+                if (j->state == JOB_QUEUED) j->state = JOB_ACTIVE;   // a cancelled job is retired by its lane
+                if (j->solo) s->solo_waiting.push_back(j);
+                else s->active.push_back(j);
             }
         }
         // solo lane: at most kSoloInFlight runs queued on the solo stream at a time, so that its launches

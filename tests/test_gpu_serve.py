@@ -124,3 +124,26 @@ def test_solo_lane_and_pitched_inputs(cuda, st, abi):
             got, _ = srv.fetch(i)
             want = _alone(st, abi, np.asfortranarray(a), None, hood, red, bnd, steps)
             assert np.array_equal(got, want)
+
+
+def test_fetch_into_caller_buffer(cuda, st, abi):
+    """stc_server_fetch (the copying form) writes the same result into the caller's memory as the zero-copy
+    form, and the pinned buffer of the zero-copy form outlives the server."""
+    import ctypes as C
+    from stencils_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(8)
+    a = np.asfortranarray(rng.random((300, 257)).astype(np.float32))
+    want = _alone(st, abi, a, None, st.Window(1), st.mean, st.Wrap(), 12)
+    with st.Server(hbm_fraction=0.5, steps_per_tick=4) as srv:
+        i1 = srv.submit(a, st.Window(1), st.mean, st.Wrap(), 12)
+        i2 = srv.submit(a, st.Window(1), st.mean, st.Wrap(), 12)
+        srv.drain(60.0)
+        out = np.empty_like(a, order="F")
+        lat = C.c_double(0.0)
+        rc = lib.stc_server_fetch(srv._h, i1, out.ctypes.data_as(C.c_void_p), out.nbytes, C.byref(lat))
+        assert rc == 0 and lat.value >= 0
+        assert np.array_equal(out, want)
+        kept, _ = srv.fetch(i2)
+    assert np.array_equal(kept, want)   # the server is gone; its pinned result is still readable
+    del kept
