@@ -34,6 +34,8 @@ CASES = {
     "window_mean": lambda st: (st.Window(1), st.mean),
     "window_sum": lambda st: (st.Window(1), st.sum),
     "moore_mean": lambda st: (st.Moore(1), st.mean),
+    "moore_sum": lambda st: (st.Moore(1), st.sum),
+    "vn_mean": lambda st: (st.VonNeumann(1), st.mean),
     "vn_diffuse": lambda st: (st.VonNeumann(1), st.Diffusion(0.1)),
     "vn_sum": lambda st: (st.VonNeumann(1), st.sum),
 }
@@ -81,3 +83,25 @@ def test_blocked_2d_not_taken(cuda, st, orc, abi):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     got, _, kern = _run_gpu(st, a, st.Window(1), st.mean, st.Wrap(), st.Conditional(), 16)
     assert "tblock2d" not in kern   # one pass of 8 would leave state n in the wrong parent: per-step
+
+
+@pytest.mark.parametrize("kind", ["signed", "tiny", "huge", "zeros_and_tiny"])
+def test_blocked_2d_mean_outside_the_fast_quotient_range(cuda, st, orc, abi, kind):
+    """Tiles whose values leave [2^-64, 2^124] (or are negative) take the range-tested quotient; mixed
+    grids take both kinds of tile in one pass.  Bit-exact either way."""
+    rng = np.random.default_rng(len(kind))
+    shape = (300, 170)
+    a = rng.standard_normal(shape).astype(np.float32)
+    if kind == "tiny":
+        a = (np.abs(a) * 1e-30).astype(np.float32)
+    elif kind == "huge":
+        a = (np.abs(a) * 3e37).astype(np.float32)
+    elif kind == "zeros_and_tiny":
+        a = np.where(rng.random(shape) < 0.5, 0.0, np.abs(a)).astype(np.float32)
+        a[:150, :] *= np.float32(1e-25)
+    a = np.asfortranarray(a)
+    got, gprev, kern = _run_gpu(st, a, st.Window(1), st.mean, st.Wrap(), st.Conditional(), 17)
+    assert "tblock2d" in kern
+    want, wprev = _run_oracle(st, orc, abi, a, st.Window(1), st.mean, st.Wrap(), 17)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert np.array_equal(gprev.view(np.uint32), wprev.view(np.uint32))
