@@ -61,8 +61,22 @@ __device__ __forceinline__ int t2_wrap(int i, int n) {
     return i < 0 ? i + n : i;
 }
 
+// Range of the staged values for the mean's division: true if every value this thread staged is +0 or
+// lies in [2^-64, 2^124].  Then every sum formed over K <= 8 levels of means of at most 9 such values is 0
+// or within [2^-90, 3e38], where the FMA-corrected quotient (div_by_len's fast branch) is exact, so the
+// per-output range test can be dropped for the tile.
+struct T2Range {
+    uint32_t lo = 0xffffffffu, hi = 0u;   // min of (bits - 1) (a +0 wraps to the top), max of bits
+    __device__ __forceinline__ void add(float v) {
+        const uint32_t b = __float_as_uint(v);
+        lo = min(lo, b - 1u);
+        hi = max(hi, b);
+    }
+    __device__ __forceinline__ bool ok() const { return lo >= 0x1F7FFFFFu && hi <= 0x7D800000u; }
+};
+
 // Stage box rows [0, BY) x columns [0, 128) whose cell (0, 0) is grid cell (gx0, gy0).
-__device__ __forceinline__ void t2_load_box(const TB2Params& p, float* box, int gx0, int gy0, bool inside) {
+__device__ __forceinline__ void t2_load_box(const TB2Params& p, float* box, int gx0, int gy0, bool inside, T2Range& rg) {
     const int BY = p.BY;
     if (inside && p.vec_ok) {
         // 32 float4 per row; gx0 is a multiple of 4 and so is the row stride
@@ -70,11 +84,16 @@ __device__ __forceinline__ void t2_load_box(const TB2Params& p, float* box, int 
             const int r = i >> 5, c4 = i & 31;
             const float4 v = __ldg((const float4*)(p.src + (int64_t)(gy0 + r) * p.sstr + gx0) + c4);
             *((float4*)(box + r * kT2BX) + c4) = v;
+            rg.add(v.x);
+            rg.add(v.y);
+            rg.add(v.z);
+            rg.add(v.w);
         }
     } else if (inside) {
         for (int i = threadIdx.x; i < kT2BX * BY; i += blockDim.x) {
             const int r = i >> 7, c = i & 127;
             box[i] = __ldg(p.src + (int64_t)(gy0 + r) * p.sstr + gx0 + c);
+            rg.add(box[i]);
         }
     } else {
         for (int i = threadIdx.x; i < kT2BX * BY; i += blockDim.x) {
@@ -89,6 +108,7 @@ __device__ __forceinline__ void t2_load_box(const TB2Params& p, float* box, int 
                 v = __ldg(p.src + (int64_t)gy * p.sstr + gx);
             }
             box[i] = v;
+            rg.add(v);
         }
     }
 }
@@ -96,7 +116,7 @@ __device__ __forceinline__ void t2_load_box(const TB2Params& p, float* box, int 
 // One strip of one level: outputs (x, y) for y in [ra, rb) from the level below in `cur`.  LAST: the
 // outputs are the tile's and go to the destination parent (column pointer gcol, row gy0 + y, rows
 // below n1 only); else they go to `oth`, as padval where `patch` says the cell is outside the grid.
-template <class Op, class Sh, bool LAST>
+template <class Op, class Sh, bool LAST, bool FASTQ>
 __device__ __forceinline__ void t2_strip(const TB2Params& p, const float* cur, float* oth, int x, int ra, int rb,
                                          bool patch, bool xin, int gy0, float* gcol) {
     constexpr int R = Sh::kR, D = 2 * R + 1, L = Sh::L;
@@ -125,8 +145,17 @@ __device__ __forceinline__ void t2_strip(const TB2Params& p, const float* cur, f
     };
     auto finish = [&](const int slot, const int y) {
         float out;
-        if constexpr (std::is_same_v<Op, OpMean<float, float, A>>) out = Op::template finish_c<L>(acc[slot], ctr[slot], p);
-        else out = Op::finish(acc[slot], ctr[slot], p);
+        if constexpr (FASTQ) {
+            // the mean's quotient without the range test (the tile's range was checked when staged)
+            const float a = acc[slot];
+            const float q = __fmul_rn(a, p.rcp_f);
+            const float e = __fmaf_rn(-q, p.Lf, a);
+            out = __fmaf_rn(e, p.rcp_f, q);
+        } else if constexpr (std::is_same_v<Op, OpMean<float, float, A>>) {
+            out = Op::template finish_c<L>(acc[slot], ctr[slot], p);
+        } else {
+            out = Op::finish(acc[slot], ctr[slot], p);
+        }
         if constexpr (LAST) {
             if (gy0 + y < p.n1) gcol[(int64_t)(gy0 + y) * p.dstr] = out;
         } else {
@@ -172,6 +201,8 @@ __global__ void __launch_bounds__(kT2Threads) tb2_kernel(const TB2Params p) {
     extern __shared__ __align__(16) float t2sm[];
     constexpr int R = Sh::kR;
     static_assert(R == 1, "the box halo is K cells");
+    static_assert(K <= 8 && Sh::L <= 9, "the staged-range test assumes at most 8 levels of at most 9 taps");
+    constexpr bool kMean = std::is_same_v<Op, OpMean<float, float, float>>;
     const int BY = p.BY;
     float* const buf0 = t2sm;
     float* const buf1 = t2sm + kT2BX * BY;
@@ -181,8 +212,9 @@ __global__ void __launch_bounds__(kT2Threads) tb2_kernel(const TB2Params p) {
         const int gx0 = tx * p.TX - K, gy0 = ty * p.TY - K;   // grid cell of box (0, 0)
         const bool inside = gx0 >= 0 && gy0 >= 0 && gx0 + kT2BX <= p.n0 && gy0 + BY <= p.n1;
         __syncthreads();   // the previous tile's last level has read buf0 / buf1
-        t2_load_box(p, buf0, gx0, gy0, inside);
-        __syncthreads();
+        T2Range rg;
+        t2_load_box(p, buf0, gx0, gy0, inside, rg);
+        const bool fastq = __syncthreads_and(rg.ok()) && kMean && p.fastdiv_f;
         const bool patch = p.remove && !inside;
         const int gx = gx0 + x;
         const bool xin = gx >= 0 && gx < p.n0;
@@ -192,8 +224,10 @@ __global__ void __launch_bounds__(kT2Threads) tb2_kernel(const TB2Params p) {
         for (int g = 1; g < K; ++g) {
             const int lo = g * R, nr = BY - 2 * g * R;
             const int ra = lo + nr * s / kT2Strips, rb = lo + nr * (s + 1) / kT2Strips;
-            if (x >= g * R && x < kT2BX - g * R)
-                t2_strip<Op, Sh, false>(p, cur, oth, x, ra, rb, patch, xin, gy0, nullptr);
+            if (x >= g * R && x < kT2BX - g * R) {
+                if (kMean && fastq) t2_strip<Op, Sh, false, kMean>(p, cur, oth, x, ra, rb, patch, xin, gy0, nullptr);
+                else t2_strip<Op, Sh, false, false>(p, cur, oth, x, ra, rb, patch, xin, gy0, nullptr);
+            }
             __syncthreads();
             const float* t = cur;
             cur = oth;
@@ -202,8 +236,10 @@ __global__ void __launch_bounds__(kT2Threads) tb2_kernel(const TB2Params p) {
         {
             const int lo = K * R, nr = BY - 2 * K * R;
             const int ra = lo + nr * s / kT2Strips, rb = lo + nr * (s + 1) / kT2Strips;
-            if (x >= K * R && x < kT2BX - K * R && gx < p.n0)
-                t2_strip<Op, Sh, true>(p, cur, nullptr, x, ra, rb, false, true, gy0, p.dst + gx);
+            if (x >= K * R && x < kT2BX - K * R && gx < p.n0) {
+                if (kMean && fastq) t2_strip<Op, Sh, true, kMean>(p, cur, nullptr, x, ra, rb, false, true, gy0, p.dst + gx);
+                else t2_strip<Op, Sh, true, false>(p, cur, nullptr, x, ra, rb, false, true, gy0, p.dst + gx);
+            }
         }
     }
 }
