@@ -35,12 +35,12 @@ namespace stc {
 constexpr int kLifeMaxThreads = 1024;
 
 // CTA size of the Life kernels: 512 threads (16 warps; for 4096^2 the measured best of 128, 256 and 512
-// with the warp-row split: 1.49, 1.10 and 0.96 ms per 1000 generations).  STC_LIFE_THREADS = 128, 256
-// or 1024 overrides for the warp-row split, 1024 for the column split (a tuning knob).
+// with the warp-row split: 1.49, 1.10 and 0.96 ms per 1000 generations).  STC_LIFE_THREADS = 128 or 256
+// overrides for the warp-row split, 1024 for the column split (a tuning knob).
 static int life_threads(int W) {
     const char* e = getenv("STC_LIFE_THREADS");
     const int v = e ? atoi(e) : 0;
-    if (W == 128) return (v == 128 || v == 256 || v == 1024) ? v : 512;
+    if (W == 128) return (v == 128 || v == 256) ? v : 512;
     return v == 1024 ? 1024 : 512;
 }
 
@@ -304,20 +304,35 @@ __device__ __forceinline__ void life_warp_rows(const uint32_t* __restrict__ src,
     }
 }
 
-// Advance a band kk generations in the shared ping-pong pair (cur, oth), pitch life_pitch<WPL>(W).  Generation g
-// computes rows [max(g+1, lo_lim), min(rows-g-1, hi_lim)) — the rows whose three source rows are still
-// valid, and (Remove) only rows inside the grid; rows outside it stay zero in both buffers — split into
-// the lanes' strips.  Returns the buffer holding the result.  Ends with a barrier.
+// Generation g of a band computes rows [max(g+1, lo_lim), min(rows-g-1, hi_lim)) — the rows whose three
+// source rows are still valid, and (Remove) only rows inside the grid; rows outside it stay zero in both
+// buffers — split into the lanes' strips: this lane's strip is [*ra, *rb).
+__device__ __forceinline__ void life_strip_bounds(const LifeLane& L, int g, int rows, int lo_lim, int hi_lim, int* ra,
+                                                  int* rb) {
+    const int lo = max(g + 1, lo_lim), hi = min(rows - g - 1, hi_lim);
+    const int nr = hi - lo;
+    // the same monotone expression for a strip's end and the next strip's start, so the strips tile
+    // [lo, hi) exactly whatever the float rounding
+    *ra = lo + (int)((float)(nr * L.s) * L.inv_strips);
+    *rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
+}
+
+// Advance a band kk generations in the shared ping-pong pair (cur, oth), pitch life_pitch<WPL>(W).  Returns
+// the buffer holding the result.  Ends with a barrier.  `bounds` (optional): this strip's (ra, rb) for
+// generations 0 .. kk-1, computed once per run instead of every generation.
 template <bool CONWAY, bool WRAP, int WT, int WPL>
 __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
-                                               int kk, int lo_lim, int hi_lim, uint32_t birth, uint32_t survive) {
+                                               int kk, int lo_lim, int hi_lim, uint32_t birth, uint32_t survive,
+                                               const int2* bounds = nullptr) {
     for (int g = 0; g < kk; ++g) {
-        const int lo = max(g + 1, lo_lim), hi = min(rows - g - 1, hi_lim);
-        const int nr = hi - lo;
-        // strip bounds: the same monotone expression for a strip's end and the next strip's start, so
-        // the strips tile [lo, hi) exactly whatever the float rounding
-        const int ra = lo + (int)((float)(nr * L.s) * L.inv_strips);
-        const int rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
+        int ra, rb;
+        if (bounds) {
+            const int2 b = bounds[g];
+            ra = b.x;
+            rb = b.y;
+        } else {
+            life_strip_bounds(L, g, rows, lo_lim, hi_lim, &ra, &rb);
+        }
         if (L.active && ra < rb) {
             if constexpr (WPL > 0) life_warp_rows<CONWAY, WRAP, WPL>(cur, oth, ra, rb, birth, survive);
             else if (L.edge_warp) life_strip<CONWAY, WRAP, WT, true>(L, cur, oth, W, ra, rb, birth, survive);
@@ -387,7 +402,7 @@ template <int WT>
 __host__ __device__ constexpr int life_wpl() { return (WT > 0 && WT % 32 == 0 && WT / 32 <= 4 && WT / 32 != 3) ? WT / 32 : 0; }
 
 template <bool CONWAY, bool WRAP, int WT>
-__global__ void __launch_bounds__(kLifeMaxThreads) life_block_kernel(const LifeParams p) {
+__global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1) life_block_kernel(const LifeParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
     constexpr int WPL = life_wpl<WT>();
     const int W = WT > 0 ? WT : p.W, P = life_pitch<WPL>(W), k = p.k;
@@ -456,7 +471,7 @@ __device__ __forceinline__ bool take_tagged(uint64_t v, const uint64_t* p, uint3
 }
 
 template <bool CONWAY, bool WRAP, int WT>
-__global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCoopParams p) {
+__global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1) life_coop_kernel(const LifeCoopParams p) {
     extern __shared__ __align__(16) uint32_t lsm[];
     constexpr int WPL = life_wpl<WT>();
     const int W = WT > 0 ? WT : p.W, P = life_pitch<WPL>(W), k = p.k, G = gridDim.x, b = blockIdx.x;
@@ -475,6 +490,20 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCo
     const int slab = k * W;                            // one published row block
     const int64_t nmain = p.nsteps - 1;                // generations before the last one
     const LifeLane lane = life_lane<WPL>(W, p.n0);
+    // every super-step's generation g uses the same strip bounds: computed once, [strip][g]
+    __shared__ int2 s_bounds[WPL > 0 ? 1024 : 1];
+    const bool tabled = WPL > 0 && lane.strips * k <= 1024;
+    if (tabled) {
+        for (int i = threadIdx.x; i < lane.strips * k; i += blockDim.x) {
+            LifeLane t = lane;
+            t.s = i / k;
+            int ra, rb;
+            life_strip_bounds(t, i - t.s * k, rows, lo_lim, hi_lim, &ra, &rb);
+            s_bounds[i] = make_int2(ra, rb);
+        }
+        __syncthreads();
+    }
+    const int2* my_bounds = tabled ? s_bounds + lane.s * k : nullptr;
     int64_t gen = 0;
     for (int step = 0;; ++step) {
         const bool final = gen >= nmain;
@@ -522,7 +551,8 @@ __global__ void __launch_bounds__(kLifeMaxThreads) life_coop_kernel(const LifeCo
                 }
             }
         }
-        cur = life_gens<CONWAY, WRAP, WT, WPL>(lane, cur, oth, rows, W, kk, lo_lim, hi_lim, p.birth, p.survive);
+        cur = life_gens<CONWAY, WRAP, WT, WPL>(lane, cur, oth, rows, W, kk, lo_lim, hi_lim, p.birth, p.survive,
+                                               my_bounds);
         oth = (cur == lsm) ? buf1 : lsm;
         gen += kk;
         if (final) {
