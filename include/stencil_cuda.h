@@ -61,8 +61,10 @@ typedef enum {
     STC_ERR_BUSY = -10,           /* result not ready / queue full */
     STC_ERR_CANCELLED = -11,      /* job was cancelled before it finished */
     STC_ERR_TOO_LARGE = -12,      /* grid larger than the fixed scratch of stc_life_steps_noalloc */
-    STC_ERR_INEXACT = -13         /* a result does not convert exactly to the destination element type
+    STC_ERR_INEXACT = -13,        /* a result does not convert exactly to the destination element type
                                      (the reference's InexactError on setindex!) */
+    STC_ERR_BOUNDS = -14          /* debug build (libstencilcuda_debug.so) only: a kernel's computed index
+                                     fell outside the buffer it addresses; the access was skipped */
 } stc_status;
 
 /* ---- element types ---- */
@@ -170,6 +172,12 @@ typedef struct {
 STC_API int         stc_abi_version(void);
 STC_API const char* stc_strerror(int status);
 STC_API int         stc_last_cuda_error(void);              /* the cudaError_t behind the last STC_ERR_CUDA */
+/* 1 in the debug build (device-side bounds tests, STC_ERR_BOUNDS), 0 in the release build. */
+STC_API int         stc_debug_bounds(void);
+/* Debug build: queue on `stream` a one-thread kernel that reports a failed bounds test through the stream's
+ * status slot, as a failing test inside a kernel would (no access is made), so the next synchronising call
+ * on that stream returns STC_ERR_BOUNDS.  The release build returns STC_ERR_UNSUPPORTED. */
+STC_API int         stc_debug_report_bounds(void* stream);
 /* No counterpart in the reference.  Multi-step runs that work on an internal padded pair (3D grids:
  * the temporally blocked path and the edge-patching path) keep that pair's device memory per device
  * for the next run (stream-ordered: a run on another stream waits for the previous one to finish

@@ -19,7 +19,7 @@ STATUS_NAMES = {
     0: "STC_OK", -1: "STC_ERR_SIZE_MISMATCH", -2: "STC_ERR_RADIUS", -3: "STC_ERR_KERNEL_LENGTH",
     -4: "STC_ERR_UNSUPPORTED", -5: "STC_ERR_INVALID", -6: "STC_ERR_CUDA", -7: "STC_ERR_TIMEOUT",
     -8: "STC_ERR_NO_DEVICE", -9: "STC_ERR_BUDGET", -10: "STC_ERR_BUSY", -11: "STC_ERR_CANCELLED",
-    -12: "STC_ERR_TOO_LARGE", -13: "STC_ERR_INEXACT",
+    -12: "STC_ERR_TOO_LARGE", -13: "STC_ERR_INEXACT", -14: "STC_ERR_BOUNDS",
 }
 STC_ERR_BUSY = -10
 STC_ASYNC = 1

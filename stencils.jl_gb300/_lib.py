@@ -10,7 +10,11 @@ from pathlib import Path
 
 from . import _abi as A
 
+import os
+
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libstencilcuda.so"
+# the debug build (device-side bounds tests, STC_ERR_BOUNDS), loaded instead when STC_DEBUG_BOUNDS=1
+LIB_DEBUG_PATH = Path(__file__).resolve().parent / "_build" / "debug" / "libstencilcuda_debug.so"
 _lib = None
 
 
@@ -37,7 +41,7 @@ def load(path: str | Path | None = None):
     global _lib
     if _lib is not None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else (LIB_DEBUG_PATH if os.environ.get("STC_DEBUG_BOUNDS") == "1" else LIB_PATH)
     if not p.exists():
         raise RuntimeError(f"libstencilcuda.so not built ({p}); run __graft_entry__.build()")
     lib = C.CDLL(str(p))
@@ -47,6 +51,8 @@ def load(path: str | Path | None = None):
         "stc_abi_version": ([], C.c_int),
         "stc_strerror": ([C.c_int], C.c_char_p),
         "stc_last_cuda_error": ([], C.c_int),
+        "stc_debug_bounds": ([], C.c_int),
+        "stc_debug_report_bounds": ([vp], C.c_int),
         "stc_release_workspace": ([], C.c_int),
         "stc_result_dtype": ([C.c_int32, C.c_int32, C.c_int32], C.c_int),
         "stc_neighbor_dtype": ([C.c_int32, P(A.BcDesc)], C.c_int),

@@ -43,14 +43,20 @@ def _stale(target: Path, deps) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
-    OUT_DIR.mkdir(exist_ok=True)
+def build(force: bool = False, verbose: bool = False, extra_flags=(), debug: bool = False) -> Path:
+    """Compile and link the library; debug=True builds libstencilcuda_debug.so (in _build/debug/) with the
+    kernels' device-side bounds tests compiled in (-DSTC_DEBUG_BOUNDS)."""
+    out_dir = OUT_DIR / "debug" if debug else OUT_DIR
+    lib = out_dir / "libstencilcuda_debug.so" if debug else LIB
+    if debug:
+        extra_flags = (*extra_flags, "-DSTC_DEBUG_BOUNDS")
+    out_dir.mkdir(parents=True, exist_ok=True)
     headers = _headers()
     srcs = _sources()
     objs = []
     jobs = []
     for s in srcs:
-        o = OUT_DIR / (s.stem + ".o")
+        o = out_dir / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra_flags, "-c", str(s), "-o", str(o)]
@@ -68,14 +74,14 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> Path:
                     errors.append(f"{futs[f].name}:\n{r.stderr}")
             if errors:
                 raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    if force or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcuda"]
+    if force or _stale(lib, objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcuda"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
     import sys
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, debug="--debug" in sys.argv))

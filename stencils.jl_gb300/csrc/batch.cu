@@ -195,6 +195,8 @@ template <int NW> struct BatchTileP {
     float alpha_f;
     float wf[NW];
     const double* w;
+    uint32_t box_bytes;   // the staged box (bounds tests of the debug build)
+    int32_t* status;
 };
 
 // Geometry of the vector-column tiles of the batched kernel (shared with the host planner).
@@ -215,7 +217,7 @@ template <class T, int R> struct BatchVecBox {
 // into the destination parent, so each cell's fold is the one stc_map_steps performs.
 template <class T, class Op, class Sh>
 __device__ void batch_tile_vec(const BatchJob& j, const BatchItem& it, unsigned char* smem, const float* sw,
-                               const OpArgs& oa) {
+                               const OpArgs& oa, int32_t* status) {
     using G = BatchVecGeom<T>;
     constexpr int R = Sh::kR;
     using B = BatchVecBox<T, R>;
@@ -263,6 +265,8 @@ __device__ void batch_tile_vec(const BatchJob& j, const BatchItem& it, unsigned 
     p.dstr[0] = 1; p.dstr[1] = j.sy[dstb]; p.dstr[2] = 0;
     p.L = oa.L; p.birth = oa.birth; p.survive = oa.survive; p.alpha = oa.alpha; p.rcp_f = oa.rcp_f;
     p.fastdiv_f = oa.fastdiv_f; p.Lf = oa.Lf; p.Ld = oa.Ld; p.alpha_f = oa.alpha_f; p.w = nullptr;
+    p.box_bytes = (uint32_t)(BW * BH * sizeof(T));
+    p.status = status;
 #pragma unroll
     for (int k = 0; k < NW; ++k) p.wf[k] = NW > 1 ? sw[k] : 0.f;
     compute_shape_vec<T, T, Op, Sh, G::XV, G::VS>(p, TileOrigin{x0, y0, 0}, box);
@@ -339,7 +343,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(const BatchDev d) 
     }
 #define STC_BV(DT, OPV, T, OP, KIND, RR)                                                        \
     if (key == DT * 16 + OPV && j.shape == KIND && j.R == RR && j.vec) {                        \
-        batch_tile_vec<T, OP, Shape<KIND, RR, 2>>(j, it, bsm, sw, oa);                          \
+        batch_tile_vec<T, OP, Shape<KIND, RR, 2>>(j, it, bsm, sw, oa, d.status);                          \
         goto item_done;                                                                         \
     }
         // vector-column tiles (one step per round) for the shapes batched workloads use

@@ -224,7 +224,9 @@ int take_status(const StatusSlot& sl) {
     const int v = *sl.host;
     if (!v) return STC_OK;
     *sl.host = 0;
-    return (v & DEV_ERR_TIMEOUT) ? STC_ERR_TIMEOUT : STC_ERR_INEXACT;
+    if (v & DEV_ERR_TIMEOUT) return STC_ERR_TIMEOUT;
+    if (v & DEV_ERR_BOUNDS) return STC_ERR_BOUNDS;
+    return STC_ERR_INEXACT;
 }
 
 // waits for the stream, then reads and clears its status slot
@@ -604,6 +606,10 @@ int launch_map(const stc_grid* src, const stc_grid* dst, int dst_padded, const s
     return cuda_fail(err);
 }
 
+#ifdef STC_DEBUG_BOUNDS
+__global__ void report_bounds_kernel(int* status) { atomicOr(status, DEV_ERR_BOUNDS); }
+#endif
+
 }  // namespace stc
 
 using namespace stc;
@@ -611,6 +617,28 @@ using namespace stc;
 extern "C" {
 
 int stc_abi_version(void) { return STC_ABI_VERSION; }
+
+int stc_debug_bounds(void) {
+#ifdef STC_DEBUG_BOUNDS
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+int stc_debug_report_bounds(void* stream) {
+#ifdef STC_DEBUG_BOUNDS
+    DeviceCtx* ctx = nullptr;
+    int rc = device_ctx(&ctx);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    report_bounds_kernel<<<1, 1, 0, s>>>(status_slot(ctx, s).dev);
+    return cuda_fail(cudaGetLastError());
+#else
+    (void)stream;
+    return STC_ERR_UNSUPPORTED;
+#endif
+}
 
 const char* stc_strerror(int status) {
     switch (status) {
@@ -628,6 +656,7 @@ const char* stc_strerror(int status) {
     case STC_ERR_CANCELLED: return "cancelled";
     case STC_ERR_TOO_LARGE: return "grid exceeds the fixed no-allocation scratch (4096*4096 cells)";
     case STC_ERR_INEXACT: return "InexactError: a result does not convert exactly to the destination element type";
+    case STC_ERR_BOUNDS: return "a device-side bounds test failed (debug build); the access was skipped";
     }
     return "unknown status";
 }

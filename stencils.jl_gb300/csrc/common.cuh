@@ -19,6 +19,21 @@ namespace stc {
 // Kernels that give up a bounded wait OR a bit into this word; the host reads and clears it.
 enum : int { DEV_ERR_TIMEOUT = 1, DEV_ERR_BOUNDS = 2, DEV_ERR_INEXACT = 4 };
 
+// Debug builds (-DSTC_DEBUG_BOUNDS: `build.py --debug`, libstencilcuda_debug.so): kernels test the indices
+// of their computed shared-memory accesses against the buffers they address before making them.  An index
+// out of range skips the access and ORs DEV_ERR_BOUNDS into the launch's status slot — never a trap — so the
+// host call returns STC_ERR_BOUNDS.  Release builds compile the tests out.
+#ifdef STC_DEBUG_BOUNDS
+__device__ __forceinline__ bool bounds_ok(int64_t i, int64_t n, int* status) {
+    if (i >= 0 && i < n) return true;
+    if (status) atomicOr(status, DEV_ERR_BOUNDS);
+    return false;
+}
+#define STC_IN_BOUNDS(i, n, status) ::stc::bounds_ok((int64_t)(i), (int64_t)(n), (status))
+#else
+#define STC_IN_BOUNDS(i, n, status) true
+#endif
+
 // ------------------------------------------------------------------ element traits
 template <int DT> struct Elem;
 template <> struct Elem<STC_F64>  { using T = double;          static constexpr bool is_float = true; };

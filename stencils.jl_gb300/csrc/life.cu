@@ -323,7 +323,7 @@ __device__ __forceinline__ void life_strip_bounds(const LifeLane& L, int g, int 
 template <bool CONWAY, bool WRAP, int WT, int WPL>
 __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
                                                int kk, int lo_lim, int hi_lim, uint32_t birth, uint32_t survive,
-                                               const int2* bounds = nullptr) {
+                                               const int2* bounds = nullptr, int* status = nullptr) {
     for (int g = 0; g < kk; ++g) {
         int ra, rb;
         if (bounds) {
@@ -333,7 +333,8 @@ __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur,
         } else {
             life_strip_bounds(L, g, rows, lo_lim, hi_lim, &ra, &rb);
         }
-        if (L.active && ra < rb) {
+        // the strip reads band rows ra-1 .. rb (debug build: tested against the band)
+        if (L.active && ra < rb && STC_IN_BOUNDS(ra - 1, rows, status) && STC_IN_BOUNDS(rb, rows, status)) {
             if constexpr (WPL > 0) life_warp_rows<CONWAY, WRAP, WPL>(cur, oth, ra, rb, birth, survive);
             else if (L.edge_warp) life_strip<CONWAY, WRAP, WT, true>(L, cur, oth, W, ra, rb, birth, survive);
             else life_strip<CONWAY, WRAP, WT, false>(L, cur, oth, W, ra, rb, birth, survive);
@@ -388,6 +389,7 @@ __device__ __forceinline__ void load_band(const uint32_t* in, uint32_t* buf, uin
 struct LifeParams {
     const uint32_t* in;
     uint32_t* out;
+    int* status;    // debug build: bounds tests
     int n0;         // cells per row
     int W;          // words per row
     int n1;         // rows
@@ -415,7 +417,8 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
     int lo_lim, hi_lim;
     band_limits<WRAP>(rows, y0 - k, p.n1, &lo_lim, &hi_lim);
     const LifeLane lane = life_lane<WPL>(W, p.n0);
-    uint32_t* fin = life_gens<CONWAY, WRAP, WT, WPL>(lane, buf0, buf1, rows, W, k, lo_lim, hi_lim, p.birth, p.survive);
+    uint32_t* fin = life_gens<CONWAY, WRAP, WT, WPL>(lane, buf0, buf1, rows, W, k, lo_lim, hi_lim, p.birth, p.survive,
+                                                     nullptr, p.status);
     for (int i = threadIdx.x; i < p.TB * W; i += blockDim.x) {
         const int r = i / W, w = i - r * W;
         const int gy = y0 + r;
@@ -552,7 +555,7 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
             }
         }
         cur = life_gens<CONWAY, WRAP, WT, WPL>(lane, cur, oth, rows, W, kk, lo_lim, hi_lim, p.birth, p.survive,
-                                               my_bounds);
+                                               my_bounds, p.status);
         oth = (cur == lsm) ? buf1 : lsm;
         gen += kk;
         if (final) {
@@ -861,6 +864,7 @@ int life_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     if (rc) { cudaFreeAsync(P, stream); return rc; }
 
     LifeParams lp{};
+    lp.status = status_slot(ctx, stream).dev;
     lp.n0 = (int)n0;
     lp.W = W;
     lp.n1 = (int)n1;

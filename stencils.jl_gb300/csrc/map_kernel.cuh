@@ -449,6 +449,22 @@ __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOr
         const int lz = p.tiles3d ? s : 0;
         c[s] = box + ((lz + p.rz) * p.bh + (ly + p.ry)) * p.bw + (lane + p.padl);
     }
+#ifdef STC_DEBUG_BOUNDS
+    {
+        // every read of this thread lies within the staged box (centre and every offset, all columns)
+        int dmin = 0, dmax = 0;
+        for (int k = 0; k < p.L; ++k) {
+            const int d = (p.off[k][2] * p.bh + p.off[k][1]) * p.bw + p.off[k][0];
+            dmin = min(dmin, d);
+            dmax = max(dmax, d);
+        }
+        const int64_t n = p.box_bytes / sizeof(Tin);
+        for (int s = 0; s < VS; ++s) {
+            const int64_t b = c[s] - box;
+            if (!STC_IN_BOUNDS(b + dmin, n, p.status) || !STC_IN_BOUNDS(b + 32 * (XT - 1) + dmax, n, p.status)) return;
+        }
+    }
+#endif
     typename Op::A a[VS][XT];
     int k0 = 0;
     if constexpr (Op::kZeroInit) {
@@ -518,6 +534,15 @@ __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrig
     // bb[r * sr + yy * p.bw + xx + 32 i]
     const int sr = (N == 3) ? p.bh * p.bw : p.bw;
     const Tin* bb = box + ((N == 3) ? (warp + p.ry - RY) * p.bw : p.rz * p.bh * p.bw + warp * VS * p.bw) + lane + p.padl - R;
+#ifdef STC_DEBUG_BOUNDS
+    {
+        // the first and the last element this thread reads lie within the staged box
+        const int64_t n = p.box_bytes / sizeof(Tin), b = bb - box;
+        if (!STC_IN_BOUNDS(b, n, p.status) ||
+            !STC_IN_BOUNDS(b + (NROW - 1) * sr + 2 * RY * p.bw + (D - 1) + 32 * (XT - 1), n, p.status))
+            return;
+    }
+#endif
     // tile-local extents that hold real outputs (ragged last tiles)
     const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0);
     const int nvs = (N == 3) ? (int)min((int64_t)VS, p.n[2] - o.z0) : (int)min((int64_t)VS, p.n[1] - o.y0 - warp * VS);
@@ -705,6 +730,14 @@ __device__ __forceinline__ void compute_shape_vec(const P& p, const TileOrigin& 
     const int sr = (N == 3) ? p.bh * p.bw : p.bw;
     const Tin* bb = box + ((N == 3) ? (warp + p.ry - RY) * p.bw : p.rz * p.bh * p.bw + warp * VS * p.bw) +
                     p.padl - PA + lane * XV;
+#ifdef STC_DEBUG_BOUNDS
+    {
+        // the first and the last element this thread reads lie within the staged box
+        const int64_t n = p.box_bytes / sizeof(Tin), b = bb - box;
+        if (!STC_IN_BOUNDS(b, n, p.status) || !STC_IN_BOUNDS(b + (NROW - 1) * sr + 2 * RY * p.bw + NE - 1, n, p.status))
+            return;
+    }
+#endif
     const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0) - lane * XV;   // valid outputs of this thread's XV
     const int nvs = (N == 3) ? (int)min((int64_t)VS, p.n[2] - o.z0) : (int)min((int64_t)VS, p.n[1] - o.y0 - warp * VS);
     const bool row_ok = (N == 3) ? (o.y0 + warp < p.n[1]) : true;

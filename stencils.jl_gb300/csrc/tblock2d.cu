@@ -42,6 +42,7 @@ struct TB2Params {
     int32_t BY;            // box rows
     int32_t TX, TY;        // tile outputs (TX = 128 - 2K, TY = BY - 2K)
     int32_t ntx, ntiles;
+    int32_t* status;       // debug build: bounds tests
     int32_t remove;        // Remove: cells outside the grid hold padval at every level
     int32_t vec_ok;        // interior boxes may be staged with 16-byte loads
     float padf;
@@ -224,7 +225,9 @@ __global__ void __launch_bounds__(kT2Threads) tb2_kernel(const TB2Params p) {
         for (int g = 1; g < K; ++g) {
             const int lo = g * R, nr = BY - 2 * g * R;
             const int ra = lo + nr * s / kT2Strips, rb = lo + nr * (s + 1) / kT2Strips;
-            if (x >= g * R && x < kT2BX - g * R) {
+            // the strip reads box rows ra-1 .. rb and columns x-1 .. x+1 (debug build: tested against the box)
+            if (x >= g * R && x < kT2BX - g * R && STC_IN_BOUNDS(ra - 1, BY, p.status) && STC_IN_BOUNDS(rb, BY, p.status) &&
+                STC_IN_BOUNDS(x - 1, kT2BX, p.status) && STC_IN_BOUNDS(x + 1, kT2BX, p.status)) {
                 if (kMean && fastq) t2_strip<Op, Sh, false, kMean>(p, cur, oth, x, ra, rb, patch, xin, gy0, nullptr);
                 else t2_strip<Op, Sh, false, false>(p, cur, oth, x, ra, rb, patch, xin, gy0, nullptr);
             }
@@ -236,7 +239,8 @@ __global__ void __launch_bounds__(kT2Threads) tb2_kernel(const TB2Params p) {
         {
             const int lo = K * R, nr = BY - 2 * K * R;
             const int ra = lo + nr * s / kT2Strips, rb = lo + nr * (s + 1) / kT2Strips;
-            if (x >= K * R && x < kT2BX - K * R && gx < p.n0) {
+            if (x >= K * R && x < kT2BX - K * R && gx < p.n0 && STC_IN_BOUNDS(ra - 1, BY, p.status) &&
+                STC_IN_BOUNDS(rb, BY, p.status)) {
                 if (kMean && fastq) t2_strip<Op, Sh, true, kMean>(p, cur, nullptr, x, ra, rb, false, true, gy0, p.dst + gx);
                 else t2_strip<Op, Sh, true, false>(p, cur, nullptr, x, ra, rb, false, true, gy0, p.dst + gx);
             }
@@ -339,6 +343,7 @@ int tb2d_try_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, 
     if ((int64_t)p.ntx * nty >= (1ll << 31)) return STC_OK;
     p.ntiles = (int32_t)(p.ntx * nty);
     p.remove = bc->boundary == STC_REMOVE;
+    p.status = status_slot(ctx, stream).dev;
     p.padf = (float)bc->padval;
     p.L = st->len;
     p.alpha = op->alpha;
