@@ -8,8 +8,10 @@ namespace stc {
 static RegisterShapeVec<STC_F32, OPV_KDOT_F, STC_SHAPE_WINDOW, 3, 2, 4, 8> v0;
 static RegisterShapeVec<STC_BF16, OPV_KDOT_F, STC_SHAPE_WINDOW, 3, 2, 4, 8> v1;
 static RegisterShapeVec<STC_F32, OPV_KDOT_F, STC_SHAPE_WINDOW, 2, 2, 4, 8> v2;
-// mean blur Window(1)
-static RegisterShapeVec<STC_F64, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 2, 8> v3;
+// mean blur Window(1); Float64 on 64 x 16 tiles (2 stream rows per warp): the FP64 map of a 1000^2 grid is
+// latency-bound, and more, smaller tiles per SM measured 26.8 us per map against 29.9 us with 64 x 32 tiles
+// and 35.7 us with 64 x 64
+static RegisterShapeVec<STC_F64, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 2, 2> v3;
 static RegisterShapeVec<STC_F32, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 4, 8> v4;
 static RegisterShapeVec<STC_BF16, OPV_MEAN, STC_SHAPE_WINDOW, 1, 2, 4, 8> v5;
 // Circle(3) mean, Cross(2) sum
