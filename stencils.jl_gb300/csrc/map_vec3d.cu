@@ -6,5 +6,6 @@
 namespace stc {
 static RegisterShapeVec<STC_F32, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, 1, 3, 2, 8, 3> w0;
 static RegisterShapeVec<STC_BF16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, 1, 3, 4, 8> w1;
+static RegisterShapeVec<STC_F16, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, 1, 3, 4, 8> w1h;
 static RegisterShapeVec<STC_F64, OPV_DIFFUSE, STC_SHAPE_VONNEUMANN, 1, 3, 2, 8> w2;
 }  // namespace stc

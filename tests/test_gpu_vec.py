@@ -24,6 +24,7 @@ VEC_CONFIGS = [
     ("life", "U8", "Moore", 1, 2), ("life", "BOOL", "Moore", 1, 2),
     ("diffuse", "F32", "VonNeumann", 1, 3), ("diffuse", "BF16", "VonNeumann", 1, 3),
     ("diffuse", "F64", "VonNeumann", 1, 3),
+    ("kdot_f", "F16", "Window", 3, 2), ("mean", "F16", "Window", 1, 2), ("diffuse", "F16", "VonNeumann", 1, 3),
 ]
 BOUNDARIES = ["remove0", "remove_nz", "wrap", "reflect"]
 
@@ -55,6 +56,8 @@ def _tolerance(st, abi, ora, stencil, a, want, code, bnd, pad):
     tol = 2 * len(stencil) * 2.0 ** -24 * mag + 1e-30
     if code == abi.BF16:
         tol = tol + np.abs(as_f64(want, code, abi)) * 2.0 ** -7 + 1e-6
+    if code == abi.F16:
+        tol = tol + np.abs(as_f64(want, code, abi)) * 2.0 ** -10 + 1e-7
     return tol
 
 
