@@ -667,7 +667,7 @@ def cfg_diffusion(args):
 
 def cfg_blocked2d(args):
     """2D multi-step maps on Float32 state: Window(1) mean and VonNeumann(1) diffusion, 8192^2 U[0,1), Wrap,
-    100 steps, temporally blocked (4 steps per pass over HBM) against the per-step map (STC_TBLOCK=0)."""
+    100 steps, temporally blocked (8 steps per pass over HBM) against the per-step map (STC_TBLOCK=0)."""
     import torch
     st = entry.load_package()
     from stencils_gb300 import _lib
