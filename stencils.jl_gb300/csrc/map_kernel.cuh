@@ -730,12 +730,16 @@ __device__ __forceinline__ void compute_shape_vec(const P& p, const TileOrigin& 
     const int sr = (N == 3) ? p.bh * p.bw : p.bw;
     const Tin* bb = box + ((N == 3) ? (warp + p.ry - RY) * p.bw : p.rz * p.bh * p.bw + warp * VS * p.bw) +
                     p.padl - PA + lane * XV;
+    // the lanes that store outputs (every lane of the warp takes part in the vote)
+    const unsigned storing = __ballot_sync(0xffffffffu, (int)min((int64_t)p.tw, p.n[0] - o.x0) - lane * XV > 0);
 #ifdef STC_DEBUG_BOUNDS
     {
-        // the first and the last element this thread reads lie within the staged box
+        // the first and the last element this thread reads lie within the staged box (the whole warp leaves
+        // together if one lane fails: the fold below votes across the warp)
         const int64_t n = p.box_bytes / sizeof(Tin), b = bb - box;
-        if (!STC_IN_BOUNDS(b, n, p.status) || !STC_IN_BOUNDS(b + (NROW - 1) * sr + 2 * RY * p.bw + NE - 1, n, p.status))
-            return;
+        const bool bad = !STC_IN_BOUNDS(b, n, p.status) ||
+                         !STC_IN_BOUNDS(b + (NROW - 1) * sr + 2 * RY * p.bw + NE - 1, n, p.status);
+        if (__any_sync(0xffffffffu, bad)) return;
     }
 #endif
     const int nvx = (int)min((int64_t)p.tw, p.n[0] - o.x0) - lane * XV;   // valid outputs of this thread's XV
@@ -780,12 +784,36 @@ __device__ __forceinline__ void compute_shape_vec(const P& p, const TileOrigin& 
             }
             if (q == D - 1 && sidx < nvs && row_ok && nvx > 0) {
                 Tout res[XV];
+                if constexpr (std::is_same_v<OpV, OpMean<V, Tout, A>> && std::is_same_v<A, float>) {
+                    // The Float32 mean's correctly rounded division: when every sum of the warp's row lies
+                    // in [2^-90, 3e38] (the range where the FMA-corrected quotient is exact, checked on the
+                    // host for this L) all lanes take that quotient after one vote, instead of a range
+                    // test and a branch per output; otherwise every output takes the tested division.
+                    bool fast = p.fastdiv_f != 0;
+                    float qf[XV];
 #pragma unroll
-                for (int c = 0; c < XV; ++c) {
-                    if constexpr (std::is_same_v<OpV, OpMean<V, Tout, A>>)
-                        res[c] = OpV::template finish_c<L>(acc[slot][c], ctr[slot][c], p);
-                    else
-                        res[c] = OpV::finish(acc[slot][c], ctr[slot][c], p);
+                    for (int c = 0; c < XV; ++c) {
+                        const float a = acc[slot][c];
+                        fast = fast && fabsf(a) >= 0x1p-90f && fabsf(a) <= 3.0e38f;
+                        const float q0 = __fmul_rn(a, p.rcp_f);
+                        const float e = __fmaf_rn(-q0, p.Lf, a);
+                        qf[c] = __fmaf_rn(e, p.rcp_f, q0);
+                    }
+                    if (__all_sync(storing, fast)) {
+#pragma unroll
+                        for (int c = 0; c < XV; ++c) res[c] = from_f32<Tout>(qf[c]);
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < XV; ++c) res[c] = OpV::template finish_c<L>(acc[slot][c], ctr[slot][c], p);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < XV; ++c) {
+                        if constexpr (std::is_same_v<OpV, OpMean<V, Tout, A>>)
+                            res[c] = OpV::template finish_c<L>(acc[slot][c], ctr[slot][c], p);
+                        else
+                            res[c] = OpV::finish(acc[slot][c], ctr[slot][c], p);
+                    }
                 }
                 st_row_vec<Tout, XV>(dbase + sidx * dstep, res, aligned, nvx);
             }
