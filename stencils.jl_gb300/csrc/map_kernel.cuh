@@ -91,6 +91,17 @@ template <class P> __device__ __forceinline__ double div_by_len(double a, const 
     return __ddiv_rn(a, p.Ld);
 }
 
+// The mean's Float32 quotient without a per-output range test: true if the FMA-corrected quotient of a
+// (div_by_len's fast branch) is exact, i.e. the host verified it for this L and a is in [2^-90, 3e38].
+template <class P> __device__ __forceinline__ bool fastdiv_in_range(float a, const P& p) {
+    return p.fastdiv_f && fabsf(a) >= 0x1p-90f && fabsf(a) <= 3.0e38f;
+}
+template <class P> __device__ __forceinline__ float fastdiv_quotient(float a, const P& p) {
+    const float q = __fmul_rn(a, p.rcp_f);
+    const float e = __fmaf_rn(-q, p.Lf, a);
+    return __fmaf_rn(e, p.rcp_f, q);
+}
+
 // Correctly rounded a / LC for a compile-time 2 <= LC <= 512, in integer arithmetic (schoolbook
 // binary division with guard and sticky bits, IEEE 754 round to nearest even): the 53-bit significand
 // shifted left by 11 is divided by the constant (a multiply-high, no division instruction), the quotient
@@ -459,10 +470,12 @@ __device__ __forceinline__ void compute_generic(const MapParams& p, const TileOr
             dmax = max(dmax, d);
         }
         const int64_t n = p.box_bytes / sizeof(Tin);
+        bool bad = false;
         for (int s = 0; s < VS; ++s) {
             const int64_t b = c[s] - box;
-            if (!STC_IN_BOUNDS(b + dmin, n, p.status) || !STC_IN_BOUNDS(b + 32 * (XT - 1) + dmax, n, p.status)) return;
+            bad = bad || !STC_IN_BOUNDS(b + dmin, n, p.status) || !STC_IN_BOUNDS(b + 32 * (XT - 1) + dmax, n, p.status);
         }
+        if (__any_sync(0xffffffffu, bad)) return;   // the whole warp: the finish below votes across it
     }
 #endif
     typename Op::A a[VS][XT];
@@ -536,11 +549,12 @@ __device__ __forceinline__ void compute_shape(const MapParams& p, const TileOrig
     const Tin* bb = box + ((N == 3) ? (warp + p.ry - RY) * p.bw : p.rz * p.bh * p.bw + warp * VS * p.bw) + lane + p.padl - R;
 #ifdef STC_DEBUG_BOUNDS
     {
-        // the first and the last element this thread reads lie within the staged box
+        // the first and the last element this thread reads lie within the staged box (the whole warp leaves
+        // together if one lane fails: the fold below votes across the warp)
         const int64_t n = p.box_bytes / sizeof(Tin), b = bb - box;
-        if (!STC_IN_BOUNDS(b, n, p.status) ||
-            !STC_IN_BOUNDS(b + (NROW - 1) * sr + 2 * RY * p.bw + (D - 1) + 32 * (XT - 1), n, p.status))
-            return;
+        const bool bad = !STC_IN_BOUNDS(b, n, p.status) ||
+                         !STC_IN_BOUNDS(b + (NROW - 1) * sr + 2 * RY * p.bw + (D - 1) + 32 * (XT - 1), n, p.status);
+        if (__any_sync(0xffffffffu, bad)) return;
     }
 #endif
     // tile-local extents that hold real outputs (ragged last tiles)
@@ -789,15 +803,12 @@ __device__ __forceinline__ void compute_shape_vec(const P& p, const TileOrigin& 
                     // in [2^-90, 3e38] (the range where the FMA-corrected quotient is exact, checked on the
                     // host for this L) all lanes take that quotient after one vote, instead of a range
                     // test and a branch per output; otherwise every output takes the tested division.
-                    bool fast = p.fastdiv_f != 0;
+                    bool fast = true;
                     float qf[XV];
 #pragma unroll
                     for (int c = 0; c < XV; ++c) {
-                        const float a = acc[slot][c];
-                        fast = fast && fabsf(a) >= 0x1p-90f && fabsf(a) <= 3.0e38f;
-                        const float q0 = __fmul_rn(a, p.rcp_f);
-                        const float e = __fmaf_rn(-q0, p.Lf, a);
-                        qf[c] = __fmaf_rn(e, p.rcp_f, q0);
+                        fast = fast && fastdiv_in_range(acc[slot][c], p);
+                        qf[c] = fastdiv_quotient(acc[slot][c], p);
                     }
                     if (__all_sync(storing, fast)) {
 #pragma unroll
