@@ -206,7 +206,11 @@ STC_API int stc_map(const stc_grid* src, const stc_grid* dst, int32_t dst_padded
 
 /* nsteps of `A = mapstencil!(f, A)` on a SwitchingStencilArray whose two parents are a and b,
  * a holding the current source.  On return *out_src_is_b says which parent holds the result
- * (the reference's switch()).  Multi-step runs of registered shapes are temporally blocked. */
+ * (the reference's switch()).  Multi-step runs are temporally blocked where the library has a blocked
+ * kernel: Moore(1) cellular automata on packed words (rows of 32 cells or more), 2D Float32 radius-1
+ * Window / Moore / VonNeumann maps under Wrap or Remove (runs of 17 steps or more), 3D Float32
+ * VonNeumann / Cross radius-1 maps (8 steps or more; 16-bit state in the STC_KEEP_F32 mode); results
+ * are those of nsteps separate maps, bit for bit. */
 STC_API int stc_map_steps(const stc_grid* a, const stc_grid* b,
                   const stc_stencil* stencil, const stc_op* op, const stc_bc* bc,
                   int64_t nsteps, int32_t* out_src_is_b, void* stream, uint32_t flags);
