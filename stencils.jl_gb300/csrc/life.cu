@@ -261,16 +261,19 @@ __device__ __forceinline__ void life_warp_rows(const uint32_t* __restrict__ src,
     constexpr int W = 32 * WPL;
     const int lane = threadIdx.x & 31;
     const int lane_l = (lane + 31) & 31, lane_r = (lane + 1) & 31;
+    // lane 31 sends word W-1 to lane 0 as its ghost (rotated or shifted left by one), lane 0 sends word 0
+    // to lane 31 rotated or shifted right: a shift by 0 or 1 per lane, one instruction on each side
+    const uint32_t s_last = lane == 31 ? 1u : 0u, s_first = lane == 0 ? 1u : 0u;
     const uint32_t* ps = src + (ra - 1) * W + lane * WPL;   // row ra-1
     uint32_t* pd = dst + ra * W + lane * WPL;
     struct RowW { RowV v[WPL]; };
     auto load = [&](int q) -> RowW {
         uint32_t c[WPL];
         ld_words<WPL>(ps + q * W, c);
-        uint32_t left = __shfl_sync(0xffffffffu, c[WPL - 1], lane_l);
-        uint32_t right = __shfl_sync(0xffffffffu, c[0], lane_r);
-        if (lane == 0) left = ghost_left<WRAP>(left);      // word W-1 seen from word 0
-        if (lane == 31) right = ghost_right<WRAP>(right);  // word 0 seen from word W-1
+        const uint32_t to_r = WRAP ? __funnelshift_l(c[WPL - 1], c[WPL - 1], s_last) : c[WPL - 1] << s_last;
+        const uint32_t to_l = WRAP ? __funnelshift_r(c[0], c[0], s_first) : c[0] >> s_first;
+        const uint32_t left = __shfl_sync(0xffffffffu, to_r, lane_l);    // lane 0: word W-1 seen from word 0
+        const uint32_t right = __shfl_sync(0xffffffffu, to_l, lane_r);   // lane 31: word 0 seen from word W-1
         RowW r;
 #pragma unroll
         for (int i = 0; i < WPL; ++i) r.v[i] = row_v(i ? c[i - 1] : left, c[i], i < WPL - 1 ? c[i + 1] : right);
@@ -458,20 +461,8 @@ __device__ __forceinline__ void st_relaxed_gpu(uint64_t* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// the word of a tagged pair once its tag equals `tag`, starting from v, a value already read from p;
-// false after ~limit SM clocks
-__device__ __forceinline__ bool take_tagged(uint64_t v, const uint64_t* p, uint32_t tag, uint32_t* out,
-                                            long long limit = 4000000000ll) {
-    if ((uint32_t)(v >> 32) != tag) {
-        const long long t0 = clock64();
-        do {
-            if (clock64() - t0 > limit) return false;
-            v = ld_relaxed_gpu(p);
-        } while ((uint32_t)(v >> 32) != tag);
-    }
-    *out = (uint32_t)v;
-    return true;
-}
+// tag of a tagged pair
+__device__ __forceinline__ uint32_t tag_of(uint64_t v) { return (uint32_t)(v >> 32); }
 
 template <bool CONWAY, bool WRAP, int WT>
 __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1) life_coop_kernel(const LifeCoopParams p) {
@@ -517,27 +508,49 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
             const uint64_t* from_up = xs + ((size_t)up * 2 + 1) * slab;   // neighbour's last k rows
             const uint64_t* from_dn = xs + ((size_t)dn * 2 + 0) * slab;   // neighbour's first k rows
             bool ok = true;
-            // kB elements per thread at a time: all their first reads are in flight together, so a
-            // super-step's exchange costs about one L2 round trip when the neighbours are ready
+            // kB elements per thread at a time: all their first reads are in flight together, and the
+            // elements whose tag is not there yet are read again together (bounded), so a super-step's
+            // exchange costs about two L2 round trips when the neighbours publish at the same time
             constexpr int kB = 4;
+            const uint32_t want = (uint32_t)step;
             for (int i0 = threadIdx.x; i0 < slab; i0 += kB * blockDim.x) {
                 uint64_t vu[kB], vd[kB];
+                // a missing neighbour (Remove edge) reads as a zero word that already carries the tag
+                const uint64_t none = (uint64_t)want << 32;
 #pragma unroll
                 for (int j = 0; j < kB; ++j) {
                     const int i = i0 + j * (int)blockDim.x;
-                    vu[j] = (has_up && i < slab) ? ld_relaxed_gpu(from_up + i) : 0ull;
-                    vd[j] = (has_dn && i < slab) ? ld_relaxed_gpu(from_dn + i) : 0ull;
+                    vu[j] = (has_up && i < slab) ? ld_relaxed_gpu(from_up + i) : none;
+                    vd[j] = (has_dn && i < slab) ? ld_relaxed_gpu(from_dn + i) : none;
+                }
+                bool ready = true;
+#pragma unroll
+                for (int j = 0; j < kB; ++j) ready = ready && tag_of(vu[j]) == want && tag_of(vd[j]) == want;
+                if (!ready && ok) {   // after a timeout the remaining batches are not waited for
+                    const long long t0 = clock64();
+                    while (!ready) {
+                        if (clock64() - t0 > 4000000000ll) {
+                            ok = false;
+                            break;
+                        }
+#pragma unroll
+                        for (int j = 0; j < kB; ++j) {
+                            const int i = i0 + j * (int)blockDim.x;
+                            if (tag_of(vu[j]) != want) vu[j] = ld_relaxed_gpu(from_up + i);
+                            if (tag_of(vd[j]) != want) vd[j] = ld_relaxed_gpu(from_dn + i);
+                        }
+                        ready = true;
+#pragma unroll
+                        for (int j = 0; j < kB; ++j) ready = ready && tag_of(vu[j]) == want && tag_of(vd[j]) == want;
+                    }
                 }
 #pragma unroll
                 for (int j = 0; j < kB; ++j) {
                     const int i = i0 + j * (int)blockDim.x;
                     if (i < slab) {
-                        uint32_t u = 0u, d = 0u;
-                        if (has_up && ok) ok = take_tagged(vu[j], from_up + i, (uint32_t)step, &u);
-                        if (has_dn && ok) ok = take_tagged(vd[j], from_dn + i, (uint32_t)step, &d);
                         const int r = i / W, w = i - r * W;
-                        put_word<WRAP, WPL>(cur, P, W, r, w, u);
-                        put_word<WRAP, WPL>(cur, P, W, k + TB + r, w, d);
+                        put_word<WRAP, WPL>(cur, P, W, r, w, (uint32_t)vu[j]);
+                        put_word<WRAP, WPL>(cur, P, W, k + TB + r, w, (uint32_t)vd[j]);
                     }
                 }
             }
