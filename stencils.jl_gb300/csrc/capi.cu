@@ -100,6 +100,17 @@ int device_ctx(DeviceCtx** out) {
         if (e != cudaSuccess) return cuda_fail(e);
         c.status = d;
         c.status_host = h;
+        // The runs' stream-ordered scratch (packed Life grids and exchange slots, padded pairs, batch
+        // scratch) goes back to the device's default pool, which by default unmaps it at every
+        // synchronisation, so a synchronising caller paid for fresh pages on every call.  Keep up to 1 GiB
+        // mapped (a higher threshold set by the application stays).
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t cur = 0, keep = 1ull << 30;
+            if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur) == cudaSuccess && cur < keep)
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
         c.device = dev;
     }
     *out = &c;

@@ -768,6 +768,34 @@ static cudaError_t coop_dispatch(bool query, bool conway, bool wrap, const LifeC
                            : coop_dispatch_w<0>(query, conway, wrap, cp, grid, smem, s, num_sms, fits);
 }
 
+// The co-residency answer (and the shared-memory attribute it sets) per (device, instantiation, grid,
+// shared memory): asked once, not on every call.
+static cudaError_t coop_fits_cached(bool conway, bool wrap, int n0, int W, int G, size_t smem, cudaStream_t stream,
+                                    DeviceCtx* ctx, bool* fits) {
+    struct Entry { int dev; bool conway, wrap, split; int G, threads; size_t smem; bool fits; };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    const bool split = life_split_rows(n0, W);
+    const int threads = life_threads(W);
+    {
+        std::lock_guard<std::mutex> g(mu);
+        for (const Entry& c : cache)
+            if (c.dev == ctx->device && c.conway == conway && c.wrap == wrap && c.split == split && c.G == G &&
+                c.threads == threads && c.smem == smem) {
+                *fits = c.fits;
+                return cudaSuccess;
+            }
+    }
+    LifeCoopParams q{};
+    q.n0 = n0;
+    q.W = W;
+    cudaError_t e = coop_dispatch(true, conway, wrap, q, G, smem, stream, ctx->num_sms, fits);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    if (cache.size() < 256) cache.push_back(Entry{ctx->device, conway, wrap, split, G, threads, smem, *fits});
+    return cudaSuccess;
+}
+
 // The persistent path: every generation in one cooperative launch.  Returns STC_OK with *done = nsteps
 // when it ran, STC_OK with *done = 0 when the grid does not suit it (caller falls back).
 static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* op, bool halo, bool wrap, int64_t n0,
@@ -775,11 +803,14 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
                            int64_t* done) {
     *done = 0;
     if (!life_coop_enabled()) return STC_OK;
-    int coop = 0;
-    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop) {
+    static int coop_attr[64];   // per device: 0 unknown, 1 cooperative launch supported, 2 not
+    if (ctx->device >= 0 && ctx->device < 64 && coop_attr[ctx->device] == 0) {
+        int coop = 0;
+        const bool ok = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) == cudaSuccess && coop;
         cudaGetLastError();
-        return STC_OK;
+        coop_attr[ctx->device] = ok ? 1 : 2;
     }
+    if (ctx->device < 0 || ctx->device >= 64 || coop_attr[ctx->device] != 1) return STC_OK;
     const int W = life_words(n0);
     int k = (int)std::min<int64_t>(life_coop_depth(n1, ctx->num_sms), std::max<int64_t>(1, nsteps - 1));
     int G = (int)std::min<int64_t>(ctx->num_sms, n1 / k);
@@ -793,10 +824,7 @@ static int life_coop_steps(const stc_grid* a, const stc_grid* b, const stc_op* o
 
     const bool conway = op->birth_mask == (1u << 3) && op->survive_mask == ((1u << 2) | (1u << 3));
     bool fits = false;
-    LifeCoopParams q{};
-    q.n0 = (int)n0;
-    q.W = W;
-    cudaError_t e = coop_dispatch(true, conway, wrap, q, G, smem, stream, ctx->num_sms, &fits);
+    cudaError_t e = coop_fits_cached(conway, wrap, (int)n0, W, G, smem, stream, ctx, &fits);
     if (e != cudaSuccess) return cuda_fail(e);
     if (!fits) return STC_OK;   // not enough co-resident CTAs: the caller uses the multi-launch kernel
 
