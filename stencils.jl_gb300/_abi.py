@@ -36,13 +36,19 @@ NP_DTYPE = {F64: np.float64, F32: np.float32, BF16: np.uint16, F16: np.float16, 
             BOOL: np.uint8, I32: np.int32, I64: np.int64}
 
 
+_TORCH_CODES = None
+
+
 def torch_dtype_code(dt) -> int:
-    import torch
-    table = {torch.float64: F64, torch.float32: F32, torch.bfloat16: BF16, torch.float16: F16,
-             torch.uint8: U8, torch.bool: BOOL, torch.int32: I32, torch.int64: I64}
-    if dt not in table:
+    global _TORCH_CODES
+    if _TORCH_CODES is None:
+        import torch
+        _TORCH_CODES = {torch.float64: F64, torch.float32: F32, torch.bfloat16: BF16, torch.float16: F16,
+                        torch.uint8: U8, torch.bool: BOOL, torch.int32: I32, torch.int64: I64}
+    code = _TORCH_CODES.get(dt)
+    if code is None:
         raise TypeError(f"unsupported element type {dt}")
-    return table[dt]
+    return code
 
 
 def torch_dtype(code: int):
@@ -97,25 +103,34 @@ class JobDesc(C.Structure):
                 ("nsteps", C.c_int64)]
 
 
+_PAD_SIZE = ((), (1, 1), (1,), ())
+_PAD_STRIDE = ((), (0, 0), (0,), ())
+
+
 def make_grid(ndims, dtype, size, stride, ptr) -> Grid:
     g = Grid()
     g.ndims = ndims
     g.dtype = dtype
-    for d in range(3):
-        g.size[d] = int(size[d]) if d < ndims else 1
-        g.stride[d] = int(stride[d]) if d < ndims else 0
-    g.data = C.c_void_p(int(ptr))
+    g.size[:] = tuple(int(x) for x in size[:ndims]) + _PAD_SIZE[ndims]
+    g.stride[:] = tuple(int(x) for x in stride[:ndims]) + _PAD_STRIDE[ndims]
+    g.data = int(ptr)
     return g
 
 
 def grid_from_torch(t) -> Grid:
-    if t.dim() < 1 or t.dim() > 3:
+    nd = t.dim()
+    if nd < 1 or nd > 3:
         raise ValueError("grids have 1 to 3 dimensions")
-    if t.stride(0) != 1 and t.shape[0] > 1:
+    shape, strides = t.shape, t.stride()
+    if strides[0] != 1 and shape[0] > 1:
         raise ValueError("axis 0 must be contiguous (column-major, as a Julia Array)")
-    strides = list(t.stride())
-    strides[0] = 1
-    return make_grid(t.dim(), torch_dtype_code(t.dtype), t.shape, strides, t.data_ptr())
+    g = Grid()
+    g.ndims = nd
+    g.dtype = torch_dtype_code(t.dtype)
+    g.size[:] = tuple(shape) + _PAD_SIZE[nd]
+    g.stride[:] = (1,) + tuple(strides[1:]) + _PAD_STRIDE[nd]
+    g.data = t.data_ptr()
+    return g
 
 
 def grid_from_numpy(a: np.ndarray, code: int | None = None) -> Grid:
@@ -152,6 +167,24 @@ class LoweredStencil:
         d.weights = C.cast(self.weights, C.POINTER(C.c_double)) if self.weights is not None else None
         d.weight_dtype = wdt
         self.desc = d
+
+
+_KERNEL_CLS = None
+
+
+def lowered_stencil(stencil) -> LoweredStencil:
+    """LoweredStencil(stencil), lowered once and kept on the stencil object (a stencil's offsets never
+    change); a Kernel, whose weights the caller may still change, is lowered on every call."""
+    global _KERNEL_CLS
+    if _KERNEL_CLS is None:
+        from .stencil import Kernel
+        _KERNEL_CLS = Kernel
+    if isinstance(stencil, _KERNEL_CLS):
+        return LoweredStencil(stencil)
+    ls = stencil.__dict__.get("_stc_lowered")
+    if ls is None:
+        ls = stencil.__dict__["_stc_lowered"] = LoweredStencil(stencil)
+    return ls
 
 
 def lower_op(red) -> OpDesc:
@@ -218,4 +251,23 @@ def lower_bc(boundary, padding, grid_code: int | None = None) -> BcDesc:
             pv = int(pv)
         b.padval = float(pv)
         b.padval_int = int(pv) if float(pv).is_integer() else 0
+    return b
+
+
+_BC_CACHE: dict = {}
+
+
+def lower_bc_shared(boundary, padding, grid_code: int | None = None) -> BcDesc:
+    """lower_bc for the per-call paths, memoised on (boundary kind, padval and its type, padding, element
+    type).  The descriptor is shared: callers only pass it by reference to the library, never change it."""
+    pv = getattr(boundary, "padval", None)
+    key = (boundary.code, type(pv), pv, padding.code, grid_code)
+    try:
+        b = _BC_CACHE.get(key)
+    except TypeError:   # an unhashable padval
+        return lower_bc(boundary, padding, grid_code)
+    if b is None:
+        b = lower_bc(boundary, padding, grid_code)
+        if len(_BC_CACHE) < 1024:
+            _BC_CACHE[key] = b
     return b

@@ -17,12 +17,18 @@ from .boundary import Conditional, Halo, Remove, Use, Wrap, Reflect, BoundaryCon
 from .stencil import Stencil, Window
 
 
+_TENSOR = None
+
+
 def _is_torch(x) -> bool:
-    try:
-        import torch
-        return isinstance(x, torch.Tensor)
-    except ImportError:  # pragma: no cover
-        return False
+    global _TENSOR
+    if _TENSOR is None:
+        try:
+            import torch
+            _TENSOR = torch.Tensor
+        except ImportError:  # pragma: no cover
+            _TENSOR = ()
+    return isinstance(x, _TENSOR)
 
 
 def colmajor_empty(shape: Sequence[int], dtype, device="cuda"):

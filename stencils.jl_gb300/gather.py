@@ -75,13 +75,13 @@ def _flags(sync: bool, staged) -> int:
 
 def _run_map(red, dest, src: AbstractStencilArray, dst_padded: bool, sync: bool = True):
     lib = _lib.load()
-    st = A.LoweredStencil(src.stencil)
+    st = A.lowered_stencil(src.stencil)
     op = A.lower_op(red)
     halo = isinstance(src.padding, Halo)
     stage = _Staged(src.parent, dest, writeback=(0, 1) if halo else (1,))
     sp, dp = stage.dev
-    bc = A.lower_bc(src.boundary, src.padding if not isinstance(src, SwitchingStencilArray) else
-                    (Halo("in") if isinstance(src.padding, Halo) else src.padding), _code_of(src.parent))
+    bc = A.lower_bc_shared(src.boundary, src.padding if not isinstance(src, SwitchingStencilArray) else
+                           (Halo("in") if isinstance(src.padding, Halo) else src.padding), _code_of(src.parent))
     _require_device(sp)
     gs, gd = _grid(sp), _grid(dp)
     stream = _lib.current_stream_handle()
@@ -215,10 +215,10 @@ def _run_steps(red, S: SwitchingStencilArray, steps: int, sync: bool = True,
     if steps < 0:
         raise ValueError("steps must be >= 0")
     lib = _lib.load()
-    st = A.LoweredStencil(S.stencil)
+    st = A.lowered_stencil(S.stencil)
     op = A.lower_op(red)
     pad = Halo("in") if isinstance(S.padding, Halo) else Conditional()
-    bc = A.lower_bc(S.boundary, pad, _code_of(S.source))
+    bc = A.lower_bc_shared(S.boundary, pad, _code_of(S.source))
     stage = _Staged(S.source, S.dest, writeback=(0, 1))
     a, b = stage.dev
     _require_device(a)
