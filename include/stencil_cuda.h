@@ -275,7 +275,7 @@ STC_API int stc_scatter(const stc_grid* src, const stc_grid* dst, const stc_sten
  * the device grid may be a strided view, e.g. the interior of a Halo parent (as the reference's
  * StencilArray constructor copies an array into the padded parent, src/padding.jl:102-110, or a user
  * copies a result back with copyto!).  One pitched copy per call (per plane when the planes are not
- * stacked at one pitch); with STC_ASYNC the host buffer must stay valid until the stream reaches the
+ * stacked at one pitch; one linear copy when the rows are contiguous); with STC_ASYNC the host buffer must stay valid until the stream reaches the
  * copy (pinned host memory makes the copy asynchronous). */
 STC_API int stc_grid_upload(const stc_grid* dst, const void* host, void* stream, uint32_t flags);
 STC_API int stc_grid_download(void* host, const stc_grid* src, void* stream, uint32_t flags);

@@ -942,7 +942,8 @@ int stc_map_steps(const stc_grid* a, const stc_grid* b, const stc_stencil* st, c
 }
 
 // Host <-> device copies of a grid whose device side may be a strided view (the interior of a Halo
-// parent): one pitched copy (2D: cudaMemcpy2DAsync, 3D: cudaMemcpy3DAsync), no staging kernel.
+// parent): one pitched copy (cudaMemcpy2DAsync; one per plane when the planes are not stacked at one
+// pitch), or one linear copy when the rows are contiguous; no staging kernel.
 static int host_grid_copy(const stc_grid* g, void* host, bool upload, void* stream, uint32_t flags) {
     int rc = check_grid(g);
     if (rc) return rc;
@@ -963,6 +964,11 @@ static int host_grid_copy(const stc_grid* g, void* host, bool upload, void* stre
                                    : cudaMemcpy2DAsync(hp, w, dp, dpitch, w, h, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
             rc = cuda_fail(e);
         }
+    } else if (dpitch == w) {
+        // contiguous rows: one linear copy (less host work to issue than a pitched one)
+        cudaError_t e = upload ? cudaMemcpyAsync(g->data, host, w * h * d, cudaMemcpyHostToDevice, (cudaStream_t)stream)
+                               : cudaMemcpyAsync(host, g->data, w * h * d, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+        rc = cuda_fail(e);
     } else {
         cudaError_t e = upload
             ? cudaMemcpy2DAsync(g->data, dpitch, host, w, w, h * d, cudaMemcpyHostToDevice, (cudaStream_t)stream)
