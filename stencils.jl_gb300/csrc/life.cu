@@ -593,11 +593,28 @@ constexpr int kLifeWT = 128;
 // The warp-row split runs rows of exactly kLifeWT words with no spare bits; everything else the column split.
 static bool life_split_rows(int64_t n0, int W) { return W == kLifeWT && n0 == 32ll * W; }
 
+// A kernel's dynamic shared-memory limit only ever rises to the largest size a launch asked for, so a
+// launch never finds it lowered by a smaller one (another grid, another host thread).
+static cudaError_t ensure_smem_attr(const void* fn, size_t smem) {
+    static std::mutex mu;
+    static std::vector<std::pair<const void*, size_t>> set;
+    std::lock_guard<std::mutex> g(mu);
+    for (auto& f : set)
+        if (f.first == fn) {
+            if (f.second >= smem) return cudaSuccess;
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) f.second = smem;
+            return e;
+        }
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) set.emplace_back(fn, smem);
+    return e;
+}
+
 // launch one k-generation pass (both entry points use this)
 template <bool C, bool WR, int WT>
 static cudaError_t life_launch_t(const LifeParams& lp, int grid, size_t smem, cudaStream_t s) {
-    cudaError_t e = cudaFuncSetAttribute(life_block_kernel<C, WR, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = ensure_smem_attr((const void*)life_block_kernel<C, WR, WT>, smem);
     if (e != cudaSuccess) return e;
     life_block_kernel<C, WR, WT><<<grid, life_threads(lp.W), smem, s>>>(lp);
     return cudaGetLastError();
@@ -736,7 +753,7 @@ static bool life_coop_enabled() {
 template <bool C, bool WR, int WT>
 static cudaError_t coop_fits_t(int W, int grid, size_t smem, int num_sms, bool* fits) {
     auto fn = life_coop_kernel<C, WR, WT>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_smem_attr((const void*)fn, smem);
     if (e != cudaSuccess) return e;
     int nb = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, life_threads(W), smem);
@@ -746,6 +763,8 @@ static cudaError_t coop_fits_t(int W, int grid, size_t smem, int num_sms, bool* 
 
 template <bool C, bool WR, int WT>
 static cudaError_t coop_launch_t(const LifeCoopParams& cp, int grid, size_t smem, cudaStream_t s) {
+    cudaError_t e = ensure_smem_attr((const void*)life_coop_kernel<C, WR, WT>, smem);
+    if (e != cudaSuccess) return e;
     LifeCoopParams arg = cp;
     void* args[] = {&arg};
     return cudaLaunchCooperativeKernel((const void*)life_coop_kernel<C, WR, WT>, dim3(grid), dim3(life_threads(cp.W)), args,
