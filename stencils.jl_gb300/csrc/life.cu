@@ -253,36 +253,52 @@ __device__ __forceinline__ void st_words(uint32_t* p, const uint32_t (&c)[WPL]) 
 
 // Rows [ra, rb) of a band with W = 32 WPL words per row, computed by one warp: lane l holds words
 // l WPL .. l WPL + WPL - 1 of every row it reads.  Each source row is read once (one vector load per
-// lane), its two outer neighbour words arrive by shuffle, and it is reduced to its 3-cell sums as it
-// enters the rolling three-row window.
+// lane) into a rolling three-row window of raw words.  Per output row the three rows are summed first,
+// word by word (va + 2 vb = up + middle + down, two LOP3 per word); the 3x3 total of a word is then the
+// sum of its own and its two neighbour words' column sums, the words beyond the lane's run arriving by
+// shuffle (row ends: the sending lane shifts its sums by 0 or 1 bit, which is the ghost word's rotation
+// or shift applied to the sums).  So a row costs its load once, not the three horizontal sums of every
+// row a strip reads.
 template <bool CONWAY, bool WRAP, int WPL>
 __device__ __forceinline__ void life_warp_rows(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, int ra,
                                                int rb, uint32_t birth, uint32_t survive) {
     constexpr int W = 32 * WPL;
     const int lane = threadIdx.x & 31;
     const int lane_l = (lane + 31) & 31, lane_r = (lane + 1) & 31;
-    // lane 31 sends word W-1 to lane 0 as its ghost (rotated or shifted left by one), lane 0 sends word 0
-    // to lane 31 rotated or shifted right: a shift by 0 or 1 per lane, one instruction on each side
+    // lane 31 sends word W-1's sums to lane 0 as its ghost (rotated or shifted left by one), lane 0 sends
+    // word 0's to lane 31 rotated or shifted right: a shift by 0 or 1 per lane
     const uint32_t s_last = lane == 31 ? 1u : 0u, s_first = lane == 0 ? 1u : 0u;
+    auto to_r = [&](uint32_t x) { return WRAP ? __funnelshift_l(x, x, s_last) : x << s_last; };
+    auto to_l = [&](uint32_t x) { return WRAP ? __funnelshift_r(x, x, s_first) : x >> s_first; };
     const uint32_t* ps = src + (ra - 1) * W + lane * WPL;   // row ra-1
     uint32_t* pd = dst + ra * W + lane * WPL;
-    struct RowW { RowV v[WPL]; };
+    struct RowW { uint32_t c[WPL]; };
     auto load = [&](int q) -> RowW {
-        uint32_t c[WPL];
-        ld_words<WPL>(ps + q * W, c);
-        const uint32_t to_r = WRAP ? __funnelshift_l(c[WPL - 1], c[WPL - 1], s_last) : c[WPL - 1] << s_last;
-        const uint32_t to_l = WRAP ? __funnelshift_r(c[0], c[0], s_first) : c[0] >> s_first;
-        const uint32_t left = __shfl_sync(0xffffffffu, to_r, lane_l);    // lane 0: word W-1 seen from word 0
-        const uint32_t right = __shfl_sync(0xffffffffu, to_l, lane_r);   // lane 31: word 0 seen from word W-1
         RowW r;
-#pragma unroll
-        for (int i = 0; i < WPL; ++i) r.v[i] = row_v(i ? c[i - 1] : left, c[i], i < WPL - 1 ? c[i + 1] : right);
+        ld_words<WPL>(ps + q * W, r.c);
         return r;
     };
     auto emit = [&](int q, const RowW& u, const RowW& m, const RowW& d) {
+        uint32_t va[WPL], vb[WPL];
+#pragma unroll
+        for (int i = 0; i < WPL; ++i) {
+            va[i] = u.c[i] ^ m.c[i] ^ d.c[i];
+            vb[i] = (u.c[i] & m.c[i]) | (d.c[i] & (u.c[i] ^ m.c[i]));
+        }
+        const uint32_t la = __shfl_sync(0xffffffffu, to_r(va[WPL - 1]), lane_l);
+        const uint32_t lb = __shfl_sync(0xffffffffu, to_r(vb[WPL - 1]), lane_l);
+        const uint32_t ra_ = __shfl_sync(0xffffffffu, to_l(va[0]), lane_r);
+        const uint32_t rb_ = __shfl_sync(0xffffffffu, to_l(vb[0]), lane_r);
         uint32_t o[WPL];
 #pragma unroll
-        for (int i = 0; i < WPL; ++i) o[i] = next_state<CONWAY>(u.v[i], m.v[i], d.v[i], birth, survive);
+        for (int i = 0; i < WPL; ++i) {
+            // the column sums of the left word, this word and the right word, as the three "rows" of
+            // next_state (its fold is symmetric in the three)
+            const RowV L{i ? va[i - 1] : la, i ? vb[i - 1] : lb, 0u};
+            const RowV M{va[i], vb[i], m.c[i]};
+            const RowV R{i < WPL - 1 ? va[i + 1] : ra_, i < WPL - 1 ? vb[i + 1] : rb_, 0u};
+            o[i] = next_state<CONWAY>(L, M, R, birth, survive);
+        }
         st_words<WPL>(pd + q * W, o);
     };
     RowW v0 = load(0), v1 = load(1), v2;
