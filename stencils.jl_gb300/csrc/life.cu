@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
             // kB elements per thread at a time: all their first reads are in flight together, and the
             // elements whose tag is not there yet are read again together (bounded), so a super-step's
             // exchange costs about two L2 round trips when the neighbours publish at the same time
-            constexpr int kB = WPL > 0 ? 2 : 4;   // the warp-row split has 2 pairs per thread and direction
+            constexpr int kB = WPL > 0 ? 2 : 4;   // warp-row split at depth 8: 2 pairs per thread and direction
             const uint32_t want = (uint32_t)step;
             for (int i0 = threadIdx.x; i0 < slab; i0 += kB * blockDim.x) {
                 uint64_t vu[kB], vd[kB];
