@@ -343,6 +343,23 @@ template <bool CONWAY, bool WRAP, int WT, int WPL>
 __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
                                                int kk, int lo_lim, int hi_lim, uint32_t birth, uint32_t survive,
                                                const int2* bounds = nullptr, int* status = nullptr) {
+    if constexpr (WPL > 0) {
+        if (bounds && kk == 8) {
+            // a full super-step at the default depth: the eight generations unrolled, their strip bounds
+            // read together up front
+            int2 b[8];
+#pragma unroll
+            for (int g = 0; g < 8; ++g) b[g] = bounds[g];
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                const int ra = b[g].x, rb = b[g].y;
+                if (ra < rb && STC_IN_BOUNDS(ra - 1, rows, status) && STC_IN_BOUNDS(rb, rows, status))
+                    life_warp_rows<CONWAY, WRAP, WPL>((g & 1) ? oth : cur, (g & 1) ? cur : oth, ra, rb, birth, survive);
+                __syncthreads();
+            }
+            return cur;   // an even number of generations: the result is back in cur
+        }
+    }
 #pragma unroll 2
     for (int g = 0; g < kk; ++g) {
         int ra, rb;
