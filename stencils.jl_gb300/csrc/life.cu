@@ -336,13 +336,15 @@ __device__ __forceinline__ void life_strip_bounds(const LifeLane& L, int g, int 
     *rb = (L.s == L.strips - 1) ? hi : lo + (int)((float)(nr * (L.s + 1)) * L.inv_strips);
 }
 
-// Advance a band kk generations in the shared ping-pong pair (cur, oth), pitch life_pitch<WPL>(W).  Returns
-// the buffer holding the result.  Ends with a barrier.  `bounds` (optional): this strip's (ra, rb) for
-// generations 0 .. kk-1, computed once per run instead of every generation.
+// Advance a band through generations first .. kk-1 in the shared ping-pong pair (cur, oth), pitch
+// life_pitch<WPL>(W): generation g reads cur when g is even, oth when odd (so with first = 1 the caller
+// has already written generation 0 into oth).  Returns the buffer holding the result.  Ends with a
+// barrier when it runs a generation.  `bounds` (optional): this strip's (ra, rb) for generations
+// 0 .. kk-1, computed once per run instead of every generation.
 template <bool CONWAY, bool WRAP, int WT, int WPL>
 __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur, uint32_t* oth, int rows, int W,
                                                int kk, int lo_lim, int hi_lim, uint32_t birth, uint32_t survive,
-                                               const int2* bounds = nullptr, int* status = nullptr) {
+                                               const int2* bounds = nullptr, int* status = nullptr, int first = 0) {
     if constexpr (WPL > 0) {
         if (bounds && kk == 8) {
             // a full super-step at the default depth: the eight generations unrolled, their strip bounds
@@ -352,6 +354,7 @@ __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur,
             for (int g = 0; g < 8; ++g) b[g] = bounds[g];
 #pragma unroll
             for (int g = 0; g < 8; ++g) {
+                if (g < first) continue;
                 const int ra = b[g].x, rb = b[g].y;
                 if (ra < rb && STC_IN_BOUNDS(ra - 1, rows, status) && STC_IN_BOUNDS(rb, rows, status))
                     life_warp_rows<CONWAY, WRAP, WPL>((g & 1) ? oth : cur, (g & 1) ? cur : oth, ra, rb, birth, survive);
@@ -360,8 +363,13 @@ __device__ __forceinline__ uint32_t* life_gens(const LifeLane& L, uint32_t* cur,
             return cur;   // an even number of generations: the result is back in cur
         }
     }
+    if (first & 1) {
+        uint32_t* t = cur;
+        cur = oth;
+        oth = t;
+    }
 #pragma unroll 2
-    for (int g = 0; g < kk; ++g) {
+    for (int g = first; g < kk; ++g) {
         int ra, rb;
         if (bounds) {
             const int2 b = bounds[g];
@@ -520,7 +528,8 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
     const LifeLane lane = life_lane<WPL>(W, p.n0);
     // every super-step's generation g uses the same strip bounds: computed once, [strip][g]
     __shared__ int2 s_bounds[WPL > 0 ? 1024 : 1];
-    const bool tabled = WPL > 0 && lane.strips * k <= 1024;
+    __shared__ int4 s_split[WPL > 0 ? 32 : 1];
+    const bool tabled = WPL > 0 && lane.strips * k <= 1024 && lane.strips <= 32;
     if (tabled) {
         for (int i = threadIdx.x; i < lane.strips * k; i += blockDim.x) {
             LifeLane t = lane;
@@ -529,9 +538,33 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
             life_strip_bounds(t, i - t.s * k, rows, lo_lim, hi_lim, &ra, &rb);
             s_bounds[i] = make_int2(ra, rb);
         }
+        // generation 1 of a super-step split around the neighbour exchange: the rows whose three source
+        // rows all lie in the band (computed while the exchange's first reads are in flight), then the
+        // rows next to the ghost rows, the upper ones by the first half of the strips, the lower ones by
+        // the second half
+        if (threadIdx.x < lane.strips) {
+            const int sidx = threadIdx.x, S = lane.strips, H = S / 2;
+            const int lo0 = max(1, lo_lim), hi0 = min(rows - 1, hi_lim);
+            int ilo = max(k + 1, lo0), ihi = min(k + TB - 1, hi0);
+            if (ihi <= ilo) ilo = ihi = lo0;   // no inner rows: every row in the lower group
+            int4 v;
+            v.x = ilo + (ihi - ilo) * sidx / S;
+            v.y = ilo + (ihi - ilo) * (sidx + 1) / S;
+            if (sidx < H) {
+                v.z = lo0 + (ilo - lo0) * sidx / H;
+                v.w = lo0 + (ilo - lo0) * (sidx + 1) / H;
+            } else {
+                v.z = ihi + (hi0 - ihi) * (sidx - H) / (S - H);
+                v.w = ihi + (hi0 - ihi) * (sidx - H + 1) / (S - H);
+            }
+            s_split[sidx] = v;
+        }
         __syncthreads();
     }
     const int2* my_bounds = tabled ? s_bounds + lane.s * k : nullptr;
+    // exchange reads that fit one batch per thread can overlap generation 1's inner rows
+    constexpr int kB = WPL > 0 ? 2 : 4;   // pairs per thread and direction in flight (warp-row split at depth 8: 2)
+    const bool split = tabled && lane.strips >= 2 && slab <= kB * (int)blockDim.x;
     int64_t gen = 0;
     for (int step = 0;; ++step) {
         const bool final = gen >= nmain;
@@ -545,18 +578,18 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
             // kB elements per thread at a time: all their first reads are in flight together, and the
             // elements whose tag is not there yet are read again together (bounded), so a super-step's
             // exchange costs about two L2 round trips when the neighbours publish at the same time
-            constexpr int kB = WPL > 0 ? 2 : 4;   // warp-row split at depth 8: 2 pairs per thread and direction
             const uint32_t want = (uint32_t)step;
-            for (int i0 = threadIdx.x; i0 < slab; i0 += kB * blockDim.x) {
-                uint64_t vu[kB], vd[kB];
-                // a missing neighbour (Remove edge) reads as a zero word that already carries the tag
-                const uint64_t none = (uint64_t)want << 32;
+            // a missing neighbour (Remove edge) reads as a zero word that already carries the tag
+            const uint64_t none = (uint64_t)want << 32;
+            auto first_reads = [&](int i0, uint64_t (&vu)[kB], uint64_t (&vd)[kB]) {
 #pragma unroll
                 for (int j = 0; j < kB; ++j) {
                     const int i = i0 + j * (int)blockDim.x;
                     vu[j] = (has_up && i < slab) ? ld_relaxed_gpu(from_up + i) : none;
                     vd[j] = (has_dn && i < slab) ? ld_relaxed_gpu(from_dn + i) : none;
                 }
+            };
+            auto take = [&](int i0, uint64_t (&vu)[kB], uint64_t (&vd)[kB]) {
                 bool ready = true;
 #pragma unroll
                 for (int j = 0; j < kB; ++j) ready = ready && tag_of(vu[j]) == want && tag_of(vd[j]) == want;
@@ -587,6 +620,23 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
                         put_word<WRAP, WPL>(cur, P, W, k + TB + r, w, (uint32_t)vd[j]);
                     }
                 }
+            };
+            if (split) {
+                uint64_t vu[kB], vd[kB];
+                first_reads((int)threadIdx.x, vu, vd);
+                if constexpr (WPL > 0) {
+                    // generation 1's inner rows read band rows only, which the exchange does not write
+                    const int4 sp = s_split[lane.s];
+                    if (sp.x < sp.y && STC_IN_BOUNDS(sp.x - 1, rows, p.status) && STC_IN_BOUNDS(sp.y, rows, p.status))
+                        life_warp_rows<CONWAY, WRAP, WPL>(cur, oth, sp.x, sp.y, p.birth, p.survive);
+                }
+                take((int)threadIdx.x, vu, vd);
+            } else {
+                for (int i0 = threadIdx.x; i0 < slab; i0 += kB * blockDim.x) {
+                    uint64_t vu[kB], vd[kB];
+                    first_reads(i0, vu, vd);
+                    take(i0, vu, vd);
+                }
             }
             if (!__syncthreads_and(ok)) {
                 if (threadIdx.x == 0 && p.status) atomicOr(p.status, DEV_ERR_TIMEOUT);
@@ -601,8 +651,19 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
                 }
             }
         }
+        int first = 0;
+        if constexpr (WPL > 0) {
+            if (split && step > 0) {
+                // generation 1's rows next to the ghost rows, now that those are in place
+                const int4 sp = s_split[lane.s];
+                if (sp.z < sp.w && STC_IN_BOUNDS(sp.z - 1, rows, p.status) && STC_IN_BOUNDS(sp.w, rows, p.status))
+                    life_warp_rows<CONWAY, WRAP, WPL>(cur, oth, sp.z, sp.w, p.birth, p.survive);
+                __syncthreads();
+                first = 1;
+            }
+        }
         cur = life_gens<CONWAY, WRAP, WT, WPL>(lane, cur, oth, rows, W, kk, lo_lim, hi_lim, p.birth, p.survive,
-                                               my_bounds, p.status);
+                                               my_bounds, p.status, first);
         oth = (cur == lsm) ? buf1 : lsm;
         gen += kk;
         if (final) {
