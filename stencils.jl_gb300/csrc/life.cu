@@ -776,6 +776,57 @@ __global__ void life_unpack_kernel(const PackParams p) {
     }
 }
 
+// Byte grids (UInt8, Bool) whose rows are whole packed words (n0 = 32 W, W a multiple of 32) on 16-byte
+// aligned rows: one warp packs 32 words of a row at a time.  Lane j reads cells j W + 32 c .. j W + 32 c + 31
+// (one 32-byte sector, two 16-byte loads); byte b of lane j is bit j of word 32 c + b, so one ballot per byte
+// forms a whole word, and the 32 words leave as one 128-byte store.  Unpacking is the mirror image: every
+// lane reads the same 32 words and writes its 32 cells as one sector.  (The one-thread-per-word kernels
+// above need 32 one-byte accesses per word.)
+__global__ void life_pack_bytes_kernel(const PackParams p) {
+    const uint8_t* base = (const uint8_t*)p.base;
+    const int lane = threadIdx.x & 31;
+    const int G = p.W / 32;
+    const int64_t units = (int64_t)p.n1 * G;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units; u += nw) {
+        const int y = (int)(u / G), c = (int)(u - (int64_t)y * G);
+        const uint4* src = (const uint4*)(base + p.org + (int64_t)y * p.sy + (int64_t)lane * p.W + 32 * c);
+        const uint4 v0 = src[0], v1 = src[1];
+        const uint32_t q[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+        uint32_t mine = 0;
+#pragma unroll
+        for (int b = 0; b < 32; ++b) {
+            const uint32_t word = __ballot_sync(0xffffffffu, ((q[b >> 2] >> (8 * (b & 3))) & 0xffu) != 0u);
+            if (lane == b) mine = word;
+        }
+        p.P[(int64_t)y * p.W + 32 * c + lane] = mine;
+    }
+}
+
+__global__ void life_unpack_bytes_kernel(const PackParams p) {
+    uint8_t* base = (uint8_t*)p.base;
+    const int lane = threadIdx.x & 31;
+    const int G = p.W / 32;
+    const int64_t units = (int64_t)p.n1 * G;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; u < units; u += nw) {
+        const int y = (int)(u / G), c = (int)(u - (int64_t)y * G);
+        // each lane takes its bit of the 32 words: one word per lane, then shuffled round
+        const uint32_t word = p.P[(int64_t)y * p.W + 32 * c + lane];
+        uint32_t o[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            o[i] = 0;
+#pragma unroll
+            for (int bb = 0; bb < 4; ++bb)
+                o[i] |= ((__shfl_sync(0xffffffffu, word, 4 * i + bb) >> lane) & 1u) << (8 * bb);
+        }
+        uint4* dst = (uint4*)(base + p.org + (int64_t)y * p.sy + (int64_t)lane * p.W + 32 * c);
+        dst[0] = make_uint4(o[0], o[1], o[2], o[3]);
+        dst[1] = make_uint4(o[4], o[5], o[6], o[7]);
+    }
+}
+
 static int launch_pack(bool pack, const stc_grid* g, int64_t org, int64_t n0, int W, int n1, uint32_t* P,
                        cudaStream_t s, int num_sms) {
     PackParams p{};
@@ -787,6 +838,17 @@ static int launch_pack(bool pack, const stc_grid* g, int64_t org, int64_t n0, in
     p.W = W;
     p.n1 = n1;
     p.P = P;
+    const bool bytes_fast = (g->dtype == STC_U8 || g->dtype == STC_BOOL) && n0 == 32ll * W && W % 32 == 0 &&
+                            ((uintptr_t)((const uint8_t*)g->data + org) % 16) == 0 && g->stride[1] % 16 == 0;
+    if (bytes_fast) {
+        const int64_t warps = (int64_t)n1 * (W / 32);
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)num_sms * 16));
+        void* prof = prof_begin(s);
+        if (pack) life_pack_bytes_kernel<<<blocks, 256, 0, s>>>(p);
+        else life_unpack_bytes_kernel<<<blocks, 256, 0, s>>>(p);
+        prof_end(prof, s, pack ? "life_pack" : "life_unpack", (double)W * 32 * n1 * 1.125, (double)W * 32 * n1);
+        return cuda_fail(cudaGetLastError());
+    }
     const int64_t groups = (int64_t)n1 * ((W + 31) / 32);
     int blocks = (int)std::min<int64_t>((groups * 32 + 255) / 256, (int64_t)num_sms * 8);
     blocks = std::max(blocks, 1);
