@@ -8,19 +8,22 @@
 // bit of words w-1 and w+1 — no shifts — except across the row's two ends: the left neighbour word of
 // word 0 is word W-1 rotated left by one bit (cell jW - 1 is bit j-1 of word W-1; cell -1 is cell
 // n0-1 under Wrap), and the right neighbour word of word W-1 is word 0 rotated right by one.  Under
-// Remove(0) the rotations become shifts that bring in a dead cell.  In shared memory each row is kept
-// with those two derived words around it, [left ghost | words 0 .. W-1 | right ghost] (pitch W + 2),
-// written by the two threads that produce words W-1 and 0, so every thread reads its three neighbour
-// words at fixed offsets.
+// Remove(0) the rotations become shifts that bring in a dead cell.  Two ways to split a band among
+// threads: one packed column per thread (any width), with each row kept in shared memory between its two
+// derived words, [left ghost | words 0 .. W-1 | right ghost] (pitch W + 2), written by the two threads
+// that produce words W-1 and 0, so every thread reads its three neighbour words at fixed offsets; or,
+// for rows of 128 words, one warp per row strip with four consecutive words per lane, rows stored bare,
+// the words beyond a lane's run arriving by shuffle and the row ends' ghosts made on the sending lane.
 //
 // A launch advances every row band by up to k generations: each CTA holds full rows for its band plus
 // k halo rows above and below (y-wrap, zero rows, or the neighbouring bands' rows), steps them k times
 // in a shared ping-pong pair — the valid band shrinks by one row per generation — and writes the band
-// back.  Per word, each row's 3-cell sum (2 bit planes) is formed once as the row enters a rolling
-// three-row window; a carry-save adder adds the three rows' sums into the 3x3 total t, and the rule
-// is evaluated bitwise on it (neighbours = t - centre).  The neighbour count is the count of nonzero
-// neighbours, exactly what the LIFE op counts, so the result is bit-identical to the per-cell gather
-// for any input values.
+// back.  The 3x3 total t of every cell (2 bit planes per 3-cell sum, added by a carry-save adder) is
+// formed bitwise: the column split sums each row's three words once as the row enters a rolling
+// three-row window and then adds three rows; the warp-row split sums each word's three rows first and
+// then adds three words.  The rule is evaluated bitwise on t (neighbours = t - centre).  The neighbour
+// count is the count of nonzero neighbours, exactly what the LIFE op counts, so the result is
+// bit-identical to the per-cell gather for any input values.
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
