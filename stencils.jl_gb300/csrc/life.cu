@@ -479,9 +479,11 @@ __global__ void __launch_bounds__(life_wpl<WT>() > 0 ? 512 : kLifeMaxThreads, 1)
 // shared memory for the whole run, with k ghost rows above and below.  A super-step advances the band
 // kk <= k generations; then the CTA publishes its first and last k band rows to an exchange slot in
 // global memory, each word as a 64-bit (super-step tag, word) pair written with a single relaxed
-// gpu-scope store.  Before the next super-step every thread reloads its share of the neighbours'
-// rows until each pair carries the expected tag (bounded) and copies the words in as ghost rows.  No
-// fence or flag sits on the critical path: a pair is atomic, so a matching tag means the word is the
+// gpu-scope store.  At the next super-step every thread issues the first reads of its share of the
+// neighbours' rows, computes its strip of the next generation's rows that need no ghost row (warp-row
+// split) while they are in flight, reads again until each pair carries the expected tag (bounded),
+// and copies the words in as ghost rows; the rows next to the ghost rows follow.  No fence or flag
+// sits on the critical path: a pair is atomic, so a matching tag means the word is the
 // one published for that super-step.  Two slots alternate: a neighbour overwrites a slot only after
 // it has read this CTA's following publication, which this CTA makes after reading that slot.
 // Every CTA must be resident at once (cooperative launch), and each band holds at least k rows, so
