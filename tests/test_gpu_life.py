@@ -135,6 +135,25 @@ def test_life_persistent_depths(cuda, st, orc, abi, monkeypatch, depth, bname):
             assert np.array_equal(_logical(S2.dest, st.Conditional(), st), prev), (depth, steps)
 
 
+@pytest.mark.parametrize("depth", ["1", "2", "5", "8", "13"])
+@pytest.mark.parametrize("bname", ["wrap", "remove0"])
+def test_life_warp_rows_persistent_depths(cuda, st, orc, abi, monkeypatch, depth, bname):
+    """Rows of 4096 cells (the warp-row split, whose first generation per super-step is split around the
+    neighbour exchange) over 300 rows: bands of 2 to 13 rows, so some have no row that needs no ghost row
+    (depths 1 and 2) and Remove clips the first and last bands; both states bit-exact against the oracle."""
+    monkeypatch.setenv("STC_LIFE_K", depth)
+    rng = np.random.default_rng(97 + len(depth) + len(bname))
+    a = np.asfortranarray((rng.random((4096, 300)) < 0.33).astype(np.uint8))
+    bnd = st.Wrap() if bname == "wrap" else st.Remove(0)
+    for steps in (1, 2, 29):
+        S2, kern = _gpu_run(st, st.to_device(a), st.life, bnd, st.Conditional(), steps)
+        assert "life_coop" in kern, kern
+        res, prev, _ = _oracle_steps(orc, abi, st, a, abi.U8, st.life, bnd, st.Conditional(), steps)
+        assert np.array_equal(_logical(S2.source, st.Conditional(), st), res), (depth, steps)
+        if steps > 1:
+            assert np.array_equal(_logical(S2.dest, st.Conditional(), st), prev), (depth, steps)
+
+
 def test_queued_calls_equal_waiting_calls(cuda, st):
     """mapstencil_(..., sync=False) only skips the wait: three queued 100-generation calls give the state
     one waiting 300-generation call gives."""
