@@ -4,7 +4,11 @@
  *
  * Every entry point takes plain pointers and sizes.  Grids are column-major (axis 0 is the
  * contiguous one, exactly as a Julia `Array`), live in caller-owned device memory, and are
- * described by `stc_grid`.  The library never frees caller memory.  Calls are ordered on the
+ * described by `stc_grid`.  The library never frees caller memory.  Its own scratch (packed Life
+ * grids, padded pairs, batch tables) is stream-ordered memory from the device's default pool, whose
+ * release threshold the library raises to 1 GiB on first use (a higher threshold the application set
+ * stays), so scratch pages stay mapped across synchronisations; applications that share that pool
+ * see it keep up to 1 GiB of freed memory.  Calls are ordered on the
  * CUDA stream passed as `void* stream` (a `cudaStream_t`; NULL is the legacy default stream).
  * Every call returns STC_OK (0) or a negative `stc_status`; `stc_strerror` names it.  The
  * statuses mirror the `ArgumentError`s the reference raises, so a Julia shim can rethrow them.
