@@ -181,9 +181,14 @@ def lowered_stencil(stencil) -> LoweredStencil:
         _KERNEL_CLS = Kernel
     if isinstance(stencil, _KERNEL_CLS):
         return LoweredStencil(stencil)
-    ls = stencil.__dict__.get("_stc_lowered")
-    if ls is None:
-        ls = stencil.__dict__["_stc_lowered"] = LoweredStencil(stencil)
+    # the lowering is reused only for the same radius, shape, rank and offsets object (a copy with another
+    # radius, as an enclosing Layered stencil makes, is lowered afresh)
+    key = (stencil.radius, getattr(stencil, "shape_id", None), stencil.ndims, id(getattr(stencil, "_offsets", None)))
+    hit = stencil.__dict__.get("_stc_lowered")
+    if hit is not None and hit[0] == key:
+        return hit[1]
+    ls = LoweredStencil(stencil)
+    stencil.__dict__["_stc_lowered"] = (key, ls)
     return ls
 
 

@@ -418,6 +418,7 @@ def with_radius(stencil: Stencil, R: int) -> Stencil:
     """The same offsets (and weights) with the halo radius R of an enclosing Layered stencil."""
     import copy
     s = copy.copy(stencil)
+    s.__dict__.pop("_stc_lowered", None)   # the original's lowering (radius, shape) does not apply
     s.radius = int(R)
     s.shape_id = SHAPE_TABLE
     return s

@@ -112,3 +112,22 @@ def test_halo_out_parents_align_interior_rows(st):
     p = pad_array(st.Halo("out"), st.Moore(2), a)
     assert tuple(p.shape) == (11, 9)
     assert np.array_equal(p[2:-2, 2:-2].numpy(), a.numpy()) and float(p.sum()) == float(a.sum())
+
+
+def test_lowered_stencil_cache_follows_radius_and_shape(st):
+    """The per-stencil lowering is reused for the same stencil and redone for a copy with another radius
+    (an enclosing Layered stencil's), so the descriptor always carries the stencil's own radius and shape."""
+    from stencils_gb300 import _abi as A
+    from stencils_gb300.stencil import with_radius
+    s = st.Window(1)
+    a = A.lowered_stencil(s)
+    assert A.lowered_stencil(s) is a
+    assert (a.desc.radius, a.desc.shape) == (1, s.shape_id)
+    w = with_radius(s, 3)
+    b = A.lowered_stencil(w)
+    assert b is not a and (b.desc.radius, b.desc.shape) == (3, w.shape_id)
+    assert A.lowered_stencil(s).desc.radius == 1
+    w.radius = 2   # changed in place: lowered again
+    assert A.lowered_stencil(w).desc.radius == 2
+    k = st.Kernel(st.Window(1), list(range(9)))
+    assert A.lowered_stencil(k) is not A.lowered_stencil(k)   # kernels: weights may change, never reused
